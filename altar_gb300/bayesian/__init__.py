@@ -1,0 +1,11 @@
+"""CATMIP engine (altar/altar/bayesian): controller, sampler, scheduler, solvers."""
+from .coolingstep import CoolingStep, StageState
+from .notifier import Notifier, Profiler
+from .metropolis import Metropolis
+from .grid import Grid
+from .cov import COV
+from .annealing import CUDAAnnealing
+from .annealer import Annealer
+
+__all__ = ["CoolingStep", "StageState", "Notifier", "Profiler", "Metropolis", "Grid", "COV",
+           "CUDAAnnealing", "Annealer"]

@@ -1,0 +1,109 @@
+"""Single-GPU annealing method (altar/altar/bayesian/CUDAAnnealing.py,
+AnnealingMethod.py:55-147).
+
+Each phase of a stage (cool, walk, resample) is a fixed sequence of C-ABI
+launches whose stage-dependent inputs (β, scaling, Σ, the random-stream
+epoch) live on the device.  After one eager stage has allocated every
+buffer, each phase is captured once into a CUDA graph and replayed for all
+later stages; the host only reads β (and the stage report) once per stage.
+"""
+import ctypes
+import logging
+
+import torch
+
+from .. import _native
+from ..device import stream_handle
+from .coolingstep import CoolingStep
+
+log = logging.getLogger("altar_gb300")
+
+
+class CUDAAnnealing:
+    def __init__(self, annealer, graphs=True):
+        self.annealer = annealer
+        self.graphs = bool(graphs)
+        self.step = None
+        self.iteration = 0
+        self.stream = None
+        self._graphs = {}
+        self._eager_done = set()
+        self.reports = []
+
+    def initialize(self, application):
+        self.stream = torch.cuda.Stream()
+        return self
+
+    @property
+    def beta(self):
+        return self.step.beta
+
+    def start(self, annealer):
+        self.iteration = 0
+        self.step = CoolingStep.start(annealer)
+        annealer.sampler.prime(self.step)
+        return self
+
+    def top(self, annealer):
+        annealer.model.top(step=self.step)
+        return self
+
+    def _phase(self, name, fn):
+        """Run fn eagerly the first time (allocating its buffers), as a captured graph afterwards."""
+        if not self.graphs or name not in self._eager_done:
+            self._eager_done.add(name)
+            return fn()
+        ex = self._graphs.get(name)
+        if ex is None:
+            s = stream_handle()
+            _native.call("ag_graph_begin", s)
+            try:
+                fn()
+            except Exception:
+                dummy = ctypes.c_void_p()
+                _native.load().ag_graph_end(s, ctypes.byref(dummy))
+                raise
+            handle = ctypes.c_void_p()
+            _native.call("ag_graph_end", s, ctypes.byref(handle))
+            ex = self._graphs[name] = handle
+        _native.call("ag_graph_launch", ex, stream_handle())
+        return None
+
+    def cool(self, annealer):
+        self._phase("cool", lambda: annealer.scheduler.update(step=self.step))
+        self.iteration += 1
+        return self
+
+    def walk(self, annealer):
+        self._phase("walk", lambda: annealer.sampler.samplePosterior(annealer=annealer, step=self.step))
+        return self.step.state.counters
+
+    def resample(self, annealer, statistics):
+        # report of the stage before the counters are cleared
+        st = self.step.state
+        self._last = (st.scalars.clone(), st.counters.clone(), st.flags.clone())
+        self._phase("resample", lambda: annealer.sampler.resample(annealer=annealer, statistics=statistics))
+        return self
+
+    def bottom(self, annealer):
+        scal, cnt, flags = (t.cpu() for t in self._last)
+        acc, rej, unl = (int(v) for v in cnt)
+        rep = {"stage": self.iteration, "beta": float(scal[0]), "dbeta": float(scal[1]),
+               "cov": float(scal[2]), "scaling": float(self.step.state.scaling.item()),
+               "accepted": acc, "rejected": rej, "unlikely": unl, "flags": int(flags[0])}
+        self.reports.append(rep)
+        if rep["flags"] & _native.AG_DEV_ERR_TIMEOUT:
+            raise RuntimeError("a device wait timed out during the stage")
+        if rep["flags"] & _native.AG_DEV_ERR_NOT_SPD:
+            log.warning("stage %d: scaled Σ not positive definite; diagonal proposal used", self.iteration)
+        log.info("stage %(stage)d beta %(beta).6g cov %(cov).4g accepted %(accepted)d", rep)
+        annealer.model.bottom(step=self.step)
+        return self
+
+    def finish(self, annealer):
+        if annealer.archiver is not None:
+            annealer.archiver.record(step=self.step)
+        for ex in self._graphs.values():
+            _native.load().ag_graph_destroy(ex)
+        self._graphs.clear()
+        return self

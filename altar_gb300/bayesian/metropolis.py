@@ -1,0 +1,89 @@
+"""Metropolis sampler (altar/altar/bayesian/Metropolis.py:21-291).
+
+Same configuration (scaling .1, acceptanceWeight 8, rejectionWeight 1) and
+the same per-step semantics: propose θ' = θ + (L z)ᵀ with L = chol(scaling² Σ),
+reject samples outside the model's support (and, for the CDM, above the free
+surface), evaluate the likelihoods of every candidate, accept where
+log u <= post' - post.  Each step is three launches: propose (+verify +prior),
+the fused forward model, accept.
+"""
+import torch
+
+from .. import _native
+from ..device import DEVICE, ptr, stream_handle
+
+
+class Metropolis:
+    def __init__(self, scaling=0.1, acceptanceWeight=8.0, rejectionWeight=1.0):
+        self.scaling = float(scaling)
+        self.acceptanceWeight = float(acceptanceWeight)
+        self.rejectionWeight = float(rejectionWeight)
+        self.steps = 1
+        self.seed = 0
+        self._buf = None
+
+    def initialize(self, application):
+        self.steps = application.job.steps
+        self.seed = application.rng.seed
+        return self
+
+    def _buffers(self, n, p):
+        if self._buf is None or self._buf[0].shape != (n, p):
+            f64 = dict(dtype=torch.float64, device=DEVICE)
+            self._buf = (torch.zeros(n, p, **f64), torch.zeros(n, **f64), torch.zeros(n, **f64),
+                         torch.zeros(n, dtype=torch.int32, device=DEVICE))
+        return self._buf
+
+    def prime(self, step):
+        """Set the initial proposal scaling on the device."""
+        step.state.scaling.fill_(self.scaling)
+        return self
+
+    def samplePosterior(self, annealer, step):
+        d = annealer.dispatcher
+        d.notify(event=d.samplePosteriorStart, controller=annealer)
+        self.prepareSamplingPDF(annealer=annealer, step=step)
+        stats = self.walkChains(annealer=annealer, step=step)
+        d.notify(event=d.samplePosteriorFinish, controller=annealer)
+        return stats
+
+    def resample(self, annealer, statistics):
+        """Adapt the proposal scaling from the acceptance counters (device)."""
+        self.adjustCovarianceScaling(annealer.worker.step)
+        return
+
+    def prepareSamplingPDF(self, annealer, step):
+        d = annealer.dispatcher
+        d.notify(event=d.prepareSamplingPDFStart, controller=annealer)
+        _native.call("ag_cholesky_scaled", step.state.struct, step.parameters, stream_handle())
+        d.notify(event=d.prepareSamplingPDFFinish, controller=annealer)
+
+    def walkChains(self, annealer, step):
+        model = annealer.model
+        d = annealer.dispatcher
+        n, p = step.samples, step.parameters
+        cand, cprior, cdata, mask = self._buffers(n, p)
+        st = step.state.struct
+        s = stream_handle()
+        for k in range(self.steps):
+            d.notify(event=d.chainAdvanceStart, controller=annealer)
+            d.notify(event=d.verifyStart, controller=annealer)
+            _native.call("ag_propose", st, ptr(step.theta), n, p, ptr(model.lo), ptr(model.hi),
+                         self.seed, k, ptr(cand), ptr(mask), ptr(cprior), s)
+            d.notify(event=d.verifyFinish, controller=annealer)
+            d.notify(event=d.dataStart, controller=annealer)
+            model.strategy.forward(cand, cdata, mask=mask, status=mask)
+            d.notify(event=d.dataFinish, controller=annealer)
+            d.notify(event=d.acceptStart, controller=annealer)
+            _native.call("ag_accept", st, n, p, self.seed, k, ptr(mask), ptr(cand), ptr(cprior),
+                         ptr(cdata), ptr(step.theta), ptr(step.prior), ptr(step.data),
+                         ptr(step.posterior), s)
+            d.notify(event=d.acceptFinish, controller=annealer)
+            d.notify(event=d.chainAdvanceFinish, controller=annealer)
+        # accepted, rejected, unlikely stay on the device until the stage report
+        return step.state.counters
+
+    def adjustCovarianceScaling(self, step):
+        _native.call("ag_adapt_scaling", step.state.struct, self.acceptanceWeight,
+                     self.rejectionWeight, stream_handle())
+        return self

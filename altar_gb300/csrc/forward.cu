@@ -1,0 +1,643 @@
+// Fused batched forward models + diagonal-Cd misfit + per-chain log-likelihood.
+//
+// CDM (Compound Dislocation Model, Nikkhoo et al. 2016), following the
+// reference numpy CDM models/cdm/cdm/libcdm.py:39-430, and the Mogi point
+// source, following models/mogi/lib/libmogi/Source.cc:65-154.
+//
+// CDM evaluation strategy.  The reference sums, over the 12 sides of three
+// rectangles, the difference v(B) - v(A) of two angular dislocations
+// (libcdm.py:310-372).  Evaluated in FP32 as written, that difference loses
+// up to ~4 digits: each term is O(1) while the side's contribution is
+// O(side length / distance).  Here every quantity of the angular-dislocation
+// formula is carried as a pair (value at A, difference B - A), with the
+// difference propagated by exact identities (product rule
+// Δ(uv) = Δu·v_B + u_A·Δv, Δ(1/u) = -Δu/(u_A u_B),
+// Δr = Δ(r²)/(r_A + r_B), Δlog u = log1p(Δu/u_A), and the Burgers-function
+// difference as a single atan2 of the rotation from A to B), so the
+// cancellation never happens in floating point.
+//
+// Work decomposition: one warp per chain, lanes over stations; a CTA holds
+// WARPS chains whose per-side constants (precomputed in FP64 by
+// cdm_setup_kernel) live in shared memory and are read with broadcast
+// vector loads; station tiles are staged into shared memory by 1-D bulk
+// copies (cp.async.bulk + mbarrier), double buffered, and shared by the
+// CTA's warps.  Each lane accumulates w·r² in float-float; the warp's sum is
+// reduced in FP64 in a fixed order.
+#include <math.h>
+#include <stdint.h>
+
+#include "common.cuh"
+#include "internal.h"
+
+namespace ag {
+
+constexpr int kMaxOffsets = 16;      // datasets with their own offset parameter
+constexpr int kSides = 12;
+constexpr int kTile = AG_STATION_TILE;
+constexpr uint32_t kWaitLimit = 1u << 24;
+
+// ---------------------------------------------------------------------------
+// per-side constants of one angular-dislocation pair (36 floats)
+struct __align__(16) SideC {
+    float4 q[9];
+};
+// q0: c, s, k1, k2          frame (unit horizontal side direction) and vertex A
+// q1: dy1, aA, aB, da       y1(B) - y1(A); depths of A and B; aB - aA
+// q2: sb, cb, tb2, ctb2     sin β, cos β, tan(β/2), cot(β/2) (configuration II)
+// q3: daS, C1F, C2F, C3F    da·(aA+aB); coefficients of ΔFi
+// q4: C1P, C2P, kc1, kc2    coefficients of Δlog(r+a); k·cot·b1, k·cot·b2
+// q5: nb1, nb2, hb1, hb2    2ν b1, 2ν b2, k b1/2, k b2/2
+// q6: b1, b2, C1m10, C3m10
+// q7: C1Q, C2Q, C3Q, C1m11  configuration-signed coefficients
+// q8: C3m11, C1m12, 0, 0
+
+struct __align__(16) ChainC {
+    float4 hdr;                 // x0_hi, x0_lo, y0_hi, y0_lo
+    uint32_t side_mask;         // active sides; 0 = chain inactive
+    uint32_t status;
+    uint32_t pad0, pad1;
+    float off[kMaxOffsets];     // per-dataset offsets θ[offset_idx + k]
+    float pad2[8];
+    SideC side[kSides];
+};
+static_assert(sizeof(ChainC) % 16 == 0, "ChainC must be a whole number of float4");
+
+// ---------------------------------------------------------------------------
+// FP64 per-chain set-up: rotation, corners, geometry check, per-side constants
+struct Vec3 { double x, y, z; };
+__device__ inline Vec3 v_sub(Vec3 a, Vec3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ inline Vec3 v_add(Vec3 a, Vec3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ inline Vec3 v_scale(Vec3 a, double s) { return {a.x * s, a.y * s, a.z * s}; }
+__device__ inline Vec3 v_cross(Vec3 a, Vec3 b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+__device__ inline double v_dot(Vec3 a, Vec3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+
+__device__ inline void split_hilo(double v, float& hi, float& lo) {
+    hi = (float)v;
+    lo = (float)(v - (double)hi);
+}
+
+__device__ void fill_side(SideC& S, Vec3 pa, Vec3 pb, Vec3 bvec, double nu, double x0, double y0,
+                          bool& active) {
+    const double PI = 3.14159265358979323846;
+    Vec3 side = v_sub(pb, pa);
+    double L = sqrt(v_dot(side, side));
+    double beta = acos(-side.z / L);
+    // vertical sides contribute nothing (libcdm.py:320-324)
+    const double eps = 2.220446049250313e-16;
+    if (!(L > 0.0) || fabs(beta) < eps || fabs(PI - beta) < eps) {
+        active = false;
+        return;
+    }
+    active = true;
+    double hl = sqrt(side.x * side.x + side.y * side.y);
+    double c = side.x / hl, s = side.y / hl;         // e1 = (c, s, 0), e2 = (s, -c, 0)
+    double sb = hl / L, cb = -side.z / L;            // β in (0, π): sin β >= 0
+    double tb2 = (cb >= 0.0) ? sb / (1.0 + cb) : (1.0 - cb) / sb;
+    double ctb2 = 1.0 / tb2;
+    double cot = cb / sb;
+    double k = 1.0 - 2.0 * nu;
+    double rx = pa.x - x0, ry = pa.y - y0;
+    double k1 = c * rx + s * ry;
+    double k2 = s * rx - c * ry;
+    double aA = -pa.z, aB = -pb.z, da = aB - aA;
+    double dy1 = -hl;                                // y1(B) - y1(A) = -e1·side
+    // slip in the angular-dislocation frame, with the 1/(2π) of the formula folded in
+    const double inv2pi = 0.5 / PI;
+    double b1 = (c * bvec.x + s * bvec.y) * inv2pi;
+    double b2 = (s * bvec.x - c * bvec.y) * inv2pi;
+    double b3 = -bvec.z * inv2pi;
+    double kc1 = k * cot * b1, kc2 = k * cot * b2;
+    double C1F = b1 * (1.0 - k * cot * cot);
+    double C2F = b2 * (1.0 + k * cot * cot);
+    double C3F = kc1 + b3;
+    double C1P = -b2 * k * (0.5 - cot * cot);
+    double C2P = b1 * k * (0.5 + cot * cot);
+    double C1m10 = -b1 * sb * cb + b3 * sb * sb;
+    double C3m10 = -b1 * cb * cb + b3 * sb * cb;
+    double C1Q = -kc2 * cot * cb;
+    double C2Q = -kc1 / sb;
+    double C3Q = kc2 * cb;
+    double C1m11 = b2 * sb;
+    double C3m11 = b2 * cb;
+    double C1m12 = b1 * cb - b3 * sb;
+    S.q[0] = make_float4((float)c, (float)s, (float)k1, (float)k2);
+    S.q[1] = make_float4((float)dy1, (float)aA, (float)aB, (float)da);
+    S.q[2] = make_float4((float)sb, (float)cb, (float)tb2, (float)ctb2);
+    S.q[3] = make_float4((float)(da * (aA + aB)), (float)C1F, (float)C2F, (float)C3F);
+    S.q[4] = make_float4((float)C1P, (float)C2P, (float)kc1, (float)kc2);
+    S.q[5] = make_float4((float)(2.0 * nu * b1), (float)(2.0 * nu * b2), (float)(0.5 * k * b1),
+                         (float)(0.5 * k * b2));
+    S.q[6] = make_float4((float)b1, (float)b2, (float)C1m10, (float)C3m10);
+    S.q[7] = make_float4((float)C1Q, (float)C2Q, (float)C3Q, (float)C1m11);
+    S.q[8] = make_float4((float)C3m11, (float)C1m12, 0.f, 0.f);
+}
+
+// corners of the three rectangles (libcdm.py:174-217); returns true if any is above the surface
+__device__ bool cdm_corners(const double* th, const ag_layout& L, Vec3 V[3][4]) {
+    const double x0 = th[L.x_idx], y0 = th[L.x_idx + 1], depth = th[L.depth_idx];
+    const double lx = 2.0 * th[L.axes_idx], ly = 2.0 * th[L.axes_idx + 1],
+                 lz = 2.0 * th[L.axes_idx + 2];
+    double sx, cx, sy, cy, sz, cz;
+    sincospi(th[L.omega_idx] / 180.0, &sx, &cx);
+    sincospi(th[L.omega_idx + 1] / 180.0, &sy, &cy);
+    sincospi(th[L.omega_idx + 2] / 180.0, &sz, &cz);
+    // R = Rz·Ry·Rx with Rx = [[1,0,0],[0,cx,sx],[0,-sx,cx]], Ry = [[cy,0,-sy],[0,1,0],[sy,0,cy]],
+    // Rz = [[cz,sz,0],[-sz,cz,0],[0,0,1]]; columns ex, ey, ez are the body axes in EFCS
+    const double ryx[3][3] = {{cy, sy * sx, -sy * cx},   // Ry·Rx
+                              {0.0, cx, sx},
+                              {sy, cy * -sx, cy * cx}};
+    double R[3][3];
+    const double rz[3][3] = {{cz, sz, 0.0}, {-sz, cz, 0.0}, {0.0, 0.0, 1.0}};
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            R[i][j] = rz[i][0] * ryx[0][j] + rz[i][1] * ryx[1][j] + rz[i][2] * ryx[2][j];
+    Vec3 ex{R[0][0], R[1][0], R[2][0]}, ey{R[0][1], R[1][1], R[2][1]}, ez{R[0][2], R[1][2], R[2][2]};
+    Vec3 c0{x0, y0, -depth};
+    Vec3 p1 = v_add(c0, v_add(v_scale(ey, 0.5 * ly), v_scale(ez, 0.5 * lz)));
+    Vec3 p2 = v_sub(p1, v_scale(ey, ly));
+    Vec3 p3 = v_sub(p2, v_scale(ez, lz));
+    Vec3 p4 = v_sub(p1, v_scale(ez, lz));
+    Vec3 q1 = v_add(v_sub(c0, v_scale(ex, 0.5 * lx)), v_scale(ez, 0.5 * lz));
+    Vec3 q2 = v_add(q1, v_scale(ex, lx));
+    Vec3 q3 = v_sub(q2, v_scale(ez, lz));
+    Vec3 q4 = v_sub(q1, v_scale(ez, lz));
+    Vec3 r1 = v_add(c0, v_add(v_scale(ex, 0.5 * lx), v_scale(ey, 0.5 * ly)));
+    Vec3 r2 = v_sub(r1, v_scale(ex, lx));
+    Vec3 r3 = v_sub(r2, v_scale(ey, ly));
+    Vec3 r4 = v_sub(r1, v_scale(ey, ly));
+    V[0][0] = p1; V[0][1] = p2; V[0][2] = p3; V[0][3] = p4;
+    V[1][0] = q1; V[1][1] = q2; V[1][2] = q3; V[1][3] = q4;
+    V[2][0] = r1; V[2][1] = r2; V[2][2] = r3; V[2][3] = r4;
+    bool above = false;
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 4; ++b) above |= (V[a][b].z > 0.0);
+    return above;
+}
+
+__global__ void cdm_setup_kernel(ag_layout L, const double* __restrict__ theta, int n,
+                                 const uint32_t* __restrict__ mask_in, ChainC* __restrict__ out,
+                                 uint32_t* __restrict__ chain_status, int noffsets) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    ChainC& C = out[i];
+    const double* th = theta + (size_t)i * L.nparams;
+    C.side_mask = 0u;
+    C.status = 0u;
+    if (mask_in && mask_in[i]) return;
+    Vec3 V[3][4];
+    bool above = cdm_corners(th, L, V);
+    const double x0 = th[L.x_idx], y0 = th[L.x_idx + 1];
+    split_hilo(x0, C.hdr.x, C.hdr.y);
+    split_hilo(y0, C.hdr.z, C.hdr.w);
+    for (int k = 0; k < kMaxOffsets; ++k)
+        C.off[k] = (k < noffsets) ? (float)th[L.offset_idx + k] : 0.f;
+    if (above) {
+        C.status = CHAIN_ABOVE_SURFACE;
+        if (chain_status) chain_status[i] |= CHAIN_ABOVE_SURFACE;
+        return;
+    }
+    // which rectangles take part (libcdm.py:226-242)
+    const double ax = th[L.axes_idx], ay = th[L.axes_idx + 1], az = th[L.axes_idx + 2];
+    bool use[3];
+    if (ax == 0.0 && ay == 0.0 && az == 0.0) {
+        use[0] = use[1] = use[2] = false;
+    } else if (ax == 0.0 && ay != 0.0 && az != 0.0) {
+        use[0] = true; use[1] = use[2] = false;
+    } else if (ax != 0.0 && ay == 0.0 && az != 0.0) {
+        use[1] = true; use[0] = use[2] = false;
+    } else if (ax != 0.0 && ay != 0.0 && az == 0.0) {
+        use[2] = true; use[0] = use[1] = false;
+    } else {
+        use[0] = use[1] = use[2] = true;
+    }
+    const double opening = th[L.strength_idx];
+    uint32_t mask = 0u;
+    for (int r = 0; r < 3; ++r) {
+        if (!use[r]) continue;
+        Vec3 nrm = v_cross(v_sub(V[r][1], V[r][0]), v_sub(V[r][3], V[r][0]));
+        nrm = v_scale(nrm, 1.0 / sqrt(v_dot(nrm, nrm)));
+        Vec3 b = v_scale(nrm, opening);
+        for (int e = 0; e < 4; ++e) {
+            bool act;
+            fill_side(C.side[r * 4 + e], V[r][e], V[r][(e + 1) & 3], b, L.nu, x0, y0, act);
+            if (act) mask |= 1u << (r * 4 + e);
+        }
+    }
+    // a chain with no active side still needs a llk: keep bit 31 as "evaluate"
+    C.side_mask = mask | 0x80000000u;
+}
+
+__global__ void cdm_check_kernel(ag_layout L, const double* __restrict__ theta, int n,
+                                 uint32_t* __restrict__ chain_status) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Vec3 V[3][4];
+    if (cdm_corners(theta + (size_t)i * L.nparams, L, V)) chain_status[i] |= CHAIN_ABOVE_SURFACE;
+}
+
+// ---------------------------------------------------------------------------
+// one angular-dislocation pair in difference arithmetic
+AG_DEVICE_INLINE float frcp(float x) { return __fdividef(1.0f, x); }
+
+AG_DEVICE_INLINE void side_pair(const SideC& S, float Xr, float Yr, float& ue, float& un,
+                                float& uv) {
+    const float4 q0 = S.q[0], q1 = S.q[1], q2 = S.q[2], q3 = S.q[3], q4 = S.q[4], q5 = S.q[5],
+                 q6 = S.q[6], q7 = S.q[7], q8 = S.q[8];
+    const float c = q0.x, s = q0.y;
+    const float dy1 = q1.x, aA = q1.y, aB = q1.z, da = q1.w;
+    // station in the angular-dislocation frame of vertex A; y2 is the same at B
+    const float y1A = fmaf(c, Xr, fmaf(s, Yr, -q0.z));
+    const float y2 = fmaf(s, Xr, fmaf(-c, Yr, -q0.w));
+    const float y1B = y1A + dy1;
+    // artefact-free configuration (libcdm.py:342-362): I if y1A >= 0 (β - π), else II (β)
+    const bool conf1 = y1A >= 0.0f;
+    const float sg = conf1 ? -1.0f : 1.0f;
+    const float sB = sg * q2.x, cB = sg * q2.y;
+    const float ct2 = conf1 ? -q2.z : q2.w;
+    const float y22 = y2 * y2;
+    // r
+    const float r2A = fmaf(y1A, y1A, fmaf(aA, aA, y22));
+    const float r2B = fmaf(y1B, y1B, fmaf(aB, aB, y22));
+    const float irA = rsqrtf(r2A), irB = rsqrtf(r2B);
+    const float rA = r2A * irA, rB = r2B * irB;
+    const float dr = fmaf(dy1, y1A + y1B, q3.x) * frcp(rA + rB);
+    const float dir = -dr * irA * irB;
+    // r + a
+    const float pA = rA + aA, pB = rB + aB, dp = dr + da;
+    const float ipA = frcp(pA), ipB = frcp(pB);
+    const float dip = -dp * ipA * ipB;
+    // z1, z3
+    const float z1A = fmaf(y1A, cB, aA * sB);
+    const float dz1 = fmaf(dy1, cB, da * sB);
+    const float z1B = z1A + dz1;
+    const float z3A = fmaf(y1A, sB, -aA * cB);
+    const float dz3 = fmaf(dy1, sB, -da * cB);
+    const float z3B = z3A + dz3;
+    // r - z3, cancellation-free: (z1² + y2²)/(r + z3) when z3 > 0
+    const bool posA = z3A > 0.0f, posB = z3B > 0.0f;
+    const float NA = fmaf(z1A, z1A, y22), NB = fmaf(z1B, z1B, y22);
+    const float DA = rA + z3A, DB = rB + z3B;
+    const float uA = posA ? NA : rA - z3A, vA = posA ? DA : 1.0f;
+    const float uB = posB ? NB : rB - z3B, vB = posB ? DB : 1.0f;
+    const float iuA = frcp(uA), ivA = frcp(vA), iuB = frcp(uB), ivB = frcp(vB);
+    const float qA = uA * ivA;
+    const float iqA = vA * iuA, iqB = vB * iuB;
+    const float dN = dz1 * (z1A + z1B);
+    const float dq = (posA && posB) ? fmaf(dN, DA, -NA * (dr + dz3)) * ivA * ivB : dr - dz3;
+    const float diq = -dq * iqA * iqB;
+    // log differences
+    const float dLp = log1pf(dp * ipA);
+    const float dLq = log1pf(dq * iqA);
+    (void)qA;
+    // Burgers function difference: rotation of (x, y2) from A to B; y2 keeps its sign so
+    // the rotation never crosses atan2's cut
+    const float xA = fmaf(pA, ct2, -y1A);
+    const float dx = fmaf(dp, ct2, -dy1);
+    const float xB = xA + dx;
+    const float dF = 2.0f * atan2f(-y2 * dx, fmaf(xA, xB, y22));
+    // monomials: value at A, value at B, difference
+    const float m1A = y2 * ipA, m1B = y2 * ipB, dm1 = y2 * dip;
+    const float m2A = y1A * ipA, m2B = y1B * ipB, dm2 = fmaf(dy1, ipB, y1A * dip);
+    const float dm3 = fmaf(da, ipB, aA * dip);
+    const float dm4 = fmaf(dm2, m1B, m2A * dm1);
+    const float dm5 = dm2 * (m2A + m2B);
+    const float dm6 = dm1 * (m1A + m1B);
+    const float y1irA = y1A * irA, y1irB = y1B * irB, dy1ir = fmaf(dy1, irB, y1A * dir);
+    const float y2irA = y2 * irA, y2irB = y2 * irB, dy2ir = y2 * dir;
+    const float airA = aA * irA, airB = aB * irB, dair = fmaf(da, irB, aA * dir);
+    const float dm7 = fmaf(dy1ir, m1B, y1irA * dm1);
+    const float dm8 = fmaf(dy1ir, m2B, y1irA * dm2);
+    const float dm9 = fmaf(dy2ir, m1B, y2irA * dm1);
+    const float m10A = y2 * iqA, m10B = y2 * iqB, dm10 = y2 * diq;
+    const float m11A = z1A * iqA, m11B = z1B * iqB, dm11 = fmaf(dz1, iqB, z1A * diq);
+    const float dm12 = fmaf(dy1ir, m10B, y1irA * dm10);
+    const float dm13 = fmaf(dy1ir, m11B, y1irA * dm11);
+    const float dm14 = fmaf(dy2ir, m10B, y2irA * dm10);
+    const float dm15 = fmaf(dy2ir, m11B, y2irA * dm11);
+    const float dm16 = fmaf(dair, m1B, airA * dm1);
+    const float dm17 = fmaf(dair, m2B, airA * dm2);
+    const float dm18 = fmaf(dair, m10B, airA * dm10);
+    const float dm19 = fmaf(dair, m11B, airA * dm11);
+    (void)airB; (void)y2irB; (void)y1irB; (void)m10A; (void)m11A;
+    // combination (coefficients precomputed per side; configuration sign applied last)
+    const float C1F = q3.y, C2F = q3.z, C3F = q3.w;
+    const float C1P = q4.x, C2P = q4.y, kc1 = q4.z, kc2 = q4.w;
+    const float nb1 = q5.x, nb2 = q5.y, hb1 = q5.z, hb2 = q5.w;
+    const float b1 = q6.x, b2 = q6.y, C1m10 = q6.z, C3m10 = q6.w;
+    const float C1Q = q7.x, C2Q = q7.y, C3Q = q7.z, C1m11 = q7.w;
+    const float C3m11 = q8.x, C1m12 = q8.y;
+    float v1 = C1F * dF;
+    v1 = fmaf(C1P, dLp, v1);
+    v1 = fmaf(kc1, dm1, v1);
+    v1 = fmaf(-kc2, dm2, v1);
+    v1 = fmaf(-hb2, dm3 + dm5, v1);
+    v1 = fmaf(hb1, dm4, v1);
+    v1 = fmaf(-b1, dm7, v1);
+    v1 = fmaf(b2, dm8 - dm13, v1);
+    v1 = fmaf(C1m10, dm10, v1);
+    float w1 = C1Q * dLq;
+    w1 = fmaf(C1m11, dm11, w1);
+    w1 = fmaf(C1m12, dm12, w1);
+    v1 = fmaf(sg, w1, v1);
+    float v2 = C2F * dF;
+    v2 = fmaf(C2P, dLp, v2);
+    v2 = fmaf(-kc2, dm1, v2);
+    v2 = fmaf(-kc1, dm2, v2);
+    v2 = fmaf(hb1, dm3 + dm6, v2);
+    v2 = fmaf(-hb2, dm4, v2);
+    v2 = fmaf(b2, dm7 - dm15, v2);
+    v2 = fmaf(-b1, dm9, v2);
+    float w2 = C2Q * dLq;
+    w2 = fmaf(C1m12, dm14, w2);
+    v2 = fmaf(sg, w2, v2);
+    float v3 = C3F * dF;
+    v3 = fmaf(-kc2, dLp, v3);
+    v3 = fmaf(nb1, dm1, v3);
+    v3 = fmaf(-nb2, dm2, v3);
+    v3 = fmaf(C3m10, dm10, v3);
+    v3 = fmaf(b1, dm16, v3);
+    v3 = fmaf(b2, dm19 - dm17, v3);
+    float w3 = C3Q * dLq;
+    w3 = fmaf(C3m11, dm11, w3);
+    w3 = fmaf(-C1m12, dm18, w3);
+    v3 = fmaf(sg, w3, v3);
+    // back to EFCS: columns e1 = (c, s, 0), e2 = (s, -c, 0), e3 = (0, 0, -1)
+    ue = fmaf(c, v1, fmaf(s, v2, ue));
+    un = fmaf(s, v1, fmaf(-c, v2, un));
+    uv -= v3;
+}
+
+// ---------------------------------------------------------------------------
+template <int WARPS>
+__global__ void __launch_bounds__(WARPS * 32, 2)
+cdm_llk_kernel(const ChainC* __restrict__ chains, int n, const float4* __restrict__ xy,
+               const float4* __restrict__ losd, const float* __restrict__ wt,
+               const int32_t* __restrict__ oid, int m_padded, double norm,
+               double* __restrict__ llk, float* __restrict__ resid, uint32_t* __restrict__ flags) {
+    __shared__ ChainC s_chain[WARPS];
+    __shared__ float4 s_xy[2][kTile];
+    __shared__ float4 s_ld[2][kTile];
+    __shared__ __align__(16) float s_w[2][kTile];
+    __shared__ __align__(16) int32_t s_oid[2][kTile];
+    __shared__ __align__(8) uint64_t bar[2];
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int chain = blockIdx.x * WARPS + warp;
+    const int ntiles = m_padded / kTile;
+    const bool with_oid = (oid != nullptr);
+    const uint32_t tile_bytes = kTile * (16u + 16u + 4u) + (with_oid ? kTile * 4u : 0u);
+
+    // this warp's chain constants
+    {
+        const float4* src = reinterpret_cast<const float4*>(chains + (chain < n ? chain : 0));
+        float4* dst = reinterpret_cast<float4*>(&s_chain[warp]);
+        constexpr int nvec = sizeof(ChainC) / 16;
+        for (int k = lane; k < nvec; k += 32) dst[k] = src[k];
+    }
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    auto issue = [&](int t, int buf) {
+        const size_t base = (size_t)t * kTile;
+        mbar_arrive_expect_tx(&bar[buf], tile_bytes);
+        bulk_g2s(&s_xy[buf][0], xy + base, kTile * 16u, &bar[buf]);
+        bulk_g2s(&s_ld[buf][0], losd + base, kTile * 16u, &bar[buf]);
+        bulk_g2s(&s_w[buf][0], wt + base, kTile * 4u, &bar[buf]);
+        if (with_oid) bulk_g2s(&s_oid[buf][0], oid + base, kTile * 4u, &bar[buf]);
+    };
+    if (threadIdx.x == 0) {
+        issue(0, 0);
+        if (ntiles > 1) issue(1, 1);
+    }
+    const ChainC& C = s_chain[warp];
+    const uint32_t smask = (chain < n) ? C.side_mask : 0u;
+    const bool active = smask != 0u;
+    const float x0h = C.hdr.x, x0l = C.hdr.y, y0h = C.hdr.z, y0l = C.hdr.w;
+    ff acc{0.f, 0.f};
+    int failed_at = -1;
+    int issued = (ntiles > 1) ? 2 : 1;
+    for (int t = 0; t < ntiles; ++t) {
+        const int buf = t & 1;
+        const uint32_t phase = (t >> 1) & 1;
+        const bool ok = mbar_wait_bounded(&bar[buf], phase, kWaitLimit);
+        if (__syncthreads_or(!ok)) { failed_at = t; break; }
+        if (active) {
+            for (int j = lane; j < kTile; j += 32) {
+                const float4 A = s_xy[buf][j];
+                const float4 B = s_ld[buf][j];
+                const float w = s_w[buf][j];
+                const float Xr = (A.x - x0h) + (A.y - x0l);
+                const float Yr = (A.z - y0h) + (A.w - y0l);
+                float ue = 0.f, un = 0.f, uv = 0.f;
+                uint32_t m = smask & 0x0FFFu;
+#pragma unroll 1
+                while (m) {
+                    const int sidx = __ffs(m) - 1;
+                    m &= m - 1;
+                    side_pair(C.side[sidx], Xr, Yr, ue, un, uv);
+                }
+                const float u = fmaf(ue, B.x, fmaf(un, B.y, uv * B.z));
+                float r = u - B.w;
+                if (with_oid) r -= C.off[s_oid[buf][j] & (kMaxOffsets - 1)];
+                if (w != 0.f) ff_add_wsq(acc, r, w);
+                if (resid) resid[(size_t)chain * m_padded + (size_t)t * kTile + j] = (w != 0.f) ? r : 0.f;
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0 && t + 2 < ntiles) {
+            issue(t + 2, buf);
+            ++issued;
+        }
+    }
+    if (failed_at >= 0) {
+        // drain the copies still in flight (bounded) before the CTA exits
+        if (threadIdx.x == 0) {
+            raise_flag(flags, DEV_ERR_TIMEOUT);
+            for (int t = failed_at; t < issued; ++t)
+                mbar_wait_bounded(&bar[t & 1], (t >> 1) & 1, kWaitLimit);
+        }
+        return;
+    }
+    const double sum = warp_sum(ff_to_double(acc));
+    if (lane == 0 && active) llk[chain] = norm - 0.5 * sum;
+}
+
+// ---------------------------------------------------------------------------
+// Mogi: one thread per station, CH chains per CTA held in shared memory
+struct __align__(16) MogiSrc {
+    float4 pos;    // x0_hi, x0_lo, y0_hi, y0_lo
+    float4 prm;    // depth, C = (nu - 1) ΔV / π, 0, 0
+};
+
+template <int CH, int NSRC>
+__global__ void __launch_bounds__(256, 2)
+mogi_llk_kernel(ag_layout L, const double* __restrict__ theta, int n,
+                const uint32_t* __restrict__ mask_in, const float4* __restrict__ xy,
+                const float4* __restrict__ losd, const float* __restrict__ wt,
+                const int32_t* __restrict__ oid, int noffsets, int m_padded, double norm,
+                double* __restrict__ llk, float* __restrict__ resid) {
+    __shared__ MogiSrc s_src[CH][NSRC];
+    __shared__ float s_off[CH][kMaxOffsets];
+    __shared__ int s_act[CH];
+    __shared__ double s_part[CH][8];
+    const int c0 = blockIdx.x * CH;
+    const double PI = 3.14159265358979323846;
+    for (int k = threadIdx.x; k < CH * NSRC; k += blockDim.x) {
+        const int c = k / NSRC, src = k % NSRC, i = c0 + c;
+        MogiSrc S{};
+        if (i < n) {
+            const double* th = theta + (size_t)i * L.nparams + src * L.source_stride;
+            split_hilo(th[L.x_idx], S.pos.x, S.pos.y);
+            split_hilo(th[L.x_idx + 1], S.pos.z, S.pos.w);
+            const double dv = L.log_strength ? pow(10.0, th[L.strength_idx]) : th[L.strength_idx];
+            S.prm = make_float4((float)th[L.depth_idx], (float)((L.nu - 1.0) * dv / PI), 0.f, 0.f);
+        }
+        s_src[c][src] = S;
+    }
+    for (int k = threadIdx.x; k < CH * kMaxOffsets; k += blockDim.x) {
+        const int c = k / kMaxOffsets, o = k % kMaxOffsets, i = c0 + c;
+        s_off[c][o] = (i < n && o < noffsets)
+                          ? (float)theta[(size_t)i * L.nparams + L.offset_idx + o] : 0.f;
+    }
+    for (int c = threadIdx.x; c < CH; c += blockDim.x) {
+        const int i = c0 + c;
+        s_act[c] = (i < n) && !(mask_in && mask_in[i]);
+    }
+    __syncthreads();
+    ff acc[CH];
+#pragma unroll
+    for (int c = 0; c < CH; ++c) acc[c] = ff{0.f, 0.f};
+    for (int j = threadIdx.x; j < m_padded; j += blockDim.x) {
+        const float4 A = __ldg(xy + j);
+        const float4 B = __ldg(losd + j);
+        const float w = __ldg(wt + j);
+        const int o = oid ? (__ldg(oid + j) & (kMaxOffsets - 1)) : 0;
+#pragma unroll
+        for (int c = 0; c < CH; ++c) {
+            float u = 0.f;
+#pragma unroll
+            for (int sidx = 0; sidx < NSRC; ++sidx) {
+                const MogiSrc S = s_src[c][sidx];
+                // source minus observation point (libmogi/Source.cc:86-88)
+                const float dx = (S.pos.x - A.x) + (S.pos.y - A.y);
+                const float dy = (S.pos.z - A.z) + (S.pos.w - A.w);
+                const float d = S.prm.x;
+                const float R2 = fmaf(dx, dx, fmaf(dy, dy, d * d));
+                const float iR = rsqrtf(R2);
+                const float iR3 = iR * iR * iR;
+                const float proj = fmaf(dx, B.x, fmaf(dy, B.y, -d * B.z));
+                u = fmaf(S.prm.y * proj, iR3, u);
+            }
+            float r = u - B.w;
+            if (oid) r -= s_off[c][o];
+            if (w != 0.f) ff_add_wsq(acc[c], r, w);
+            if (resid && c0 + c < n) resid[(size_t)(c0 + c) * m_padded + j] = (w != 0.f) ? r : 0.f;
+        }
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+    for (int c = 0; c < CH; ++c) {
+        const double v = warp_sum(ff_to_double(acc[c]));
+        if (lane == 0) s_part[c][warp] = v;
+    }
+    __syncthreads();
+    for (int c = threadIdx.x; c < CH; c += blockDim.x) {
+        if (!s_act[c]) continue;
+        double s = 0.0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += s_part[c][k];
+        llk[c0 + c] = norm - 0.5 * s;
+    }
+}
+
+}  // namespace ag
+
+// ---------------------------------------------------------------------------
+// C ABI
+using namespace ag;
+
+static constexpr int kCdmWarps = 8;
+static constexpr int kMogiChains = 16;
+
+extern "C" size_t ag_forward_workspace_bytes(int model, int32_t n) {
+    if (model == AG_MODEL_CDM && n > 0) return (size_t)n * sizeof(ChainC);
+    return 0;
+}
+
+static int check_stations(const ag_station_set* st) {
+    AG_REQUIRE(st != nullptr, "stations is NULL");
+    AG_REQUIRE(st->xy && st->losd && st->weight, "station arrays must not be NULL");
+    AG_REQUIRE(st->m > 0 && st->m_padded >= st->m && st->m_padded % AG_STATION_TILE == 0,
+               "m=%d m_padded=%d: m_padded must be a multiple of %d and >= m", st->m,
+               st->m_padded, AG_STATION_TILE);
+    AG_REQUIRE(aligned(st->xy, 16) && aligned(st->losd, 16) && aligned(st->weight, 16) &&
+                   (st->oid == nullptr || aligned(st->oid, 16)),
+               "station arrays must be 16-byte aligned");
+    return AG_OK;
+}
+
+extern "C" int ag_forward_llk(int model, const ag_layout* layout, const double* theta, int32_t n,
+                              const ag_station_set* st, double norm, const uint32_t* mask_in,
+                              double* llk, uint32_t* chain_status, float* residuals,
+                              void* workspace, size_t workspace_bytes, void* stream) {
+    AG_REQUIRE(layout != nullptr && theta != nullptr && llk != nullptr, "null argument");
+    AG_REQUIRE(n > 0, "n must be positive (got %d)", n);
+    int rc = check_stations(st);
+    if (rc) return rc;
+    const ag_layout L = *layout;
+    AG_REQUIRE(L.nparams > 0 && L.x_idx >= 0 && L.x_idx + 1 < L.nparams && L.depth_idx >= 0 &&
+                   L.depth_idx < L.nparams && L.strength_idx >= 0 && L.strength_idx < L.nparams,
+               "invalid parameter layout");
+    int noffsets = 0;
+    if (st->oid) {
+        AG_REQUIRE(L.offset_idx >= 0, "stations carry dataset ids but the layout has no offsets");
+        noffsets = L.nparams - L.offset_idx;
+        AG_REQUIRE(noffsets > 0 && noffsets <= kMaxOffsets,
+                   "between 1 and %d offset parameters are supported", kMaxOffsets);
+    }
+    cudaStream_t s = as_stream(stream);
+    const float4* xy = reinterpret_cast<const float4*>(st->xy);
+    const float4* ld = reinterpret_cast<const float4*>(st->losd);
+    if (model == AG_MODEL_CDM) {
+        AG_REQUIRE(L.axes_idx >= 0 && L.axes_idx + 2 < L.nparams && L.omega_idx >= 0 &&
+                       L.omega_idx + 2 < L.nparams,
+                   "invalid CDM layout");
+        const size_t need = ag_forward_workspace_bytes(model, n);
+        AG_REQUIRE(workspace != nullptr && workspace_bytes >= need && aligned(workspace, 256),
+                   "CDM needs %zu bytes of 256-byte aligned workspace", need);
+        ChainC* chains = reinterpret_cast<ChainC*>(workspace);
+        cdm_setup_kernel<<<(n + 127) / 128, 128, 0, s>>>(L, theta, n, mask_in, chains, chain_status,
+                                                         noffsets);
+        rc = launch_status("cdm_setup_kernel");
+        if (rc) return rc;
+        const int grid = (n + kCdmWarps - 1) / kCdmWarps;
+        cdm_llk_kernel<kCdmWarps><<<grid, kCdmWarps * 32, 0, s>>>(
+            chains, n, xy, ld, st->weight, st->oid, st->m_padded, norm, llk, residuals, nullptr);
+        return launch_status("cdm_llk_kernel");
+    }
+    if (model == AG_MODEL_MOGI) {
+        AG_REQUIRE(L.nsources == 1 || L.nsources == 2, "1 or 2 Mogi sources are supported");
+        const int grid = (n + kMogiChains - 1) / kMogiChains;
+        if (L.nsources == 1)
+            mogi_llk_kernel<kMogiChains, 1><<<grid, 256, 0, s>>>(
+                L, theta, n, mask_in, xy, ld, st->weight, st->oid, noffsets, st->m_padded, norm, llk,
+                residuals);
+        else
+            mogi_llk_kernel<kMogiChains, 2><<<grid, 256, 0, s>>>(
+                L, theta, n, mask_in, xy, ld, st->weight, st->oid, noffsets, st->m_padded, norm, llk,
+                residuals);
+        return launch_status("mogi_llk_kernel");
+    }
+    return set_error(AG_ERR_ARG, "unknown model %d", model);
+}
+
+extern "C" int ag_cdm_check(const ag_layout* layout, const double* theta, int32_t n,
+                            uint32_t* chain_status, void* stream) {
+    AG_REQUIRE(layout && theta && chain_status && n > 0, "invalid arguments");
+    cdm_check_kernel<<<(n + 127) / 128, 128, 0, as_stream(stream)>>>(*layout, theta, n, chain_status);
+    return launch_status("cdm_check_kernel");
+}

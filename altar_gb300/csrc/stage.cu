@@ -1,0 +1,834 @@
+// Per-stage CATMIP kernels: prior, Metropolis proposal/accept, COV β schedule,
+// weighted covariance, Cholesky, multinomial resampling, scaling adaptation.
+//
+// Every kernel is a fixed launch shape on the caller's stream with all
+// data-dependent control flow kept on the device (a "done" flag in the
+// schedule state instead of host round trips), so one annealing stage can be
+// captured into one CUDA graph.  All reductions run in a fixed order, so
+// repeated runs are bitwise identical.
+#include <math.h>
+#include <stdint.h>
+
+#include "common.cuh"
+#include "internal.h"
+
+namespace ag {
+
+constexpr int kMaxP = 32;          // largest parameter count of the stage kernels
+constexpr int kGridPoints = 11;    // COV.cc:276 Nbeta = 10 -> 11 points per level
+constexpr int kGridLevels = 11;    // COV.cc:313 Nloop <= Nbeta
+constexpr int kEvalChunk = 1024;   // chains per CTA in a COV evaluation
+constexpr int kSigmaChunk = 256;   // chains per CTA in the covariance
+
+// ---------------------------------------------------------------------------
+// prior
+__global__ void prior_sample_kernel(int n, int p, const double* __restrict__ lo,
+                                    const double* __restrict__ hi, uint64_t seed, uint32_t attempt,
+                                    const uint32_t* __restrict__ redraw, double* __restrict__ theta) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (redraw && !redraw[i]) return;
+    for (int j = 0; j < p; ++j) {
+        u32x4 r = draw(seed, (uint32_t)i, (uint32_t)j, STREAM_PRIOR, 0u, attempt);
+        double u = u01_closed_open(r.x, r.y);
+        // gsl_ran_flat: a (1 - u) + b u
+        theta[(size_t)i * p + j] = lo[j] * (1.0 - u) + hi[j] * u;
+    }
+}
+
+__device__ inline double uniform_log_prior(int p, const double* lo, const double* hi) {
+    double s = 0.0;
+    for (int j = 0; j < p; ++j) s -= log(hi[j] - lo[j]);
+    return s;
+}
+
+__global__ void prior_llk_kernel(const double* __restrict__ theta, int n, int p,
+                                 const double* __restrict__ lo, const double* __restrict__ hi,
+                                 uint32_t* __restrict__ mask, double* __restrict__ prior) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    bool out = false;
+    for (int j = 0; j < p; ++j) {
+        double v = theta[(size_t)i * p + j];
+        out |= !(lo[j] <= v && v <= hi[j]);
+    }
+    if (mask && out) mask[i] |= CHAIN_OUT_OF_SUPPORT;
+    if (prior) prior[i] = uniform_log_prior(p, lo, hi);
+}
+
+// ---------------------------------------------------------------------------
+// Metropolis proposal, verify and prior (Metropolis.py:160-183, 236-259)
+__global__ void propose_kernel(const double* __restrict__ theta, int n, int p,
+                               const double* __restrict__ chol, const double* __restrict__ lo,
+                               const double* __restrict__ hi, uint64_t seed, uint32_t step,
+                               const uint32_t* __restrict__ epoch, double* __restrict__ cand,
+                               uint32_t* __restrict__ mask, double* __restrict__ cprior) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t ep = *epoch;
+    double z[kMaxP];
+    for (int j = 0; j < p; j += 2) {
+        double z0, z1;
+        normal_pair(draw(seed, (uint32_t)i, (uint32_t)(j >> 1), STREAM_PROPOSAL, step, ep), z0, z1);
+        z[j] = z0;
+        if (j + 1 < p) z[j + 1] = z1;
+    }
+    const double* th = theta + (size_t)i * p;
+    double* c = cand + (size_t)i * p;
+    bool out = false;
+    for (int j = 0; j < p; ++j) {
+        double d = 0.0;
+        for (int k = 0; k <= j; ++k) d = fma(chol[j * p + k], z[k], d);
+        double v = th[j] + d;
+        c[j] = v;
+        out |= !(lo[j] <= v && v <= hi[j]);
+    }
+    if (out)
+        for (int j = 0; j < p; ++j) c[j] = th[j];
+    mask[i] = out ? CHAIN_OUT_OF_SUPPORT : 0u;
+    cprior[i] = uniform_log_prior(p, lo, hi);
+}
+
+// ---------------------------------------------------------------------------
+// Metropolis accept/reject (Metropolis.py:185-223)
+__global__ void accept_kernel(int n, int p, const double* __restrict__ beta, uint64_t seed,
+                              uint32_t step, const uint32_t* __restrict__ epoch,
+                              const uint32_t* __restrict__ mask, const double* __restrict__ cand,
+                              const double* __restrict__ cprior, const double* __restrict__ cdata,
+                              double* __restrict__ theta, double* __restrict__ prior,
+                              double* __restrict__ data, double* __restrict__ post,
+                              unsigned long long* __restrict__ counters) {
+    __shared__ unsigned int s_cnt[3];
+    if (threadIdx.x < 3) s_cnt[threadIdx.x] = 0u;
+    __syncthreads();
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        if (mask[i]) {
+            atomicAdd(&s_cnt[1], 1u);
+        } else {
+            const double b = *beta;
+            const double cp = cprior[i] + b * cdata[i];
+            u32x4 r = draw(seed, (uint32_t)i, 0u, STREAM_ACCEPT, step, *epoch);
+            const double u = u01_open_closed(r.x, r.y);
+            if (log(u) > cp - post[i]) {
+                atomicAdd(&s_cnt[2], 1u);
+            } else {
+                atomicAdd(&s_cnt[0], 1u);
+                for (int j = 0; j < p; ++j) theta[(size_t)i * p + j] = cand[(size_t)i * p + j];
+                prior[i] = cprior[i];
+                data[i] = cdata[i];
+                post[i] = cp;
+            }
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 3 && s_cnt[threadIdx.x])
+        atomicAdd(&counters[threadIdx.x], (unsigned long long)s_cnt[threadIdx.x]);
+}
+
+__global__ void posterior_kernel(int n, const double* __restrict__ beta,
+                                 const double* __restrict__ prior, const double* __restrict__ data,
+                                 double* __restrict__ post) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) post[i] = prior[i] + (*beta) * data[i];
+}
+
+// ---------------------------------------------------------------------------
+// COV β schedule (COV.cc:222-368).
+struct CovState {
+    double median;
+    double llk_max;
+    double beta0;          // β at the start of the stage
+    double low, high, step;
+    double pts[kGridPoints];
+    double cov_high;       // COV at the full remaining δβ
+    double dbeta;          // chosen δβ
+    double cov;            // COV at dbeta
+    double s1;             // shifted weight sum at dbeta
+    int npts;              // points to evaluate in the next round
+    int level;             // levels done (Nloop)
+    int done;
+    int skip;              // jumped straight to β = 1
+};
+
+// order-preserving map of a double onto uint64
+__device__ inline uint64_t dkey(double x) {
+    uint64_t b = (uint64_t)__double_as_longlong(x);
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ inline double dkey_inv(uint64_t k) {
+    uint64_t b = (k >> 63) ? (k & 0x7FFFFFFFFFFFFFFFull) : ~k;
+    return __longlong_as_double((long long)b);
+}
+
+// k-th smallest (0-based) key of llk by 8-bit radix select; one CTA
+__device__ uint64_t block_select(const double* __restrict__ llk, int n, int k, int* hist,
+                                 int* sh) {
+    uint64_t prefix = 0ull, mask = 0ull;
+    for (int pass = 0; pass < 8; ++pass) {
+        const int shift = 56 - 8 * pass;
+        for (int b = threadIdx.x; b < 256; b += blockDim.x) hist[b] = 0;
+        __syncthreads();
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            uint64_t key = dkey(llk[i]);
+            if ((key & mask) == prefix) atomicAdd(&hist[(key >> shift) & 255], 1);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int acc = 0, d = 0;
+            for (; d < 256; ++d) {
+                if (acc + hist[d] > k) break;
+                acc += hist[d];
+            }
+            sh[0] = d;
+            sh[1] = k - acc;
+        }
+        __syncthreads();
+        const int d = sh[0];
+        k = sh[1];
+        prefix |= (uint64_t)d << shift;
+        mask |= 255ull << shift;
+        __syncthreads();
+    }
+    return prefix;
+}
+
+__global__ void __launch_bounds__(1024) cov_median_kernel(const double* __restrict__ llk, int n,
+                                                          const double* __restrict__ beta,
+                                                          CovState* __restrict__ S) {
+    __shared__ int hist[256];
+    __shared__ int sh[2];
+    __shared__ double smax[32];
+    // maximum
+    double mx = -INFINITY;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) mx = fmax(mx, llk[i]);
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) smax[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    // median as gsl_stats_median_from_sorted_data: mean of elements (n-1)/2 and n/2
+    const uint64_t klo = block_select(llk, n, (n - 1) / 2, hist, sh);
+    const uint64_t khi = (n % 2) ? klo : block_select(llk, n, n / 2, hist, sh);
+    if (threadIdx.x == 0) {
+        double m = smax[0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = fmax(m, smax[w]);
+        const double lo = dkey_inv(klo), hi = dkey_inv(khi);
+        S->median = (n % 2) ? lo : (lo + hi) / 2.0;
+        S->llk_max = m;
+        S->beta0 = *beta;
+        S->low = 0.0;
+        S->high = 1.0 - *beta;
+        S->step = 0.0;
+        S->pts[0] = S->high;     // round 0 evaluates the full remaining step
+        S->npts = 1;
+        S->level = 0;
+        S->done = 0;
+        S->skip = 0;
+    }
+}
+
+// shifted weight moments of one grid point over one chunk of chains
+__global__ void __launch_bounds__(256) cov_eval_kernel(const double* __restrict__ llk, int n,
+                                                       const CovState* __restrict__ S,
+                                                       double* __restrict__ part) {
+    const int pt = blockIdx.y;
+    if (S->done || pt >= S->npts) return;
+    const double g = S->pts[pt];
+    const double med = S->median;
+    const double mx = g * (S->llk_max - med);
+    double s1 = 0.0, s2 = 0.0;
+    const int begin = blockIdx.x * kEvalChunk;
+    const int end = min(n, begin + kEvalChunk);
+    for (int i = begin + threadIdx.x; i < end; i += blockDim.x) {
+        const double e = exp(g * (llk[i] - med) - mx);
+        s1 += e;
+        s2 = fma(e, e, s2);
+    }
+    __shared__ double r1[8], r2[8];
+    s1 = warp_sum(s1);
+    s2 = warp_sum(s2);
+    if ((threadIdx.x & 31) == 0) {
+        r1[threadIdx.x >> 5] = s1;
+        r2[threadIdx.x >> 5] = s2;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0, b = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+            a += r1[w];
+            b += r2[w];
+        }
+        part[((size_t)pt * gridDim.x + blockIdx.x) * 2 + 0] = a;
+        part[((size_t)pt * gridDim.x + blockIdx.x) * 2 + 1] = b;
+    }
+}
+
+// COV of the normalised weights from the shifted moments, with the reference's
+// convention that a non-finite COV counts as 1e100 (COV.cc:355-364)
+__device__ double cov_from_moments(double s1, double s2, double mx, int n) {
+    // an infinite weight in the reference (exp overflow) or an infinite weight sum
+    if (isinf(exp(mx)) || !(s1 > 0.0) || isinf(exp(mx) * s1)) return 1e100;
+    double v = (s2 / (s1 * s1) - 1.0 / n) / (double)(n - 1);
+    if (v < 0.0) v = 0.0;
+    double c = (double)n * sqrt(v);
+    if (!isfinite(c)) return 1e100;
+    return c;
+}
+
+__global__ void cov_decide_kernel(int n, int nblk, double target, double tol,
+                                  const double* __restrict__ part, CovState* __restrict__ S) {
+    if (threadIdx.x != 0 || S->done) return;
+    double cov[kGridPoints];
+    for (int pt = 0; pt < S->npts; ++pt) {
+        double a = 0.0, b = 0.0;
+        for (int k = 0; k < nblk; ++k) {
+            a += part[((size_t)pt * nblk + k) * 2 + 0];
+            b += part[((size_t)pt * nblk + k) * 2 + 1];
+        }
+        cov[pt] = cov_from_moments(a, b, S->pts[pt] * (S->llk_max - S->median), n);
+    }
+    const double Nbeta = 10.0;
+    if (S->level == 0) {
+        // skip straight to β = 1 (COV.cc:257-268)
+        S->cov_high = cov[0];
+        if (cov[0] < target || fabs(cov[0] - target) < tol) {
+            S->done = 1;
+            S->skip = 1;
+            S->dbeta = S->high;
+            return;
+        }
+    } else {
+        // scan of one level (COV.cc:287-311)
+        bool found = false;
+        int nb = 0;
+        for (; nb < S->npts; ++nb) {
+            if (fabs(cov[nb] - target) < tol) { found = true; break; }
+            if (cov[nb] >= target) { if (nb == 0) found = true; break; }
+        }
+        const double step = S->step;
+        // a completed scan leaves the reference's accumulator one step past the last
+        // point and steps it back (COV.cc:301), which can differ from that point in the
+        // last bit
+        const double guess = (nb < S->npts) ? S->pts[nb] : (S->pts[S->npts - 1] + step) - step;
+        S->high = guess;
+        S->low = guess - step;
+        if (found || S->level >= kGridLevels) {
+            S->done = 1;
+            S->dbeta = guess;
+            return;
+        }
+    }
+    // next level: points low, low + step, ... accumulated as the reference does
+    S->level += 1;
+    const double step = (S->high - S->low) / Nbeta;
+    S->step = step;
+    double g = S->low;
+    for (int k = 0; k < kGridPoints; ++k) {
+        S->pts[k] = g;
+        g += step;
+    }
+    S->npts = kGridPoints;
+}
+
+// final weights at the chosen δβ: sums first, then normalise
+__global__ void __launch_bounds__(256) cov_final_sum_kernel(const double* __restrict__ llk, int n,
+                                                            const CovState* __restrict__ S,
+                                                            double* __restrict__ part) {
+    const double g = S->dbeta, med = S->median;
+    const double mx = g * (S->llk_max - med);
+    double s1 = 0.0, s2 = 0.0;
+    const int begin = blockIdx.x * kEvalChunk;
+    const int end = min(n, begin + kEvalChunk);
+    for (int i = begin + threadIdx.x; i < end; i += blockDim.x) {
+        const double e = exp(g * (llk[i] - med) - mx);
+        s1 += e;
+        s2 = fma(e, e, s2);
+    }
+    __shared__ double r1[8], r2[8];
+    s1 = warp_sum(s1);
+    s2 = warp_sum(s2);
+    if ((threadIdx.x & 31) == 0) {
+        r1[threadIdx.x >> 5] = s1;
+        r2[threadIdx.x >> 5] = s2;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0, b = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+            a += r1[w];
+            b += r2[w];
+        }
+        part[(size_t)blockIdx.x * 2 + 0] = a;
+        part[(size_t)blockIdx.x * 2 + 1] = b;
+    }
+}
+
+__global__ void cov_final_state_kernel(int n, int nblk, const double* __restrict__ part,
+                                       CovState* __restrict__ S, double* __restrict__ beta,
+                                       double* __restrict__ dbeta_cov) {
+    if (threadIdx.x != 0) return;
+    double a = 0.0, b = 0.0;
+    for (int k = 0; k < nblk; ++k) {
+        a += part[(size_t)k * 2 + 0];
+        b += part[(size_t)k * 2 + 1];
+    }
+    S->s1 = a;
+    S->cov = cov_from_moments(a, b, S->dbeta * (S->llk_max - S->median), n);
+    // β bookkeeping (COV.cc:264, 323)
+    *beta = S->skip ? 1.0 : S->beta0 + S->dbeta;
+    dbeta_cov[0] = S->dbeta;
+    dbeta_cov[1] = S->cov;
+}
+
+__global__ void cov_weights_kernel(const double* __restrict__ llk, int n,
+                                   const CovState* __restrict__ S, double* __restrict__ w) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double g = S->dbeta, med = S->median;
+    const double mx = g * (S->llk_max - med);
+    w[i] = exp(g * (llk[i] - med) - mx) / S->s1;
+}
+
+// ---------------------------------------------------------------------------
+// weighted covariance (COV.py:106-156): per-chunk partial sums in fixed order
+__global__ void __launch_bounds__(256) sigma_partial_kernel(const double* __restrict__ theta,
+                                                            const double* __restrict__ w, int n,
+                                                            int p, double* __restrict__ part) {
+    extern __shared__ double sm[];      // [kSigmaChunk][p] θ, then [kSigmaChunk] w
+    double* sth = sm;
+    double* sw = sm + (size_t)kSigmaChunk * p;
+    const int begin = blockIdx.x * kSigmaChunk;
+    const int cnt = min(kSigmaChunk, n - begin);
+    for (int k = threadIdx.x; k < cnt * p; k += blockDim.x) sth[k] = theta[(size_t)begin * p + k];
+    for (int k = threadIdx.x; k < cnt; k += blockDim.x) sw[k] = w[begin + k];
+    __syncthreads();
+    // entries: 0 = Σw, 1..p = Σ w θ_a, then lower triangle (a >= b) Σ w θ_a θ_b
+    const int nent = 1 + p + p * (p + 1) / 2;
+    for (int e = threadIdx.x; e < nent; e += blockDim.x) {
+        int a = -1, b = -1;
+        if (e >= 1 && e <= p) {
+            a = e - 1;
+        } else if (e > p) {
+            int t = e - 1 - p;
+            a = 0;
+            while (t > a) { t -= a + 1; ++a; }
+            b = t;
+        }
+        double acc = 0.0;
+        for (int i = 0; i < cnt; ++i) {
+            double v = sw[i];
+            if (a >= 0) v *= sth[i * p + a];
+            if (b >= 0) v *= sth[i * p + b];
+            acc += v;
+        }
+        part[(size_t)blockIdx.x * nent + e] = acc;
+    }
+}
+
+__global__ void sigma_final_kernel(int p, int nblk, const double* __restrict__ part,
+                                   double* __restrict__ sigma) {
+    const int nent = 1 + p + p * (p + 1) / 2;
+    __shared__ double tot[1 + kMaxP + kMaxP * (kMaxP + 1) / 2];
+    for (int e = threadIdx.x; e < nent; e += blockDim.x) {
+        double acc = 0.0;
+        for (int k = 0; k < nblk; ++k) acc += part[(size_t)k * nent + e];
+        tot[e] = acc;
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    double mean[kMaxP];
+    for (int a = 0; a < p; ++a) mean[a] = tot[1 + a] / tot[0];   // weighted mean (gsl_stats_wmean)
+    int e = 1 + p;
+    for (int a = 0; a < p; ++a)
+        for (int b = 0; b <= a; ++b, ++e) {
+            const double v = tot[e] - mean[a] * mean[b];
+            sigma[a * p + b] = v;
+            sigma[b * p + a] = v;
+        }
+}
+
+// chol(scaling² Σ), lower triangle row-major (Metropolis.py:103-107)
+__global__ void cholesky_kernel(int p, const double* __restrict__ sigma,
+                                const double* __restrict__ scaling, double* __restrict__ L,
+                                uint32_t* __restrict__ flags) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double A[kMaxP * kMaxP];
+    const double s2 = (*scaling) * (*scaling);
+    for (int k = 0; k < p * p; ++k) A[k] = s2 * sigma[k];
+    bool ok = true;
+    for (int j = 0; j < p; ++j) {
+        double d = A[j * p + j];
+        for (int k = 0; k < j; ++k) d -= A[j * p + k] * A[j * p + k];
+        if (!(d > 0.0)) {
+            ok = false;
+            break;
+        }
+        const double ljj = sqrt(d);
+        A[j * p + j] = ljj;
+        for (int i = j + 1; i < p; ++i) {
+            double v = A[i * p + j];
+            for (int k = 0; k < j; ++k) v -= A[i * p + k] * A[j * p + k];
+            A[i * p + j] = v / ljj;
+        }
+    }
+    if (!ok) {
+        // keep the walk defined: fall back to the scaled diagonal and report
+        raise_flag(flags, DEV_ERR_NOT_SPD);
+        for (int i = 0; i < p; ++i)
+            for (int k = 0; k < p; ++k)
+                L[i * p + k] = (i == k) ? sqrt(fmax(s2 * sigma[i * p + i], 0.0)) : 0.0;
+        return;
+    }
+    for (int i = 0; i < p; ++i)
+        for (int k = 0; k < p; ++k) L[i * p + k] = (k <= i) ? A[i * p + k] : 0.0;
+}
+
+// ---------------------------------------------------------------------------
+// multinomial resampling (COV.py:160-251)
+struct ResampleHdr {
+    int total;        // number of copied rows (Σ counts)
+    int first_src;    // source row of output row 0
+    int pad[2];
+};
+
+// sequential FP64 partial sums, as itertools.accumulate (COV.py:242-251)
+__global__ void cdf_kernel(const double* __restrict__ w, int n, double* __restrict__ edges) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double acc = 0.0;
+    edges[0] = 0.0;
+    for (int i = 0; i < n; ++i) {
+        acc += w[i];
+        edges[i + 1] = acc;
+    }
+}
+
+// counts[i] = #{j : edges[i] <= r_j < edges[i+1]}; r_j >= edges[n] dropped (gsl_histogram)
+__global__ void counts_kernel(int n, uint64_t seed, const uint32_t* __restrict__ epoch,
+                              const double* __restrict__ edges, int* __restrict__ counts) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    u32x4 r = draw(seed, (uint32_t)j, 0u, STREAM_RESAMPLE, 0u, *epoch);
+    const double x = u01_closed_open(r.x, r.y);
+    if (!(x >= edges[0]) || !(x < edges[n])) return;
+    // largest i with edges[i] <= x
+    int lo = 0, hi = n;          // edges[lo] <= x < edges[hi]
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (x >= edges[mid]) lo = mid; else hi = mid;
+    }
+    atomicAdd(&counts[lo], 1);
+}
+
+__global__ void count_hist_kernel(int n, const int* __restrict__ counts, int* __restrict__ hist) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && counts[i] > 0) atomicAdd(&hist[counts[i]], 1);
+}
+
+// base[v] = Σ_{v' > v} v'·hist[v'] (reverse exclusive scan) then stable ranks within
+// equal counts: start_i = base[c_i] + c_i · #{k < i : c_k = c_i}
+constexpr int kRankCache = 4096;
+__global__ void __launch_bounds__(1024) rank_kernel(int n, const int* __restrict__ counts,
+                                                    int* __restrict__ hist, int* __restrict__ base,
+                                                    int* __restrict__ seen, int* __restrict__ start,
+                                                    ResampleHdr* __restrict__ hdr) {
+    __shared__ int warp_tot[32];
+    __shared__ int carry;
+    __shared__ int s_seen[kRankCache];
+    if (threadIdx.x == 0) carry = 0;
+    for (int k = threadIdx.x; k < kRankCache; k += blockDim.x) s_seen[k] = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // values n .. 0 in chunks of blockDim, processed from high to low
+    for (int top = n; top >= 0; top -= (int)blockDim.x) {
+        const int v = top - (int)threadIdx.x;
+        const int x = (v >= 1) ? v * hist[v] : 0;
+        // inclusive scan inside the block in thread order (= decreasing v)
+        int s = x;
+        for (int o = 1; o < 32; o <<= 1) {
+            int t = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += t;
+        }
+        if (lane == 31) warp_tot[warp] = s;
+        __syncthreads();
+        if (warp == 0) {
+            int wt = warp_tot[lane];
+            for (int o = 1; o < 32; o <<= 1) {
+                int t = __shfl_up_sync(0xffffffffu, wt, o);
+                if (lane >= o) wt += t;
+            }
+            warp_tot[lane] = wt;
+        }
+        __syncthreads();
+        const int before = carry + (warp > 0 ? warp_tot[warp - 1] : 0) + s - x;
+        if (v >= 0) base[v] = before;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += warp_tot[31];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) hdr->total = carry;
+    // stable ranks: warp 0 walks the chains in order
+    if (warp != 0) return;
+    int first = -1;
+    for (int i0 = 0; i0 < n; i0 += 32) {
+        const int i = i0 + lane;
+        const int c = (i < n) ? counts[i] : 0;
+        const unsigned peers = __match_any_sync(0xffffffffu, c);
+        const int leader = __ffs(peers) - 1;
+        const int rank = __popc(peers & ((1u << lane) - 1u));
+        int old = 0;
+        if (lane == leader && c > 0) {
+            if (c < kRankCache) { old = s_seen[c]; s_seen[c] = old + __popc(peers); }
+            else { old = seen[c]; seen[c] = old + __popc(peers); }
+        }
+        old = __shfl_sync(0xffffffffu, old, leader);
+        if (c > 0) {
+            const int st = base[c] + c * (old + rank);
+            start[i] = st;
+            if (st == 0) first = i;
+        } else if (i < n) {
+            start[i] = -1;
+        }
+        __syncwarp();
+    }
+    for (int o = 16; o > 0; o >>= 1) first = max(first, __shfl_xor_sync(0xffffffffu, first, o));
+    if (lane == 0) hdr->first_src = first;
+}
+
+__global__ void gather_kernel(int n, int p, const double* __restrict__ beta,
+                              const int* __restrict__ counts, const int* __restrict__ start,
+                              const ResampleHdr* __restrict__ hdr,
+                              const double* __restrict__ th_in, const double* __restrict__ pr_in,
+                              const double* __restrict__ da_in, double* __restrict__ th_out,
+                              double* __restrict__ pr_out, double* __restrict__ da_out,
+                              double* __restrict__ po_out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double b = *beta;
+    const int c = counts[i];
+    if (c > 0) {
+        const int s0 = start[i];
+        for (int k = 0; k < c; ++k) {
+            const int d = s0 + k;
+            for (int j = 0; j < p; ++j) th_out[(size_t)d * p + j] = th_in[(size_t)i * p + j];
+            pr_out[d] = pr_in[i];
+            da_out[d] = da_in[i];
+            po_out[d] = pr_in[i] + b * da_in[i];
+        }
+    }
+    // rows left over when uniforms fell beyond the last edge repeat the first group's row
+    const int d = i;
+    if (d >= hdr->total && hdr->first_src >= 0) {
+        const int src = hdr->first_src;
+        for (int j = 0; j < p; ++j) th_out[(size_t)d * p + j] = th_in[(size_t)src * p + j];
+        pr_out[d] = pr_in[src];
+        da_out[d] = da_in[src];
+        po_out[d] = pr_in[src] + b * da_in[src];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// scaling adaptation (Metropolis.py:262-281); then a new epoch
+__global__ void adapt_kernel(double aw, double rw, unsigned long long* __restrict__ counters,
+                             double* __restrict__ scaling, uint32_t* __restrict__ epoch) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const double acc = (double)counters[0];
+    const double tot = (double)(counters[0] + counters[1] + counters[2]);
+    const double acceptance = tot > 0.0 ? acc / tot : 0.0;
+    double kc = (aw * acceptance + rw) / (aw + rw);
+    if (kc < 0.1) kc = 0.1;
+    if (kc > 1.0) kc = 1.0;
+    *scaling = kc;
+    counters[0] = counters[1] = counters[2] = 0ull;
+    *epoch += 1u;
+}
+
+}  // namespace ag
+
+// ---------------------------------------------------------------------------
+// C ABI
+using namespace ag;
+
+static inline int blocks(int n, int t) { return (n + t - 1) / t; }
+
+static int check_state(const ag_stage_state* st) {
+    AG_REQUIRE(st && st->beta && st->dbeta_cov && st->scaling && st->sigma && st->chol && st->w &&
+                   st->counters && st->epoch && st->dev_flags,
+               "stage state has a NULL member");
+    return AG_OK;
+}
+
+extern "C" int ag_prior_sample(int32_t n, int32_t p, const double* lo, const double* hi,
+                               uint64_t seed, uint32_t attempt, const uint32_t* redraw,
+                               double* theta, void* stream) {
+    AG_REQUIRE(n > 0 && p > 0 && lo && hi && theta, "invalid arguments");
+    prior_sample_kernel<<<blocks(n, 256), 256, 0, as_stream(stream)>>>(n, p, lo, hi, seed, attempt,
+                                                                        redraw, theta);
+    return launch_status("prior_sample_kernel");
+}
+
+extern "C" int ag_prior_llk(const double* theta, int32_t n, int32_t p, const double* lo,
+                            const double* hi, uint32_t* mask, double* prior, void* stream) {
+    AG_REQUIRE(n > 0 && p > 0 && theta && lo && hi, "invalid arguments");
+    prior_llk_kernel<<<blocks(n, 256), 256, 0, as_stream(stream)>>>(theta, n, p, lo, hi, mask, prior);
+    return launch_status("prior_llk_kernel");
+}
+
+extern "C" int ag_propose(const ag_stage_state* st, const double* theta, int32_t n, int32_t p,
+                          const double* lo, const double* hi, uint64_t seed, uint32_t step,
+                          double* cand, uint32_t* mask, double* cprior, void* stream) {
+    int rc = check_state(st);
+    if (rc) return rc;
+    AG_REQUIRE(n > 0 && p > 0 && p <= kMaxP && theta && lo && hi && cand && mask && cprior,
+               "invalid arguments (p must be in 1..%d)", kMaxP);
+    propose_kernel<<<blocks(n, 128), 128, 0, as_stream(stream)>>>(theta, n, p, st->chol, lo, hi, seed,
+                                                                   step, st->epoch, cand, mask, cprior);
+    return launch_status("propose_kernel");
+}
+
+extern "C" int ag_accept(const ag_stage_state* st, int32_t n, int32_t p, uint64_t seed,
+                         uint32_t step, const uint32_t* mask, const double* cand,
+                         const double* cprior, const double* cdata, double* theta, double* prior,
+                         double* data, double* post, void* stream) {
+    int rc = check_state(st);
+    if (rc) return rc;
+    AG_REQUIRE(n > 0 && p > 0 && mask && cand && cprior && cdata && theta && prior && data && post,
+               "invalid arguments");
+    accept_kernel<<<blocks(n, 256), 256, 0, as_stream(stream)>>>(
+        n, p, st->beta, seed, step, st->epoch, mask, cand, cprior, cdata, theta, prior, data, post,
+        st->counters);
+    return launch_status("accept_kernel");
+}
+
+extern "C" int ag_posterior(const ag_stage_state* st, int32_t n, const double* prior,
+                            const double* data, double* post, void* stream) {
+    int rc = check_state(st);
+    if (rc) return rc;
+    AG_REQUIRE(n > 0 && prior && data && post, "invalid arguments");
+    posterior_kernel<<<blocks(n, 256), 256, 0, as_stream(stream)>>>(n, st->beta, prior, data, post);
+    return launch_status("posterior_kernel");
+}
+
+static size_t cov_part_offset() { return (sizeof(CovState) + 255) / 256 * 256; }
+
+extern "C" size_t ag_cov_workspace_bytes(int32_t n) {
+    if (n <= 0) return 0;
+    const size_t nblk = (size_t)blocks(n, kEvalChunk);
+    return cov_part_offset() + nblk * kGridPoints * 2 * sizeof(double);
+}
+
+extern "C" int ag_cov_schedule(const ag_stage_state* st, const double* data_llk, int32_t n,
+                               double target, double tol, void* workspace, size_t workspace_bytes,
+                               void* stream) {
+    int rc = check_state(st);
+    if (rc) return rc;
+    AG_REQUIRE(n > 1 && data_llk, "invalid arguments (need at least two chains)");
+    const size_t need = ag_cov_workspace_bytes(n);
+    AG_REQUIRE(workspace && workspace_bytes >= need && aligned(workspace, 256),
+               "ag_cov_schedule needs %zu bytes of 256-byte aligned workspace", need);
+    cudaStream_t s = as_stream(stream);
+    CovState* S = reinterpret_cast<CovState*>(workspace);
+    double* part = reinterpret_cast<double*>(static_cast<char*>(workspace) + cov_part_offset());
+    const int nblk = blocks(n, kEvalChunk);
+    cov_median_kernel<<<1, 1024, 0, s>>>(data_llk, n, st->beta, S);
+    for (int round = 0; round <= kGridLevels; ++round) {
+        cov_eval_kernel<<<dim3(nblk, kGridPoints), 256, 0, s>>>(data_llk, n, S, part);
+        cov_decide_kernel<<<1, 32, 0, s>>>(n, nblk, target, tol, part, S);
+    }
+    cov_final_sum_kernel<<<nblk, 256, 0, s>>>(data_llk, n, S, part);
+    cov_final_state_kernel<<<1, 32, 0, s>>>(n, nblk, part, S, st->beta, st->dbeta_cov);
+    cov_weights_kernel<<<blocks(n, 256), 256, 0, s>>>(data_llk, n, S, st->w);
+    return launch_status("cov schedule kernels");
+}
+
+extern "C" size_t ag_sigma_workspace_bytes(int32_t n, int32_t p) {
+    if (n <= 0 || p <= 0) return 0;
+    const size_t nent = 1 + p + (size_t)p * (p + 1) / 2;
+    return (size_t)blocks(n, kSigmaChunk) * nent * sizeof(double);
+}
+
+extern "C" int ag_weighted_cov(const ag_stage_state* st, const double* theta, int32_t n, int32_t p,
+                               void* workspace, size_t workspace_bytes, void* stream) {
+    int rc = check_state(st);
+    if (rc) return rc;
+    AG_REQUIRE(n > 0 && p > 0 && p <= kMaxP && theta, "invalid arguments (p <= %d)", kMaxP);
+    const size_t need = ag_sigma_workspace_bytes(n, p);
+    AG_REQUIRE(workspace && workspace_bytes >= need, "ag_weighted_cov needs %zu bytes", need);
+    cudaStream_t s = as_stream(stream);
+    const int nblk = blocks(n, kSigmaChunk);
+    const size_t smem = (size_t)kSigmaChunk * (p + 1) * sizeof(double);
+    if (smem > 48 * 1024) {
+        rc = cuda_status(cudaFuncSetAttribute(sigma_partial_kernel,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                         "cudaFuncSetAttribute(sigma_partial_kernel)");
+        if (rc) return rc;
+    }
+    double* part = reinterpret_cast<double*>(workspace);
+    sigma_partial_kernel<<<nblk, 256, smem, s>>>(theta, st->w, n, p, part);
+    sigma_final_kernel<<<1, 256, 0, s>>>(p, nblk, part, st->sigma);
+    return launch_status("weighted covariance kernels");
+}
+
+extern "C" int ag_cholesky_scaled(const ag_stage_state* st, int32_t p, void* stream) {
+    int rc = check_state(st);
+    if (rc) return rc;
+    AG_REQUIRE(p > 0 && p <= kMaxP, "p must be in 1..%d", kMaxP);
+    cholesky_kernel<<<1, 32, 0, as_stream(stream)>>>(p, st->sigma, st->scaling, st->chol, st->dev_flags);
+    return launch_status("cholesky_kernel");
+}
+
+// workspace layout: hdr | edges[n+1] | counts[n] (if not given) | hist[n+1] | base[n+1] | seen[n+1] | start[n]
+static size_t align256(size_t b) { return (b + 255) / 256 * 256; }
+extern "C" size_t ag_resample_workspace_bytes(int32_t n) {
+    if (n <= 0) return 0;
+    size_t b = align256(sizeof(ResampleHdr));
+    b += align256((size_t)(n + 1) * sizeof(double));
+    b += 5 * align256((size_t)(n + 1) * sizeof(int));
+    return b;
+}
+
+extern "C" int ag_resample(const ag_stage_state* st, int32_t n, int32_t p, uint64_t seed,
+                           const double* theta_in, const double* prior_in, const double* data_in,
+                           double* theta_out, double* prior_out, double* data_out, double* post_out,
+                           int32_t* counts, void* workspace, size_t workspace_bytes, void* stream) {
+    int rc = check_state(st);
+    if (rc) return rc;
+    AG_REQUIRE(n > 0 && p > 0 && theta_in && prior_in && data_in && theta_out && prior_out &&
+                   data_out && post_out,
+               "invalid arguments");
+    AG_REQUIRE(theta_in != theta_out, "resampling is out of place: theta_in == theta_out");
+    const size_t need = ag_resample_workspace_bytes(n);
+    AG_REQUIRE(workspace && workspace_bytes >= need && aligned(workspace, 256),
+               "ag_resample needs %zu bytes of 256-byte aligned workspace", need);
+    cudaStream_t s = as_stream(stream);
+    char* ws = static_cast<char*>(workspace);
+    ResampleHdr* hdr = reinterpret_cast<ResampleHdr*>(ws);
+    ws += align256(sizeof(ResampleHdr));
+    double* edges = reinterpret_cast<double*>(ws);
+    ws += align256((size_t)(n + 1) * sizeof(double));
+    const size_t ib = align256((size_t)(n + 1) * sizeof(int));
+    int* cnt_ws = reinterpret_cast<int*>(ws); ws += ib;
+    int* hist = reinterpret_cast<int*>(ws); ws += ib;
+    int* base = reinterpret_cast<int*>(ws); ws += ib;
+    int* seen = reinterpret_cast<int*>(ws); ws += ib;
+    int* start = reinterpret_cast<int*>(ws); ws += ib;
+    int* cnt = counts ? counts : cnt_ws;
+    rc = cuda_status(cudaMemsetAsync(cnt, 0, (size_t)n * sizeof(int), s), "memset counts");
+    if (rc) return rc;
+    rc = cuda_status(cudaMemsetAsync(hist, 0, (size_t)(n + 1) * sizeof(int), s), "memset hist");
+    if (rc) return rc;
+    rc = cuda_status(cudaMemsetAsync(seen, 0, (size_t)(n + 1) * sizeof(int), s), "memset seen");
+    if (rc) return rc;
+    cdf_kernel<<<1, 32, 0, s>>>(st->w, n, edges);
+    counts_kernel<<<blocks(n, 256), 256, 0, s>>>(n, seed, st->epoch, edges, cnt);
+    count_hist_kernel<<<blocks(n, 256), 256, 0, s>>>(n, cnt, hist);
+    rank_kernel<<<1, 1024, 0, s>>>(n, cnt, hist, base, seen, start, hdr);
+    gather_kernel<<<blocks(n, 128), 128, 0, s>>>(n, p, st->beta, cnt, start, hdr, theta_in, prior_in,
+                                                 data_in, theta_out, prior_out, data_out, post_out);
+    return launch_status("resample kernels");
+}
+
+extern "C" int ag_adapt_scaling(const ag_stage_state* st, double aw, double rw, void* stream) {
+    int rc = check_state(st);
+    if (rc) return rc;
+    adapt_kernel<<<1, 32, 0, as_stream(stream)>>>(aw, rw, st->counters, st->scaling, st->epoch);
+    return launch_status("adapt_kernel");
+}

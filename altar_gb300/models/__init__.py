@@ -1,0 +1,7 @@
+"""Model plugins (altar/altar/models, models/mogi, models/cdm)."""
+from .bayesian import Bayesian
+from .contiguous import Contiguous
+from .cdm import CDM
+from .mogi import Mogi
+
+__all__ = ["Bayesian", "Contiguous", "CDM", "Mogi"]

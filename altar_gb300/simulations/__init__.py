@@ -1,0 +1,6 @@
+"""Run configuration, random streams and output (altar/altar/simulations)."""
+from .job import Job
+from .rng import RNG
+from .recorder import Recorder
+
+__all__ = ["Job", "RNG", "Recorder"]

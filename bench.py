@@ -1,0 +1,369 @@
+#!/usr/bin/env python3
+"""Benchmark of the CATMIP hot path on the plain-CDM workload.
+
+Workload (CDM, single source): 40,000 LOS observations on a 200x200 grid over
+±20 km, LOS (0.38, -0.08, 0.92), diagonal Cd with σ = 3 mm, 10 parameters with
+the workload priors (x0, y0 ~ U[±10 km], depth ~ U[1, 10] km, rotations ~
+U[±90°], semi-axes ~ U[0.1, 3] km, opening ~ U[±50 m]), ν = 0.25, 32,768
+chains, 5 Metropolis steps per stage.  Synthetic data: a source drawn from the
+prior with a fixed seed (above-surface draws rejected) plus N(0, σ²) noise.
+
+A bench "step" is one Metropolis step of all chains (proposal + verify +
+fused CDM likelihood + accept); the metric is chain-steps per second.
+--mode anneal instead runs the whole annealing to β = 1 and reports the time.
+
+--impl reference times the CPU restatement of the reference algorithm
+(oracle/csrc/catmip_ref.c, FP64, all host cores) on a bounded chain sample.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+M_SIDE = 200
+SPAN = 20e3
+SIGMA = 3e-3
+LOS = (0.38, -0.08, 0.92)
+PRIORS = [(-1e4, 1e4), (-1e4, 1e4), (1e3, 1e4), (-50.0, 50.0), (100.0, 3000.0), (100.0, 3000.0),
+          (100.0, 3000.0), (-90.0, 90.0), (-90.0, 90.0), (-90.0, 90.0)]
+# parameter order: x0, y0, depth, opening, ax, ay, az, ωx, ωy, ωz
+# FP32 operations per (chain, station) pair of the fused CDM kernel, counted from
+# altar_gb300/csrc/forward.cu (FMA = 2): 225 per angular-dislocation pair side x 12
+# sides + 31 per station, excluding the bodies of the 24 log1pf and 12 atan2f calls
+CDM_FLOP_PER_PAIR = 2731
+L2_FLUSH_BYTES = 256 << 20
+
+
+def problem(seed=2024):
+    from oracle import cdm, cref
+    g = np.linspace(-SPAN, SPAN, M_SIDE)
+    X, Y = [a.ravel() for a in np.meshgrid(g, g)]
+    los = np.tile(LOS, (X.size, 1))
+    rng = np.random.default_rng(seed)
+    while True:
+        th = np.array([rng.uniform(*b) for b in PRIORS])
+        if not cdm.above_surface(th[0], th[1], th[2], *th[4:7], *th[7:10]):
+            break
+    lay = cref.RefLayout(10, 0, 2, 3, 4, 7, 0, 0.25)
+    u, bad = cref.cdm_los(th, lay, X, Y, los)
+    d = u + rng.normal(0.0, SIGMA, X.size)
+    return X, Y, los, d, th
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except OSError:
+        return {}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            self.proc.wait()
+
+    def summary(self):
+        rows = []
+        try:
+            for line in open(self.path):
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        except OSError:
+            pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_llk_rate(X, Y, los, d, chains, seed=7, threads=None):
+    """C restatement of the reference likelihood on the host cores: chain-steps/s."""
+    from oracle import cdm, cref
+    rng = np.random.default_rng(seed)
+    rows = []
+    while len(rows) < chains:                      # valid (below-surface) sources only
+        th = np.array([rng.uniform(*b) for b in PRIORS])
+        if not cdm.above_surface(th[0], th[1], th[2], *th[4:7], *th[7:10]):
+            rows.append(th)
+    theta = np.array(rows)
+    lay = cref.RefLayout(10, 0, 2, 3, 4, 7, 0, 0.25)
+    threads = threads or os.cpu_count() or 1
+    w = np.full(X.size, 1.0 / SIGMA ** 2)
+    cref.load()
+    t0 = time.perf_counter()
+    cref.llk(2, theta, lay, X, Y, los, d, w, 0.0, nthreads=threads)
+    dt = time.perf_counter() - t0
+    return chains / dt, threads, dt
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+        return rank, world, local, dist
+    return rank, world, local, None
+
+
+def run_reference(args):
+    # under torchrun only rank 0 measures; the CPU arm needs no process group
+    if int(os.environ.get("RANK", "0")) != 0:
+        return 0
+    X, Y, los, d, truth = problem()
+    chains = args.cpu_chains
+    rates, threads = [], os.cpu_count() or 1
+    for i in range(args.warmup + args.steps):
+        r, threads, dt = cpu_llk_rate(X, Y, los, d, chains, seed=100 + i, threads=threads)
+        if i >= args.warmup:
+            rates.append(dt)
+    tot = sum(rates)
+    value = chains * args.steps / tot
+    line = {
+        "impl": "reference", "metric": "CDM chain-steps/s", "value": value, "unit": "chain-steps/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "cdm-40k-obs", "chains": 32768, "stations": X.size, "steps_per_stage": 5,
+                   "parallelism": "host threads"},
+        "cpu_baseline": {"value": value, "unit": "chain-steps/s", "cores": threads, "kind": "port",
+                         "sample": f"{chains} chains x {X.size} stations per step, likelihood only "
+                                   "(FP64 C restatement of models/cdm/cdm/libcdm.py)"},
+        "e2e": {"value": value, "unit": "chain-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args):
+    import torch
+    rank, world, local, dist = dist_setup()
+    torch.cuda.set_device(local)
+    from altar_gb300 import Application, _native
+    from altar_gb300.device import ptr, stream_handle
+    from altar_gb300.distributions import Uniform
+    from altar_gb300.models import CDM, Contiguous
+    from altar_gb300.models.observations import Observations
+    from altar_gb300.simulations import RNG, Job
+
+    _native.load()
+    X, Y, los, d, truth = problem()
+    N = args.chains
+    names = ["location", "depth", "opening", "a", "omega"]
+    counts = [2, 1, 1, 3, 3]
+    bounds = [PRIORS[0], PRIORS[2], PRIORS[3], PRIORS[4], PRIORS[7]]
+    psets = {nm: Contiguous(c, Uniform(b)) for nm, c, b in zip(names, counts, bounds)}
+    model = CDM(psets, observations=Observations(X, Y, los, d, SIGMA ** 2))
+    app = Application(model, job=Job(chains=N, steps=5), rng=RNG(1234 + rank))
+    app.initialize()
+    ann = app.controller
+    worker = ann.worker
+    stream = worker.stream
+
+    if args.mode == "anneal":
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ann.posterior(model)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        reps = worker.reports
+        steps = sum(r["accepted"] + r["rejected"] + r["unlikely"] for r in reps)
+        line = {"metric": "CDM time-to-beta=1", "value": dt, "unit": "s", "n_gpus": world,
+                "stages": len(reps), "chain_steps": steps, "chain_steps_per_s": steps / dt,
+                "higher_is_better": False, "final_beta": reps[-1]["beta"] if reps else None,
+                "config": {"workload": "cdm-40k-obs", "chains": N, "stations": X.size, "steps_per_stage": 5}}
+        if rank == 0:
+            print(json.dumps(line))
+        return 0
+
+    samp = ann.sampler
+    with torch.cuda.stream(stream):
+        ann.model = model
+        worker.start(annealer=ann)
+        # one annealing stage brings the sample to β > 0 with a data-driven Σ
+        worker.cool(annealer=ann)
+        samp.prepareSamplingPDF(annealer=ann, step=worker.step)
+        step = worker.step
+        n, p = step.samples, step.parameters
+        cand, cprior, cdata, mask = samp._buffers(n, p)
+        st = step.state.struct
+
+        def mh_step(k):
+            s = stream_handle()
+            _native.call("ag_propose", st, ptr(step.theta), n, p, ptr(model.lo), ptr(model.hi), samp.seed, k,
+                         ptr(cand), ptr(mask), ptr(cprior), s)
+            model.strategy.forward(cand, cdata, mask=mask, status=mask)
+            _native.call("ag_accept", st, n, p, samp.seed, k, ptr(mask), ptr(cand), ptr(cprior), ptr(cdata),
+                         ptr(step.theta), ptr(step.prior), ptr(step.data), ptr(step.posterior), s)
+
+        mh_step(0)                                       # allocations happen eagerly
+        import ctypes
+        h = stream_handle()
+        _native.call("ag_graph_begin", h)
+        mh_step(1)
+        gexec = ctypes.c_void_p()
+        _native.call("ag_graph_end", h, ctypes.byref(gexec))
+        launch = lambda: _native.call("ag_graph_launch", gexec, stream_handle())
+        flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+
+        for _ in range(args.warmup):
+            launch()
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(args.steps)]
+        with ClockSampler(local) as clk:
+            torch.cuda.synchronize()
+            for a, b in evs:
+                flush.zero_()                            # L2 flush between timed iterations
+                a.record(stream)
+                launch()
+                b.record(stream)
+            torch.cuda.synchronize()
+        ms = [a.elapsed_time(b) for a, b in evs]
+        t_step = sum(ms) / len(ms) / 1e3
+        if dist is not None:
+            tt = torch.tensor([t_step], device="cuda")
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            t_step = float(tt.item())
+        value = world * N / t_step
+
+        # roofline: the fused forward kernel on every chain (no mask), CUDA events on its stream
+        th_all = step.theta.clone()
+        out = torch.empty(n, dtype=torch.float64, device="cuda")
+        model.strategy.forward(th_all, out)
+        fev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(3)]
+        for a, b in fev:
+            flush.zero_()
+            a.record(stream)
+            model.strategy.forward(th_all, out)
+            b.record(stream)
+        torch.cuda.synchronize()
+        t_fwd = sum(a.elapsed_time(b) for a, b in fev) / len(fev) / 1e3
+        pairs = n * X.size
+        achieved = pairs * CDM_FLOP_PER_PAIR / t_fwd / 1e12
+        pk = peaks()
+        sm_max = float(pk.get("sm_max_mhz", 2070.0))
+        fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12   # FMA lanes x 2 FLOP x max SM clock
+
+        # end to end through host buffers: θ and the three log-likelihood vectors in and out
+        host = [torch.empty_like(t, device="cpu").pin_memory() for t in (step.theta, step.prior, step.data,
+                                                                          step.posterior)]
+        for hh, t in zip(host, (step.theta, step.prior, step.data, step.posterior)):
+            hh.copy_(t)
+        torch.cuda.synchronize()
+        e2e_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                  for _ in range(args.steps)]
+        for a, b in e2e_ev:
+            flush.zero_()
+            a.record(stream)
+            for hh, t in zip(host, (step.theta, step.prior, step.data, step.posterior)):
+                t.copy_(hh, non_blocking=True)
+            launch()
+            for hh, t in zip(host, (step.theta, step.prior, step.data, step.posterior)):
+                hh.copy_(t, non_blocking=True)
+            b.record(stream)
+        torch.cuda.synchronize()
+        t_e2e = sum(a.elapsed_time(b) for a, b in e2e_ev) / len(e2e_ev) / 1e3
+        io_bytes = sum(t.numel() * t.element_size() for t in host)
+    _native.load().ag_graph_destroy(gexec)
+
+    if rank != 0:
+        return 0
+    cpu_rate, cores, cpu_dt = cpu_llk_rate(X, Y, los, d, args.cpu_chains)
+    profile_traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            profile_traffic = json.load(f).get("cdm_llk_kernel_bytes_per_launch")
+    except OSError:
+        pass
+    line = {
+        "metric": "CDM chain-steps/s", "value": value, "unit": "chain-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "cdm-40k-obs", "chains": N, "stations": X.size, "params": 10,
+                   "steps_per_stage": 5, "parallelism": "replicas" if world > 1 else "single-gpu",
+                   "l2": "flushed (256 MB write) between timed iterations", "graph": "one CUDA graph per step"},
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": achieved / fp32_peak, "traffic": profile_traffic,
+                     "kernel": "cdm_setup_kernel + cdm_llk_kernel", "flop_per_pair": CDM_FLOP_PER_PAIR,
+                     "pairs_per_launch": pairs, "ms_per_launch": t_fwd * 1e3,
+                     "peak_source": "nominal FP32 FMA rate at the measured max SM clock "
+                                    "(MEASURED_PEAKS.json has no FP32 figure)"},
+        "e2e": {"value": world * N / t_e2e, "unit": "chain-steps/s", "h2d_bytes_per_step": io_bytes,
+                "d2h_bytes_per_step": io_bytes},
+        "gpu_launches": 4 * args.steps,
+        "cpu_baseline": {"value": cpu_rate, "unit": "chain-steps/s", "cores": cores, "kind": "port",
+                         "sample": f"{args.cpu_chains} chains x {X.size} stations, likelihood only, "
+                                   f"{cpu_dt:.1f} s (FP64 C restatement of models/cdm/cdm/libcdm.py)"},
+        "clocks": clk.summary(),
+        "pair_evals_per_s": value * X.size,
+    }
+    print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--mode", default="walk", choices=["walk", "anneal"])
+    ap.add_argument("--chains", type=int, default=32768)
+    ap.add_argument("--cpu-chains", type=int, default=128)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,244 @@
+/*
+ * altar_gb300: C ABI of the GB300 (sm_103a) CATMIP hot path.
+ *
+ * Every pointer argument is a DEVICE pointer owned by the caller unless the
+ * comment says otherwise; the library allocates nothing and keeps no global
+ * mutable state apart from a per-thread error string.  Every call is
+ * asynchronous on the given stream (a cudaStream_t passed as void*, NULL =
+ * legacy default stream) and returns AG_OK or an error code; the message of
+ * the last error of the calling thread is available from ag_last_error().
+ *
+ * Array layouts:
+ *   theta    N x p row-major FP64 (chain-major), as the reference's θ
+ *            (altar/altar/bayesian/CoolingStep.py:25)
+ *   vectors  FP64 length-N prior / data / posterior log-likelihoods
+ *   sigma    p x p row-major FP64; chol: lower-triangular p x p row-major
+ */
+#ifndef ALTAR_GB300_H
+#define ALTAR_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define AG_OK 0
+#define AG_ERR_ARG 1      /* invalid argument (null pointer, bad size, bad layout) */
+#define AG_ERR_CUDA 2     /* a CUDA runtime call failed */
+#define AG_ERR_DEVICE 3   /* a kernel raised a device flag (timeout, non-SPD pivot) */
+#define AG_ERR_SIZE 4     /* a size exceeds what the entry point supports */
+
+/* forward models */
+#define AG_MODEL_MOGI 1
+#define AG_MODEL_CDM 2
+
+/* per-chain status bits written by the forward models and the proposal */
+#define AG_CHAIN_OUT_OF_SUPPORT 1u  /* outside the prior support (Uniform.verify) */
+#define AG_CHAIN_ABOVE_SURFACE 2u   /* CDM reaches above the free surface */
+#define AG_CHAIN_NONFINITE 4u       /* non-finite log-likelihood */
+
+/* device error flags (ag_stage_state.dev_flags) */
+#define AG_DEV_ERR_TIMEOUT 1u
+#define AG_DEV_ERR_NOT_SPD 2u
+
+/* Station arrays: padded to a multiple of AG_STATION_TILE entries; padding
+ * entries carry weight 0 and contribute nothing. */
+#define AG_STATION_TILE 128
+
+/*
+ * Observation points of one or more concatenated datasets.
+ * Replaces the per-source state the reference attaches through
+ * libcudacdm.locations / los / data / oid (models/cdm/ext/cudacdm/source.cc:155,235,90,304)
+ * and the Mogi equivalents (models/mogi/ext/cudamogi/source.cc).
+ */
+typedef struct ag_station_set {
+    const float* xy;       /* [m_padded][4]: x_hi, x_lo, y_hi, y_lo; x = x_hi + x_lo (m) */
+    const float* losd;     /* [m_padded][4]: LOS east, north, up; observed LOS displacement (m) */
+    const float* weight;   /* [m_padded]: 1/σ² of each observation (diagonal Cd), 0 for padding */
+    const int32_t* oid;    /* [m_padded]: dataset id, selects θ[offset_idx + oid]; NULL = none */
+    int32_t m;             /* number of observations */
+    int32_t m_padded;      /* multiple of AG_STATION_TILE */
+} ag_station_set;
+
+/*
+ * Parameter layout of a sample row.  Replaces libcudacdm.layout
+ * (models/cdm/ext/cudacdm/source.cc:378: xIdx, dIdx, openingIdx, aXIdx,
+ * omegaXIdx, offsetIdx) and libcudamogi.layout
+ * (models/mogi/ext/cudamogi/source.cc:378: xIdx, dIdx, sIdx, offsetIdx).
+ */
+typedef struct ag_layout {
+    int32_t nparams;        /* row stride of θ (p) */
+    int32_t x_idx;          /* east coordinate of the (first) source; north is x_idx + 1 */
+    int32_t depth_idx;      /* depth, positive down (m) */
+    int32_t strength_idx;   /* Mogi: volume change; CDM: opening (m) */
+    int32_t axes_idx;       /* CDM: semi-axes ax, ay, az at axes_idx .. axes_idx + 2 */
+    int32_t omega_idx;      /* CDM: clockwise rotations about x, y, z in degrees */
+    int32_t offset_idx;     /* first per-dataset offset parameter; -1 = none */
+    int32_t log_strength;   /* Mogi: 1 = θ holds log10(ΔV) as in the reference, 0 = ΔV */
+    int32_t nsources;       /* Mogi: number of point sources (>= 1) */
+    int32_t source_stride;  /* Mogi: parameter distance between consecutive sources */
+    double nu;              /* Poisson ratio */
+} ag_layout;
+
+/* Last error message of the calling thread (NUL-terminated, truncated to len). */
+int ag_last_error(char* buf, size_t len);
+
+/* Library version string (static storage, host pointer). */
+const char* ag_version(void);
+
+/*
+ * Bytes of caller-provided device workspace the forward model needs for n chains.
+ */
+size_t ag_forward_workspace_bytes(int model, int32_t n);
+
+/*
+ * Fused batched forward model + residual + diagonal-Cd whitening + FP64
+ * per-chain data log-likelihood:
+ *     llk[i] = norm - 1/2 * sum_j w_j * (u_j(θ_i) - d_j - θ_i[offset_idx + oid_j])^2
+ * with u the LOS-projected Mogi (models/mogi/lib/libmogi/Source.cc:65-118) or
+ * CDM (models/cdm/cdm/libcdm.py:39-247, cdm/Source.py:48-91) displacement.
+ * Replaces libcudamogi.residuals / libcudacdm.residuals plus the per-chain
+ * L2.withCovariance loop (models/cdm/cdm/CUDA.py:71-107, altar/altar/norms/L2.py:39-52)
+ * for diagonal Cd.
+ *   mask_in:    optional; chains with a non-zero word are skipped (llk untouched)
+ *   chain_status: optional; receives AG_CHAIN_* bits (CDM geometry check)
+ *   residuals:  optional N x m_padded FP32 output of the residuals (tests)
+ *   workspace:  ag_forward_workspace_bytes(model, n) bytes, 256-byte aligned
+ */
+int ag_forward_llk(int model, const ag_layout* layout, const double* theta, int32_t n,
+                   const ag_station_set* stations, double norm, const uint32_t* mask_in,
+                   double* llk, uint32_t* chain_status, float* residuals,
+                   void* workspace, size_t workspace_bytes, void* stream);
+
+/*
+ * CDM geometry check only: chain_status[i] |= AG_CHAIN_ABOVE_SURFACE where a
+ * corner of the CDM lies above the free surface (models/cdm/cdm/libcdm.py:219-224).
+ */
+int ag_cdm_check(const ag_layout* layout, const double* theta, int32_t n,
+                 uint32_t* chain_status, void* stream);
+
+/*
+ * Initial sample from independent Uniform[lo_j, hi_j) priors
+ * (altar/altar/distributions/Base.py:44-54 with Uniform.py), drawn from
+ * Philox stream PRIOR at counter (chain, j, attempt).  Only rows whose
+ * redraw[i] != 0 are drawn when redraw is non-NULL.
+ */
+int ag_prior_sample(int32_t n, int32_t p, const double* lo, const double* hi, uint64_t seed,
+                    uint32_t attempt, const uint32_t* redraw, double* theta, void* stream);
+
+/*
+ * Uniform prior: mask[i] |= AG_CHAIN_OUT_OF_SUPPORT if some θ_ij is outside
+ * [lo_j, hi_j] (altar/altar/distributions/Uniform.py:45-72) and
+ * prior[i] = -sum_j log(hi_j - lo_j) (altar/altar/distributions/Base.py:61-79).
+ */
+int ag_prior_llk(const double* theta, int32_t n, int32_t p, const double* lo, const double* hi,
+                 uint32_t* mask, double* prior, void* stream);
+
+/*
+ * Device-resident annealing state shared by the stage kernels.
+ */
+typedef struct ag_stage_state {
+    double* beta;          /* [1] current β */
+    double* dbeta_cov;     /* [2] last δβ and the COV it achieved */
+    double* scaling;       /* [1] Metropolis proposal scaling */
+    double* sigma;         /* [p*p] parameter covariance Σ */
+    double* chol;          /* [p*p] lower Cholesky factor of scaling² Σ */
+    double* w;             /* [N] normalised importance weights */
+    unsigned long long* counters; /* [3] accepted, rejected, unlikely of the current stage */
+    uint32_t* epoch;       /* [1] stage counter feeding the random streams */
+    uint32_t* dev_flags;   /* [1] AG_DEV_ERR_* bits */
+} ag_stage_state;
+
+/*
+ * Metropolis proposal + Uniform verify + prior (altar/altar/bayesian/Metropolis.py:160-183,236-259):
+ *   cand = θ + (L z)ᵀ, z ~ N(0, I) (Philox stream PROPOSAL, Box-Muller);
+ *   rows outside the support are flagged in mask and replaced by θ;
+ *   cprior = uniform log prior of cand.
+ */
+int ag_propose(const ag_stage_state* st, const double* theta, int32_t n, int32_t p,
+               const double* lo, const double* hi, uint64_t seed, uint32_t step,
+               double* cand, uint32_t* mask, double* cprior, void* stream);
+
+/*
+ * Metropolis accept/reject (altar/altar/bayesian/Metropolis.py:185-223):
+ *   cpost = cprior + β cdata; rejected if mask, unlikely if log(u) > cpost - post
+ *   (u ~ U(0,1], Philox stream ACCEPT), else θ, prior, data, post take the candidate's.
+ *   Counters accumulate into st->counters.
+ */
+int ag_accept(const ag_stage_state* st, int32_t n, int32_t p, uint64_t seed, uint32_t step,
+              const uint32_t* mask, const double* cand, const double* cprior, const double* cdata,
+              double* theta, double* prior, double* data, double* post, void* stream);
+
+/*
+ * Bytes of workspace ag_cov_schedule needs for n chains.
+ */
+size_t ag_cov_workspace_bytes(int32_t n);
+
+/*
+ * COV β schedule with the iterative grid solver
+ * (altar/altar/bayesian/COV.py:91-102, Grid.py:48-59, altar/lib/libaltar/bayesian/COV.cc:222-368):
+ * median of data llk, 11-point grid refinement of δβ until COV(w) hits
+ * target within tol, β += δβ, w normalised importance weights at the final δβ.
+ */
+int ag_cov_schedule(const ag_stage_state* st, const double* data_llk, int32_t n,
+                    double target, double tol, void* workspace, size_t workspace_bytes,
+                    void* stream);
+
+/* Bytes of workspace ag_weighted_cov needs. */
+size_t ag_sigma_workspace_bytes(int32_t n, int32_t p);
+
+/*
+ * Weighted parameter covariance (altar/altar/bayesian/COV.py:106-156):
+ * θ̄ = Σ w θ / Σ w, Σ = Σ w θ θᵀ - θ̄ θ̄ᵀ, into st->sigma.
+ */
+int ag_weighted_cov(const ag_stage_state* st, const double* theta, int32_t n, int32_t p,
+                    void* workspace, size_t workspace_bytes, void* stream);
+
+/*
+ * chol = Cholesky(scaling² Σ) (altar/altar/bayesian/Metropolis.py:93-111);
+ * a non-positive pivot raises AG_DEV_ERR_NOT_SPD in st->dev_flags.
+ */
+int ag_cholesky_scaled(const ag_stage_state* st, int32_t p, void* stream);
+
+/* Bytes of workspace ag_resample needs. */
+size_t ag_resample_workspace_bytes(int32_t n);
+
+/*
+ * Multinomial resampling (altar/altar/bayesian/COV.py:160-251):
+ * edges = [0, cumsum(w)] accumulated sequentially in FP64, r_j ~ U[0,1)
+ * (Philox stream RESAMPLE), counts[i] = #{j : edges_i <= r_j < edges_{i+1}}
+ * (values >= the last edge are dropped, as gsl_histogram does), rows copied
+ * in order of decreasing count (ties by increasing index), each count times;
+ * rows left over when some r_j were dropped repeat the first copied row.
+ * posterior_out = prior + β data.  counts (optional, N ints) receives the counts.
+ */
+int ag_resample(const ag_stage_state* st, int32_t n, int32_t p, uint64_t seed,
+                const double* theta_in, const double* prior_in, const double* data_in,
+                double* theta_out, double* prior_out, double* data_out, double* post_out,
+                int32_t* counts, void* workspace, size_t workspace_bytes, void* stream);
+
+/*
+ * Proposal scaling adaptation (altar/altar/bayesian/Metropolis.py:262-281):
+ * kc = (aw·acc + rw)/(aw + rw) clamped to [0.1, 1], acc = accepted/total;
+ * then clears the counters and advances the epoch.
+ */
+int ag_adapt_scaling(const ag_stage_state* st, double aw, double rw, void* stream);
+
+/* posterior = prior + β data (altar/altar/models/Bayesian.py:105-115). */
+int ag_posterior(const ag_stage_state* st, int32_t n, const double* prior, const double* data,
+                 double* post, void* stream);
+
+/* CUDA graph capture of a sequence of calls on one stream. */
+int ag_graph_begin(void* stream);
+int ag_graph_end(void* stream, void** graph_exec);
+int ag_graph_launch(void* graph_exec, void* stream);
+int ag_graph_destroy(void* graph_exec);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ALTAR_GB300_H */

@@ -1,0 +1,237 @@
+"""FP64 restatement of the CATMIP loop and the Mogi / Gaussian pieces it drives.
+
+Oracle only (test infrastructure).  Each function cites the reference lines
+it restates.  Where the reference relies on GSL (RNG streams, histogram
+binning order, heap-sort tie order, Brent iterates) parity is unpinned: the
+random draws come from ``oracle.philox`` (the device's own streams) and ties
+in the resampling order are broken by increasing index, as on the device.
+"""
+import math
+
+import numpy as np
+
+from . import philox
+
+
+# --------------------------------------------------------------------------- forward models
+def mogi_los(theta, x, y, los, nu, x_idx=0, depth_idx=2, strength_idx=3, log_strength=True,
+             nsources=1, stride=0):
+    """LOS displacement of Mogi point sources, (N, M) (models/mogi/lib/libmogi/Source.cc:65-118)."""
+    theta = np.atleast_2d(np.asarray(theta, dtype=np.float64))
+    u = np.zeros((theta.shape[0], np.size(x)))
+    for s in range(nsources):
+        o = s * stride
+        xs = theta[:, x_idx + o, None]
+        ys = theta[:, x_idx + 1 + o, None]
+        d = theta[:, depth_idx + o, None]
+        sv = theta[:, strength_idx + o, None]
+        dv = 10.0 ** sv if log_strength else sv
+        dx = xs - np.asarray(x)[None, :]
+        dy = ys - np.asarray(y)[None, :]
+        R = np.sqrt(dx * dx + dy * dy + d * d)
+        C = (nu - 1.0) * dv / math.pi
+        u += (dx * los[None, :, 0] + dy * los[None, :, 1] - d * los[None, :, 2]) * C / R ** 3
+    return u
+
+
+def diag_llk(pred, d, variance, offsets=None, oid=None):
+    """norm - 1/2 Σ r²/σ² with r = pred - d - offset (Native.py:176-186, L2.py:39-52, diagonal Cd)."""
+    r = np.asarray(pred) - np.asarray(d)[None, :]
+    if offsets is not None:
+        r = r - offsets[:, oid]
+    var = np.broadcast_to(np.asarray(variance, dtype=np.float64), r.shape[1:])
+    norm = -0.5 * (var.size * math.log(2.0 * math.pi) + float(np.sum(np.log(var))))
+    return norm - 0.5 * np.sum(r * r / var[None, :], axis=1), r
+
+
+def llk_from_residuals(resid, weight, norm):
+    """FP64 log-likelihood of given residuals: norm - 1/2 Σ w r² (exactly summed)."""
+    r = np.asarray(resid, dtype=np.float64)
+    w = np.asarray(weight, dtype=np.float64)
+    return norm - 0.5 * np.sum(r * r * w[None, :], axis=1)
+
+
+# --------------------------------------------------------------------------- prior
+def uniform_verify(theta, lo, hi):
+    """Out-of-support mask (altar/altar/distributions/Uniform.py:45-72, closed interval)."""
+    return np.any((theta < lo[None, :]) | (theta > hi[None, :]), axis=1)
+
+
+def uniform_log_prior(theta, lo, hi):
+    """Σ_j log(1/(hi_j - lo_j)) (altar/altar/distributions/Base.py:61-79)."""
+    return np.full(theta.shape[0], -float(np.sum(np.log(hi - lo))))
+
+
+def prior_sample(seed, n, lo, hi, attempt=0):
+    """gsl_ran_flat draws a(1-u) + b u on the PRIOR stream."""
+    u = philox.prior_uniforms(seed, n, lo.size, attempt)
+    return lo[None, :] * (1.0 - u) + hi[None, :] * u
+
+
+# --------------------------------------------------------------------------- COV schedule
+def cov_of(dbeta, llk, median):
+    """COV of the normalised weights (altar/lib/libaltar/bayesian/COV.cc:335-368)."""
+    with np.errstate(over="ignore", invalid="ignore", divide="ignore"):
+        w = np.exp(dbeta * (llk - median))
+        wsum = w.size * np.mean(w)
+        w = w / wsum
+        mean = np.mean(w)
+        sd = np.sqrt(np.sum((w - mean) ** 2) / (w.size - 1))
+        cov = sd / mean
+    if not np.isfinite(cov):
+        return 1e100, w
+    return float(cov), w
+
+
+def median_gsl(llk):
+    """gsl_stats_median_from_sorted_data of the sorted vector (Grid.py:57)."""
+    s = np.sort(llk)
+    n = s.size
+    return s[(n - 1) // 2] if n % 2 else (s[(n - 1) // 2] + s[n // 2]) / 2.0
+
+
+def dbeta_grid(llk, beta, target=1.0, tol=0.01):
+    """Iterative grid δβ search (COV.cc:222-326). Returns (new β, δβ, cov, w)."""
+    median = median_gsl(llk)
+    low, high = 0.0, 1.0 - beta
+    cov, w = cov_of(high, llk, median)
+    if cov < target or abs(cov - target) < tol:
+        return 1.0, high, cov, w
+    nb_max = 10
+    nloop = 0
+    found = False
+    guess = 0.0
+    while True:
+        nloop += 1
+        step = (high - low) / nb_max
+        guess = low
+        nb = 0
+        while nb <= nb_max:
+            c, _ = cov_of(guess, llk, median)
+            if abs(c - target) < tol:
+                found = True
+                break
+            if c >= target:
+                if nb == 0:
+                    found = True
+                break
+            guess += step
+            nb += 1
+        if nb > nb_max:
+            guess -= step
+        high = guess
+        low = guess - step
+        if not (nloop <= nb_max and not found):
+            break
+    cov, w = cov_of(guess, llk, median)
+    return beta + guess, guess, cov, w
+
+
+# --------------------------------------------------------------------------- covariance and resampling
+def weighted_cov(theta, w):
+    """θ̄ = Σwθ/Σw; Σ = Σ w θθᵀ - θ̄θ̄ᵀ (altar/altar/bayesian/COV.py:106-156)."""
+    mean = (w[:, None] * theta).sum(0) / w.sum()
+    S = (w[:, None, None] * theta[:, :, None] * theta[:, None, :]).sum(0)
+    return S - np.outer(mean, mean)
+
+
+def cdf_edges(w):
+    """[0, w0, w0+w1, ...] accumulated sequentially (COV.py:242-251)."""
+    e = np.empty(w.size + 1)
+    e[0] = 0.0
+    acc = 0.0
+    for i, v in enumerate(w.tolist()):
+        acc += v
+        e[i + 1] = acc
+    return e
+
+
+def multiplicities(w, r):
+    """gsl histogram counts of r over the CDF bins; r >= last edge dropped (COV.py:222-239)."""
+    e = cdf_edges(w)
+    idx = np.searchsorted(e, r, side="right") - 1
+    ok = (r >= e[0]) & (r < e[-1])
+    counts = np.zeros(w.size, dtype=np.int64)
+    np.add.at(counts, idx[ok], 1)
+    return counts
+
+
+def rank_order(counts):
+    """Row sources of the resampled set: decreasing count, ties by increasing index (COV.py:181-206)."""
+    order = sorted(range(counts.size), key=lambda i: (-counts[i], i))
+    src = [i for i in order for _ in range(int(counts[i]))]
+    while len(src) < counts.size:          # dropped uniforms: repeat the first row
+        src.append(src[0])
+    return np.array(src, dtype=np.int64)
+
+
+# --------------------------------------------------------------------------- Metropolis
+def cholesky_scaled(sigma, scaling):
+    return np.linalg.cholesky(scaling * scaling * sigma)
+
+
+def adapt_scaling(accepted, rejected, unlikely, aw=8.0, rw=1.0):
+    """kc = (aw acc + rw)/(aw + rw) in [0.1, 1] (altar/altar/bayesian/Metropolis.py:262-281)."""
+    acc = accepted / (accepted + rejected + unlikely)
+    return min(1.0, max(0.1, (aw * acc + rw) / (aw + rw)))
+
+
+class Annealing:
+    """The CATMIP loop (altar/altar/bayesian/Annealer.py:79-135) for a data-llk function.
+
+    ``data_llk(theta) -> (llk, invalid_mask)``.  Draws use the device's Philox
+    streams, so with identical inputs the oracle and the GPU make the same
+    random choices up to floating-point ties.
+    """
+
+    def __init__(self, data_llk, lo, hi, chains, steps=5, seed=0, tolerance=1e-3, target=1.0,
+                 grid_tol=0.01, scaling=0.1):
+        self.data_llk, self.lo, self.hi = data_llk, np.asarray(lo, float), np.asarray(hi, float)
+        self.n, self.p, self.steps, self.seed = chains, self.lo.size, steps, seed
+        self.tolerance, self.target, self.grid_tol, self.scaling0 = tolerance, target, grid_tol, scaling
+
+    def initial(self, max_attempts=1000):
+        theta = prior_sample(self.seed, self.n, self.lo, self.hi)
+        for attempt in range(1, max_attempts + 1):
+            llk, bad = self.data_llk(theta)
+            if not np.any(bad):
+                return theta, llk
+            redo = prior_sample(self.seed, self.n, self.lo, self.hi, attempt)
+            theta[bad] = redo[bad]
+        raise RuntimeError("no valid initial sample")
+
+    def run(self, max_stages=1000):
+        n, p = self.n, self.p
+        theta, data = self.initial()
+        prior = uniform_log_prior(theta, self.lo, self.hi)
+        beta, scaling, epoch = 0.0, self.scaling0, 0
+        post = prior + beta * data
+        stages = []
+        while beta + self.tolerance < 1 and len(stages) < max_stages:
+            beta, dbeta, cov, w = dbeta_grid(data, beta, self.target, self.grid_tol)
+            sigma = weighted_cov(theta, w)
+            counts = multiplicities(w, philox.resample_uniforms(self.seed, n, epoch))
+            src = rank_order(counts)
+            theta, prior, data = theta[src].copy(), prior[src].copy(), data[src].copy()
+            post = prior + beta * data
+            L = cholesky_scaled(sigma, scaling)
+            acc = rej = unl = 0
+            for k in range(self.steps):
+                z = philox.proposal_normals(self.seed, n, p, k, epoch)
+                cand = theta + z @ L.T
+                bad = uniform_verify(cand, self.lo, self.hi)
+                cand[bad] = theta[bad]
+                cprior = uniform_log_prior(cand, self.lo, self.hi)
+                cdata, invalid = self.data_llk(cand)
+                bad = bad | invalid
+                cpost = cprior + beta * cdata
+                u = philox.accept_uniforms(self.seed, n, k, epoch)
+                unlikely = ~bad & (np.log(u) > cpost - post)
+                ok = ~bad & ~unlikely
+                theta[ok], prior[ok], data[ok], post[ok] = cand[ok], cprior[ok], cdata[ok], cpost[ok]
+                acc += int(ok.sum()); rej += int(bad.sum()); unl += int(unlikely.sum())
+            scaling = adapt_scaling(acc, rej, unl)
+            epoch += 1
+            stages.append(dict(beta=beta, dbeta=dbeta, cov=cov, accepted=acc, rejected=rej,
+                               unlikely=unl, scaling=scaling))
+        return dict(theta=theta, prior=prior, data=data, posterior=post, beta=beta, stages=stages)

@@ -1,0 +1,199 @@
+"""Forward models + misfit on the GPU against the oracle and the reference fixtures.
+
+Tolerances (FP32 device arithmetic against FP64 references):
+  * CDM LOS displacement, per source, normwise: |u_gpu - u_ref|_inf <= TOL_CDM * |u_ref|_inf
+    for sources whose sides all lie at least 10° from the vertical; near-vertical sides
+    lose accuracy in the angular-dislocation formula itself (terms ~cot²β cancel) and are
+    checked with the looser TOL_CDM_STEEP.  The median error over sources must stay
+    below TOL_CDM_MEDIAN.
+  * Mogi LOS displacement: normwise 1e-5.
+  * log-likelihood given the device's own FP32 residuals: 1e-9 relative (FP64 oracle sum).
+"""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from altar_gb300 import _native
+from oracle import catmip, cdm
+
+from gpu_helpers import (LOS, cdm_los_oracle, cdm_prior_rows, cdm_strategy, dev, min_vertical_angle,
+                         mogi_strategy)
+
+pytestmark = pytest.mark.gpu
+
+TOL_CDM = 1e-4
+TOL_CDM_MEDIAN = 5e-6
+TOL_CDM_STEEP = 5e-2
+G = np.load(os.path.join(os.path.dirname(__file__), "golden", "cdm_golden.npz"))
+
+
+def _residuals(strategy, theta, m):
+    n = theta.shape[0]
+    out = torch.empty(n, dtype=torch.float64, device="cuda")
+    res = torch.zeros(n, strategy.stations.m_padded, dtype=torch.float32, device="cuda")
+    strategy.forward(dev(theta), out, residuals=res)
+    torch.cuda.synchronize()
+    return out.cpu().numpy(), res.cpu().numpy()[:, :m]
+
+
+def _fixture_theta():
+    # fixture rows: x, y, depth, ax, ay, az, ωx, ωy, ωz, opening, ν
+    s = G["ref_src"]
+    return np.stack([s[:, 0], s[:, 1], s[:, 2], s[:, 9], s[:, 3], s[:, 4], s[:, 5], s[:, 6], s[:, 7],
+                     s[:, 8]], 1)
+
+
+def test_cdm_matches_reference_fixtures(cuda):
+    X, Y = G["ref_X"], G["ref_Y"]
+    los = np.tile(LOS, (X.size, 1))
+    theta = _fixture_theta()
+    strat, _ = cdm_strategy(X, Y, los, np.zeros(X.size), np.full(X.size, 9e-6))
+    _, res = _residuals(strat, theta, X.size)
+    errs = []
+    for k, u in enumerate(G["ref_u"]):
+        ref = u[0] * LOS[0] + u[1] * LOS[1] + u[2] * LOS[2]
+        err = np.max(np.abs(res[k] - ref)) / np.max(np.abs(ref))
+        steep = min_vertical_angle(theta[k]) < 10.0
+        assert err <= (TOL_CDM_STEEP if steep else TOL_CDM), (k, err)
+        errs.append(err)
+    assert np.median(errs) <= TOL_CDM_MEDIAN
+
+
+def test_cdm_matlab_goldens(cuda):
+    """Matlab test source at the 12 golden points (models/cdm/tests/libcdm.py:27-46)."""
+    X, Y = G["matlab_X"] * 1e3, G["matlab_Y"] * 1e3        # km -> m keeps FP32 in range
+    s = G["matlab_src"]
+    th = np.array([[s[0] * 1e3, s[1] * 1e3, s[2] * 1e3, s[9] * 1e3, s[3] * 1e3, s[4] * 1e3, s[5] * 1e3,
+                    s[6], s[7], s[8]]])
+    for comp, los in (("matlab_ue", [1.0, 0, 0]), ("matlab_un", [0, 1.0, 0]), ("matlab_uv", [0, 0, 1.0])):
+        strat, _ = cdm_strategy(X, Y, np.tile(los, (12, 1)), np.zeros(12), np.ones(12))
+        _, res = _residuals(strat, th, 12)
+        ref = G[comp] * 1e3                                 # displacement scales with length
+        assert np.max(np.abs(res[0] - ref)) <= 1e-5 * np.max(np.abs(ref)), comp
+
+
+def test_cdm_prior_sources_workload_grid(cuda):
+    """64 prior sources on a subsampled 200x200 ±20 km grid against the FP64 oracle."""
+    g = np.linspace(-20e3, 20e3, 200)[::5]
+    X, Y = [a.ravel() for a in np.meshgrid(g, g)]
+    los = np.tile(LOS, (X.size, 1))
+    theta = cdm_prior_rows(64, seed=11)
+    ref = cdm_los_oracle(theta, X, Y, los)
+    strat, _ = cdm_strategy(X, Y, los, np.zeros(X.size), np.full(X.size, 9e-6))
+    _, res = _residuals(strat, theta, X.size)
+    errs = np.max(np.abs(res - ref), 1) / np.max(np.abs(ref), 1)
+    steep = np.array([min_vertical_angle(t) < 10.0 for t in theta])
+    assert np.all(errs[~steep] <= TOL_CDM), errs[~steep].max()
+    assert np.all(errs[steep] <= TOL_CDM_STEEP)
+    assert np.median(errs) <= TOL_CDM_MEDIAN
+    print(f"CDM normwise error: median {np.median(errs):.2e}, max (>=10deg) {errs[~steep].max():.2e}")
+
+
+def test_cdm_llk_given_residuals(cuda):
+    rng = np.random.default_rng(2)
+    g = np.linspace(-20e3, 20e3, 40)
+    X, Y = [a.ravel() for a in np.meshgrid(g, g)]
+    los = np.tile(LOS, (X.size, 1))
+    theta = cdm_prior_rows(32, seed=5)
+    truth = cdm_los_oracle(theta[:1], X, Y, los)[0]
+    d = truth + rng.normal(0, 3e-3, X.size)
+    var = np.full(X.size, 9e-6)
+    strat, obs = cdm_strategy(X, Y, los, d, var)
+    llk, res = _residuals(strat, theta, X.size)
+    w = np.full(X.size, np.float32(1.0 / 9e-6), dtype=np.float64)
+    ref = catmip.llk_from_residuals(res.astype(np.float64), w, obs.normalization())
+    assert np.max(np.abs(llk - ref) / np.abs(ref)) < 1e-9
+    # end to end against the FP64 oracle: bounded by the FP32 forward error
+    full, _ = catmip.diag_llk(cdm_los_oracle(theta, X, Y, los), d, var)
+    rel = np.abs(llk - full) / np.abs(full)
+    assert np.median(rel) < 1e-4
+
+
+def test_cdm_mask_and_surface_status(cuda):
+    g = np.linspace(-5e3, 5e3, 10)
+    X, Y = [a.ravel() for a in np.meshgrid(g, g)]
+    los = np.tile(LOS, (X.size, 1))
+    theta = cdm_prior_rows(4, seed=9)
+    theta[1, 2] = 200.0          # shallow and large: above the surface
+    theta[1, 4:7] = 2000.0
+    strat, _ = cdm_strategy(X, Y, los, np.zeros(X.size), np.ones(X.size))
+    out = torch.full((4,), 7.0, dtype=torch.float64, device="cuda")
+    mask = torch.tensor([0, 0, 1, 0], dtype=torch.int32, device="cuda")
+    strat.forward(dev(theta), out, mask=mask, status=mask)
+    torch.cuda.synchronize()
+    m = mask.cpu().numpy()
+    o = out.cpu().numpy()
+    assert m[1] & _native.AG_CHAIN_ABOVE_SURFACE and m[2] == 1 and m[0] == 0 and m[3] == 0
+    assert o[1] == 7.0 and o[2] == 7.0 and o[0] != 7.0 and o[3] != 7.0
+
+
+def test_cdm_dataset_offsets(cuda):
+    """Per-dataset offsets θ[offset_idx + oid] (cdm/Native.py:225-227)."""
+    g = np.linspace(-10e3, 10e3, 12)
+    X, Y = [a.ravel() for a in np.meshgrid(g, g)]
+    los = np.tile(LOS, (X.size, 1))
+    oid = (X > 0).astype(np.int32)
+    base = cdm_prior_rows(3, seed=4)
+    theta = np.concatenate([base, np.array([[0.01, -0.02]] * 3)], 1)
+    d = np.zeros(X.size)
+    strat, obs = cdm_strategy(X, Y, los, d, np.full(X.size, 1e-4), oid=oid, offset_idx=10, nparams=12)
+    llk, res = _residuals(strat, theta, X.size)
+    ref = cdm_los_oracle(base, X, Y, los) - theta[:, 10 + oid]
+    assert np.max(np.abs(res - ref)) <= 1e-4 * np.max(np.abs(ref))
+
+
+def test_mogi_matches_oracle(cuda):
+    rng = np.random.default_rng(1)
+    X, Y = rng.uniform(-25e3, 25e3, 3000), rng.uniform(-25e3, 25e3, 3000)
+    los = np.tile([0.38, -0.08, 0.92], (X.size, 1))
+    theta = np.stack([rng.uniform(-1e4, 1e4, 100), rng.uniform(-1e4, 1e4, 100), rng.uniform(1e3, 8e3, 100),
+                      rng.uniform(1e5, 1e7, 100)], 1)
+    d = catmip.mogi_los(theta[:1], X, Y, los, 0.25, log_strength=False)[0] + rng.normal(0, 5e-3, X.size)
+    var = np.full(X.size, 2.5e-5)
+    strat, obs = mogi_strategy(X, Y, los, d, var)
+    llk, res = _residuals(strat, theta, X.size)
+    ref_u = catmip.mogi_los(theta, X, Y, los, 0.25, log_strength=False)
+    err = np.max(np.abs((res + d) - ref_u), 1) / np.max(np.abs(ref_u), 1)
+    assert np.all(err < 1e-5), err.max()
+    w = np.full(X.size, np.float32(1 / 2.5e-5), dtype=np.float64)
+    ref = catmip.llk_from_residuals(res.astype(np.float64), w, obs.normalization())
+    assert np.max(np.abs(llk - ref) / np.abs(ref)) < 1e-9
+
+
+def test_mogi_two_sources_log_strength(cuda):
+    rng = np.random.default_rng(3)
+    X, Y = rng.uniform(-25e3, 25e3, 500), rng.uniform(-25e3, 25e3, 500)
+    los = np.tile([0.1, 0.5, 0.86], (X.size, 1))
+    # two sources, [x, y, depth, log10 ΔV] each, stride 4
+    theta = np.stack([rng.uniform(-1e4, 1e4, 20), rng.uniform(-1e4, 1e4, 20), rng.uniform(1e3, 8e3, 20),
+                      rng.uniform(5, 7, 20), rng.uniform(-1e4, 1e4, 20), rng.uniform(-1e4, 1e4, 20),
+                      rng.uniform(1e3, 8e3, 20), rng.uniform(5, 7, 20)], 1)
+    strat, obs = mogi_strategy(X, Y, los, np.zeros(X.size), np.ones(X.size), log_strength=True, nparams=8,
+                               nsources=2, stride=4)
+    _, res = _residuals(strat, theta, X.size)
+    ref = catmip.mogi_los(theta, X, Y, los, 0.25, log_strength=True, nsources=2, stride=4)
+    err = np.max(np.abs(res - ref), 1) / np.max(np.abs(ref), 1)
+    assert np.all(err < 1e-5), err.max()
+
+
+def test_host_buffer_call_pattern(cuda):
+    """The reference's call pattern: host θ in, host data log-likelihood out."""
+    rng = np.random.default_rng(8)
+    X, Y = rng.uniform(-15e3, 15e3, 256), rng.uniform(-15e3, 15e3, 256)
+    los = np.tile([0.38, -0.08, 0.92], (X.size, 1))
+    strat, _ = mogi_strategy(X, Y, los, np.zeros(X.size), np.ones(X.size))
+    theta = np.stack([rng.uniform(-1e4, 1e4, 10), rng.uniform(-1e4, 1e4, 10), rng.uniform(1e3, 8e3, 10),
+                      rng.uniform(1e5, 1e7, 10)], 1)
+
+    class Step:
+        pass
+
+    step = Step()
+    step.theta = theta
+    step.data = np.zeros(10)
+    strat.dataLikelihood(None, step)
+    out = torch.empty(10, dtype=torch.float64, device="cuda")
+    strat.forward(dev(theta), out)
+    np.testing.assert_array_equal(step.data, out.cpu().numpy())
