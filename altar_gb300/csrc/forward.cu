@@ -239,7 +239,7 @@ __global__ void cdm_check_kernel(ag_layout L, const double* __restrict__ theta, 
 
 // ---------------------------------------------------------------------------
 // one angular-dislocation pair in difference arithmetic
-AG_DEVICE_INLINE float frcp(float x) { return __fdividef(1.0f, x); }
+AG_DEVICE_INLINE float frcp(float x) { return fast_rcp(x); }
 
 AG_DEVICE_INLINE void side_pair(const SideC& S, float Xr, float Yr, float& ue, float& un,
                                 float& uv) {
@@ -288,15 +288,15 @@ AG_DEVICE_INLINE void side_pair(const SideC& S, float Xr, float Yr, float& ue, f
     const float dq = (posA && posB) ? fmaf(dN, DA, -NA * (dr + dz3)) * ivA * ivB : dr - dz3;
     const float diq = -dq * iqA * iqB;
     // log differences
-    const float dLp = log1pf(dp * ipA);
-    const float dLq = log1pf(dq * iqA);
+    const float dLp = log1p_series(dp * ipA);
+    const float dLq = log1p_series(dq * iqA);
     (void)qA;
     // Burgers function difference: rotation of (x, y2) from A to B; y2 keeps its sign so
     // the rotation never crosses atan2's cut
     const float xA = fmaf(pA, ct2, -y1A);
     const float dx = fmaf(dp, ct2, -dy1);
     const float xB = xA + dx;
-    const float dF = 2.0f * atan2f(-y2 * dx, fmaf(xA, xB, y22));
+    const float dF = 2.0f * atan2_poly(-y2 * dx, fmaf(xA, xB, y22));
     // monomials: value at A, value at B, difference
     const float m1A = y2 * ipA, m1B = y2 * ipB, dm1 = y2 * dip;
     const float m2A = y1A * ipA, m2B = y1B * ipB, dm2 = fmaf(dy1, ipB, y1A * dip);

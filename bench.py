@@ -38,9 +38,11 @@ PRIORS = [(-1e4, 1e4), (-1e4, 1e4), (1e3, 1e4), (-50.0, 50.0), (100.0, 3000.0), 
           (100.0, 3000.0), (-90.0, 90.0), (-90.0, 90.0), (-90.0, 90.0)]
 # parameter order: x0, y0, depth, opening, ax, ay, az, ωx, ωy, ωz
 # FP32 operations per (chain, station) pair of the fused CDM kernel, counted from
-# altar_gb300/csrc/forward.cu (FMA = 2): 225 per angular-dislocation pair side x 12
-# sides + 31 per station, excluding the bodies of the 24 log1pf and 12 atan2f calls
-CDM_FLOP_PER_PAIR = 2731
+# altar_gb300/csrc/forward.cu and common.cuh (FMA = 2): per rectangle side 225 for the
+# difference-arithmetic pair + 2 x 18 (log1p_series) + 21 (atan2_poly) = 282, times 12
+# sides, + 31 per station (coordinates, LOS projection, float-float misfit);
+# special-function unit: 12 per side (2 rsqrt, 10 rcp)
+CDM_FLOP_PER_PAIR = 3415
 L2_FLUSH_BYTES = 256 << 20
 
 
@@ -220,37 +222,20 @@ def run_ours(args):
         return 0
 
     samp = ann.sampler
+    S = app.job.steps
     with torch.cuda.stream(stream):
         ann.model = model
         worker.start(annealer=ann)
-        # one annealing stage brings the sample to β > 0 with a data-driven Σ
-        worker.cool(annealer=ann)
-        samp.prepareSamplingPDF(annealer=ann, step=worker.step)
-        step = worker.step
-        n, p = step.samples, step.parameters
-        cand, cprior, cdata, mask = samp._buffers(n, p)
-        st = step.state.struct
 
-        def mh_step(k):
-            s = stream_handle()
-            _native.call("ag_propose", st, ptr(step.theta), n, p, ptr(model.lo), ptr(model.hi), samp.seed, k,
-                         ptr(cand), ptr(mask), ptr(cprior), s)
-            model.strategy.forward(cand, cdata, mask=mask, status=mask)
-            _native.call("ag_accept", st, n, p, samp.seed, k, ptr(mask), ptr(cand), ptr(cprior), ptr(cdata),
-                         ptr(step.theta), ptr(step.prior), ptr(step.data), ptr(step.posterior), s)
+        def stage():
+            worker.cool(annealer=ann)
+            stats = worker.walk(annealer=ann)
+            worker.resample(annealer=ann, statistics=stats)
 
-        mh_step(0)                                       # allocations happen eagerly
-        import ctypes
-        h = stream_handle()
-        _native.call("ag_graph_begin", h)
-        mh_step(1)
-        gexec = ctypes.c_void_p()
-        _native.call("ag_graph_end", h, ctypes.byref(gexec))
-        launch = lambda: _native.call("ag_graph_launch", gexec, stream_handle())
         flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
-
-        for _ in range(args.warmup):
-            launch()
+        for _ in range(args.warmup):                 # first stage eager, then captured graphs
+            stage()
+            worker.bottom(annealer=ann)
         torch.cuda.synchronize()
         if dist is not None:
             dist.barrier()
@@ -261,18 +246,22 @@ def run_ours(args):
             for a, b in evs:
                 flush.zero_()                            # L2 flush between timed iterations
                 a.record(stream)
-                launch()
+                stage()
                 b.record(stream)
+                worker.bottom(annealer=ann)              # host reads β and the report (outside the events)
             torch.cuda.synchronize()
         ms = [a.elapsed_time(b) for a, b in evs]
-        t_step = sum(ms) / len(ms) / 1e3
+        t_stage = sum(ms) / len(ms) / 1e3
         if dist is not None:
-            tt = torch.tensor([t_step], device="cuda")
+            tt = torch.tensor([t_stage], device="cuda")
             dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            t_step = float(tt.item())
-        value = world * N / t_step
+            t_stage = float(tt.item())
+        value = world * N * S / t_stage
+        reps = worker.reports[-args.steps:]
+        step = worker.step
+        n = step.samples
 
-        # roofline: the fused forward kernel on every chain (no mask), CUDA events on its stream
+        # roofline: the fused forward model on every chain (no mask), CUDA events on its stream
         th_all = step.theta.clone()
         out = torch.empty(n, dtype=torch.float64, device="cuda")
         model.strategy.forward(th_all, out)
@@ -290,10 +279,10 @@ def run_ours(args):
         sm_max = float(pk.get("sm_max_mhz", 2070.0))
         fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12   # FMA lanes x 2 FLOP x max SM clock
 
-        # end to end through host buffers: θ and the three log-likelihood vectors in and out
-        host = [torch.empty_like(t, device="cpu").pin_memory() for t in (step.theta, step.prior, step.data,
-                                                                          step.posterior)]
-        for hh, t in zip(host, (step.theta, step.prior, step.data, step.posterior)):
+        # end to end through host buffers: θ and the three log-likelihood vectors in and out each stage
+        state = (step.theta, step.prior, step.data, step.posterior)
+        host = [torch.empty_like(t, device="cpu").pin_memory() for t in state]
+        for hh, t in zip(host, state):
             hh.copy_(t)
         torch.cuda.synchronize()
         e2e_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
@@ -301,16 +290,17 @@ def run_ours(args):
         for a, b in e2e_ev:
             flush.zero_()
             a.record(stream)
-            for hh, t in zip(host, (step.theta, step.prior, step.data, step.posterior)):
+            for hh, t in zip(host, state):
                 t.copy_(hh, non_blocking=True)
-            launch()
-            for hh, t in zip(host, (step.theta, step.prior, step.data, step.posterior)):
+            stage()
+            for hh, t in zip(host, state):
                 hh.copy_(t, non_blocking=True)
             b.record(stream)
+            worker.bottom(annealer=ann)
         torch.cuda.synchronize()
         t_e2e = sum(a.elapsed_time(b) for a, b in e2e_ev) / len(e2e_ev) / 1e3
         io_bytes = sum(t.numel() * t.element_size() for t in host)
-    _native.load().ag_graph_destroy(gexec)
+        worker.finish(annealer=ann)
 
     if rank != 0:
         return 0
@@ -323,20 +313,23 @@ def run_ours(args):
         pass
     line = {
         "metric": "CDM chain-steps/s", "value": value, "unit": "chain-steps/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_stage * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "cdm-40k-obs", "chains": N, "stations": X.size, "params": 10,
-                   "steps_per_stage": 5, "parallelism": "replicas" if world > 1 else "single-gpu",
-                   "l2": "flushed (256 MB write) between timed iterations", "graph": "one CUDA graph per step"},
+                   "steps_per_stage": S, "parallelism": "replicas" if world > 1 else "single-gpu",
+                   "step": "one annealing stage: COV beta + Sigma + resample, 5 Metropolis steps, scaling",
+                   "l2": "flushed (256 MB write) between timed iterations",
+                   "graphs": "one CUDA graph per phase (cool, walk, resample)",
+                   "beta_range": [reps[0]["beta"], reps[-1]["beta"]] if reps else None},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved / fp32_peak, "traffic": profile_traffic,
                      "kernel": "cdm_setup_kernel + cdm_llk_kernel", "flop_per_pair": CDM_FLOP_PER_PAIR,
                      "pairs_per_launch": pairs, "ms_per_launch": t_fwd * 1e3,
                      "peak_source": "nominal FP32 FMA rate at the measured max SM clock "
                                     "(MEASURED_PEAKS.json has no FP32 figure)"},
-        "e2e": {"value": world * N / t_e2e, "unit": "chain-steps/s", "h2d_bytes_per_step": io_bytes,
+        "e2e": {"value": world * N * S / t_e2e, "unit": "chain-steps/s", "h2d_bytes_per_step": io_bytes,
                 "d2h_bytes_per_step": io_bytes},
-        "gpu_launches": 4 * args.steps,
+        "gpu_launches": (35 + 1 + 4 * S + 1) * args.steps,
         "cpu_baseline": {"value": cpu_rate, "unit": "chain-steps/s", "cores": cores, "kind": "port",
                          "sample": f"{args.cpu_chains} chains x {X.size} stations, likelihood only, "
                                    f"{cpu_dt:.1f} s (FP64 C restatement of models/cdm/cdm/libcdm.py)"},

