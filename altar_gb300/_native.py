@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "_lib")
 LIBPATH = os.path.join(LIBDIR, "libaltar_gb300.so")
-SOURCES = ("forward.cu", "stage.cu", "api.cu")
+SOURCES = ("forward.cu", "stage.cu", "surrogate.cu", "api.cu")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 
@@ -95,6 +95,10 @@ class Layout(ctypes.Structure):
                 ("source_stride", c_int32), ("nu", c_double)]
 
 
+class MLP(ctypes.Structure):
+    _fields_ = [("nlayers", c_int32), ("sizes", c_int32 * 9)]
+
+
 class StageState(ctypes.Structure):
     _fields_ = [("beta", c_void_p), ("dbeta_cov", c_void_p), ("scaling", c_void_p),
                 ("sigma", c_void_p), ("chol", c_void_p), ("w", c_void_p),
@@ -108,6 +112,20 @@ _SIGNATURES = {
     "ag_forward_workspace_bytes": (c_size_t, [c_int, c_int32]),
     "ag_forward_llk": (c_int, [c_int, P, P, c_int32, P, c_double, P, P, P, P, P, c_size_t, P]),
     "ag_cdm_check": (c_int, [P, P, c_int32, P, P]),
+    "ag_forward_llk_subset": (c_int, [c_int, P, P, c_int32, P, c_double, P, P, P, P, P, P, c_size_t, P]),
+    "ag_mlp_param_count": (ctypes.c_int64, [P]),
+    "ag_mlp_activation_floats": (ctypes.c_int64, [P, c_int32]),
+    "ag_normalize_inputs": (c_int, [P, c_int32, c_int32, P, P, P, P]),
+    "ag_mlp_forward": (c_int, [P, P, P, P, c_int32, P, P, P]),
+    "ag_mlp_backward": (c_int, [P, P, P, P, c_int32, P, P, P, P, P]),
+    "ag_mse_grad": (c_int, [c_int32, c_int32, P, P, P, P, P]),
+    "ag_adam_step": (c_int, [ctypes.c_int64, P, P, P, P, c_int32, ctypes.c_float, ctypes.c_float,
+                             ctypes.c_float, ctypes.c_float, P, P]),
+    "ag_to_bf16": (c_int, [ctypes.c_int64, P, P, P]),
+    "ag_surrogate_llk": (c_int, [c_int32, c_int32, P, P, P, P, c_double, c_double, P, P]),
+    "ag_da_screen": (c_int, [P, c_int32, c_uint64, c_uint32, P, P, P, P, P, P, P, P, P]),
+    "ag_da_accept": (c_int, [P, c_int32, c_int32, c_uint64, c_uint32, P, P, P, P, P, P, P, P, P, P, P,
+                             P, P]),
     "ag_prior_sample": (c_int, [c_int32, c_int32, P, P, c_uint64, c_uint32, P, P, P]),
     "ag_prior_llk": (c_int, [P, c_int32, c_int32, P, P, P, P, P]),
     "ag_propose": (c_int, [P, P, c_int32, c_int32, P, P, c_uint64, c_uint32, P, P, P, P]),

@@ -178,10 +178,16 @@ __device__ bool cdm_corners(const double* th, const ag_layout& L, Vec3 V[3][4]) 
 
 __global__ void cdm_setup_kernel(ag_layout L, const double* __restrict__ theta, int n,
                                  const uint32_t* __restrict__ mask_in, ChainC* __restrict__ out,
-                                 uint32_t* __restrict__ chain_status, int noffsets) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    ChainC& C = out[i];
+                                 uint32_t* __restrict__ chain_status, int noffsets,
+                                 const int32_t* __restrict__ index, const int32_t* __restrict__ count) {
+    const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= n) return;
+    ChainC& C = out[slot];
+    int i = slot;
+    if (index) {
+        if (slot >= *count) { C.side_mask = 0u; return; }
+        i = index[slot];
+    }
     const double* th = theta + (size_t)i * L.nparams;
     C.side_mask = 0u;
     C.status = 0u;
@@ -375,7 +381,10 @@ __global__ void __launch_bounds__(WARPS * 32, 2)
 cdm_llk_kernel(const ChainC* __restrict__ chains, int n, const float4* __restrict__ xy,
                const float4* __restrict__ losd, const float* __restrict__ wt,
                const int32_t* __restrict__ oid, int m_padded, double norm,
-               double* __restrict__ llk, float* __restrict__ resid, uint32_t* __restrict__ flags) {
+               double* __restrict__ llk, float* __restrict__ resid, uint32_t* __restrict__ flags,
+               const int32_t* __restrict__ index, const int32_t* __restrict__ count) {
+    // with an index list, slots beyond the device-side count have nothing to do
+    if (index && (int)(blockIdx.x * WARPS) >= *count) return;
     __shared__ ChainC s_chain[WARPS];
     __shared__ float4 s_xy[2][kTile];
     __shared__ float4 s_ld[2][kTile];
@@ -384,14 +393,16 @@ cdm_llk_kernel(const ChainC* __restrict__ chains, int n, const float4* __restric
     __shared__ __align__(8) uint64_t bar[2];
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int chain = blockIdx.x * WARPS + warp;
+    const int slot = blockIdx.x * WARPS + warp;
+    const int nslots = index ? min(n, *count) : n;
+    const int chain = (slot < nslots) ? (index ? index[slot] : slot) : n;
     const int ntiles = m_padded / kTile;
     const bool with_oid = (oid != nullptr);
     const uint32_t tile_bytes = kTile * (16u + 16u + 4u) + (with_oid ? kTile * 4u : 0u);
 
     // this warp's chain constants
     {
-        const float4* src = reinterpret_cast<const float4*>(chains + (chain < n ? chain : 0));
+        const float4* src = reinterpret_cast<const float4*>(chains + (slot < nslots ? slot : 0));
         float4* dst = reinterpret_cast<float4*>(&s_chain[warp]);
         constexpr int nvec = sizeof(ChainC) / 16;
         for (int k = lane; k < nvec; k += 32) dst[k] = src[k];
@@ -480,15 +491,24 @@ mogi_llk_kernel(ag_layout L, const double* __restrict__ theta, int n,
                 const uint32_t* __restrict__ mask_in, const float4* __restrict__ xy,
                 const float4* __restrict__ losd, const float* __restrict__ wt,
                 const int32_t* __restrict__ oid, int noffsets, int m_padded, double norm,
-                double* __restrict__ llk, float* __restrict__ resid) {
+                double* __restrict__ llk, float* __restrict__ resid, const int32_t* __restrict__ index,
+                const int32_t* __restrict__ count) {
+    if (index && (int)(blockIdx.x * CH) >= *count) return;
     __shared__ MogiSrc s_src[CH][NSRC];
+    __shared__ int s_chain[CH];
     __shared__ float s_off[CH][kMaxOffsets];
     __shared__ int s_act[CH];
     __shared__ double s_part[CH][8];
     const int c0 = blockIdx.x * CH;
     const double PI = 3.14159265358979323846;
+    const int nslots = index ? min(n, *count) : n;
+    for (int c = threadIdx.x; c < CH; c += blockDim.x) {
+        const int slot = c0 + c;
+        s_chain[c] = (slot < nslots) ? (index ? index[slot] : slot) : n;
+    }
+    __syncthreads();
     for (int k = threadIdx.x; k < CH * NSRC; k += blockDim.x) {
-        const int c = k / NSRC, src = k % NSRC, i = c0 + c;
+        const int c = k / NSRC, src = k % NSRC, i = s_chain[c];
         MogiSrc S{};
         if (i < n) {
             const double* th = theta + (size_t)i * L.nparams + src * L.source_stride;
@@ -500,12 +520,12 @@ mogi_llk_kernel(ag_layout L, const double* __restrict__ theta, int n,
         s_src[c][src] = S;
     }
     for (int k = threadIdx.x; k < CH * kMaxOffsets; k += blockDim.x) {
-        const int c = k / kMaxOffsets, o = k % kMaxOffsets, i = c0 + c;
+        const int c = k / kMaxOffsets, o = k % kMaxOffsets, i = s_chain[c];
         s_off[c][o] = (i < n && o < noffsets)
                           ? (float)theta[(size_t)i * L.nparams + L.offset_idx + o] : 0.f;
     }
     for (int c = threadIdx.x; c < CH; c += blockDim.x) {
-        const int i = c0 + c;
+        const int i = s_chain[c];
         s_act[c] = (i < n) && !(mask_in && mask_in[i]);
     }
     __syncthreads();
@@ -536,7 +556,7 @@ mogi_llk_kernel(ag_layout L, const double* __restrict__ theta, int n,
             float r = u - B.w;
             if (oid) r -= s_off[c][o];
             if (w != 0.f) ff_add_wsq(acc[c], r, w);
-            if (resid && c0 + c < n) resid[(size_t)(c0 + c) * m_padded + j] = (w != 0.f) ? r : 0.f;
+            if (resid && s_chain[c] < n) resid[(size_t)s_chain[c] * m_padded + j] = (w != 0.f) ? r : 0.f;
         }
     }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -550,7 +570,7 @@ mogi_llk_kernel(ag_layout L, const double* __restrict__ theta, int n,
         if (!s_act[c]) continue;
         double s = 0.0;
         for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += s_part[c][k];
-        llk[c0 + c] = norm - 0.5 * s;
+        llk[s_chain[c]] = norm - 0.5 * s;
     }
 }
 
@@ -580,10 +600,11 @@ static int check_stations(const ag_station_set* st) {
     return AG_OK;
 }
 
-extern "C" int ag_forward_llk(int model, const ag_layout* layout, const double* theta, int32_t n,
-                              const ag_station_set* st, double norm, const uint32_t* mask_in,
-                              double* llk, uint32_t* chain_status, float* residuals,
-                              void* workspace, size_t workspace_bytes, void* stream) {
+static int forward_llk(int model, const ag_layout* layout, const double* theta, int32_t n,
+                       const ag_station_set* st, double norm, const uint32_t* mask_in,
+                       const int32_t* index, const int32_t* count, double* llk,
+                       uint32_t* chain_status, float* residuals, void* workspace,
+                       size_t workspace_bytes, void* stream) {
     AG_REQUIRE(layout != nullptr && theta != nullptr && llk != nullptr, "null argument");
     AG_REQUIRE(n > 0, "n must be positive (got %d)", n);
     int rc = check_stations(st);
@@ -611,12 +632,13 @@ extern "C" int ag_forward_llk(int model, const ag_layout* layout, const double* 
                    "CDM needs %zu bytes of 256-byte aligned workspace", need);
         ChainC* chains = reinterpret_cast<ChainC*>(workspace);
         cdm_setup_kernel<<<(n + 127) / 128, 128, 0, s>>>(L, theta, n, mask_in, chains, chain_status,
-                                                         noffsets);
+                                                         noffsets, index, count);
         rc = launch_status("cdm_setup_kernel");
         if (rc) return rc;
         const int grid = (n + kCdmWarps - 1) / kCdmWarps;
         cdm_llk_kernel<kCdmWarps><<<grid, kCdmWarps * 32, 0, s>>>(
-            chains, n, xy, ld, st->weight, st->oid, st->m_padded, norm, llk, residuals, nullptr);
+            chains, n, xy, ld, st->weight, st->oid, st->m_padded, norm, llk, residuals, nullptr, index,
+            count);
         return launch_status("cdm_llk_kernel");
     }
     if (model == AG_MODEL_MOGI) {
@@ -625,14 +647,32 @@ extern "C" int ag_forward_llk(int model, const ag_layout* layout, const double* 
         if (L.nsources == 1)
             mogi_llk_kernel<kMogiChains, 1><<<grid, 256, 0, s>>>(
                 L, theta, n, mask_in, xy, ld, st->weight, st->oid, noffsets, st->m_padded, norm, llk,
-                residuals);
+                residuals, index, count);
         else
             mogi_llk_kernel<kMogiChains, 2><<<grid, 256, 0, s>>>(
                 L, theta, n, mask_in, xy, ld, st->weight, st->oid, noffsets, st->m_padded, norm, llk,
-                residuals);
+                residuals, index, count);
         return launch_status("mogi_llk_kernel");
     }
     return set_error(AG_ERR_ARG, "unknown model %d", model);
+}
+
+extern "C" int ag_forward_llk(int model, const ag_layout* layout, const double* theta, int32_t n,
+                              const ag_station_set* st, double norm, const uint32_t* mask_in,
+                              double* llk, uint32_t* chain_status, float* residuals,
+                              void* workspace, size_t workspace_bytes, void* stream) {
+    return forward_llk(model, layout, theta, n, st, norm, mask_in, nullptr, nullptr, llk, chain_status,
+                       residuals, workspace, workspace_bytes, stream);
+}
+
+extern "C" int ag_forward_llk_subset(int model, const ag_layout* layout, const double* theta,
+                                     int32_t n, const ag_station_set* st, double norm,
+                                     const int32_t* index, const int32_t* count, double* llk,
+                                     uint32_t* chain_status, float* residuals, void* workspace,
+                                     size_t workspace_bytes, void* stream) {
+    AG_REQUIRE(index != nullptr && count != nullptr, "index and count must not be NULL");
+    return forward_llk(model, layout, theta, n, st, norm, nullptr, index, count, llk, chain_status,
+                       residuals, workspace, workspace_bytes, stream);
 }
 
 extern "C" int ag_cdm_check(const ag_layout* layout, const double* theta, int32_t n,

@@ -1,0 +1,436 @@
+// Learned surrogate of the CDM LOS field and the delayed-acceptance steps.
+//
+// Network: dense layers y = x Wᵀ + b with GELU (x Φ(x)) between them and a
+// linear output; weights kept as an FP32 master copy for Adam plus a BF16 copy
+// that the forward and backward products read (FP32 accumulation).  Layer
+// products are a tiled SIMT GEMM with fused bias / GELU epilogues.
+//
+// Surrogate log-likelihood: the network predicts K normalised PCA coefficients
+// c of the LOS field; with the basis B (M x K), mean field μ and the diagonal
+// weights W = Cd⁻¹, Σ_j w_j (ũ_j - d_j)² for ũ = μ + B diag(s) c is
+//     q0 - 2 hᵀ c̃ + c̃ᵀ G c̃,  c̃ = s ⊙ c,  h = Bᵀ W (d - μ),  G = Bᵀ W B,
+// so each chain costs O(K²) instead of O(M).
+//
+// Delayed acceptance (Christen & Fox 2005): stage 1 accepts the proposal on
+// the surrogate posterior; only stage-1 survivors (compacted into an index
+// list) get the exact likelihood; stage 2 accepts with
+//     log u2 <= (post' - post) - (post̃' - post̃),
+// which leaves the exact posterior invariant.
+#include <math.h>
+#include <stdint.h>
+#include <cuda_bf16.h>
+
+#include "common.cuh"
+#include "internal.h"
+
+namespace ag {
+
+constexpr int kMaxLayers = 8;
+constexpr int BM = 64, BN = 64, BK = 16;
+
+AG_DEVICE_INLINE float gelu(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
+AG_DEVICE_INLINE float gelu_grad(float z) {
+    return 0.5f * (1.0f + erff(z * 0.70710678118654752f)) +
+           z * 0.39894228040143268f * __expf(-0.5f * z * z);
+}
+
+enum Epilogue : int { EPI_NONE = 0, EPI_BIAS = 1, EPI_BIAS_GELU = 2 };
+
+// C(m, n) = Σ_k A(m, k) B(k, n) with A(m,k) = A[m*sam + k*sak], B(k,n) = B[k*sbk + n*sbn]
+// (B in BF16 or FP32), then the epilogue: + bias[n], GELU (pre-activation to Z).
+template <bool B_BF16>
+__global__ void __launch_bounds__(256) gemm_kernel(int M, int N, int K, const float* __restrict__ A,
+                                                   long sam, long sak, const void* __restrict__ Bv,
+                                                   long sbk, long sbn, float* __restrict__ C, long ldc,
+                                                   const float* __restrict__ bias, int epi,
+                                                   float* __restrict__ Z) {
+    __shared__ float As[BK][BM + 4];
+    __shared__ float Bs[BK][BN + 4];
+    const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+    const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+    float acc[4][4] = {};
+    for (int k0 = 0; k0 < K; k0 += BK) {
+        for (int e = threadIdx.x; e < BK * BM; e += 256) {
+            const int kk = e / BM, mm = e % BM;
+            const int m = m0 + mm, k = k0 + kk;
+            As[kk][mm] = (m < M && k < K) ? A[(long)m * sam + (long)k * sak] : 0.f;
+        }
+        for (int e = threadIdx.x; e < BK * BN; e += 256) {
+            const int kk = e / BN, nn = e % BN;
+            const int n = n0 + nn, k = k0 + kk;
+            float v = 0.f;
+            if (n < N && k < K) {
+                const long idx = (long)k * sbk + (long)n * sbn;
+                v = B_BF16 ? __bfloat162float(reinterpret_cast<const __nv_bfloat16*>(Bv)[idx])
+                           : reinterpret_cast<const float*>(Bv)[idx];
+            }
+            Bs[kk][nn] = v;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < BK; ++kk) {
+            float a[4], b[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) a[i] = As[kk][ty * 4 + i];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx * 4 + j];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int m = m0 + ty * 4 + i;
+        if (m >= M) continue;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int n = n0 + tx * 4 + j;
+            if (n >= N) continue;
+            float v = acc[i][j];
+            if (epi != EPI_NONE) v += bias[n];
+            if (epi == EPI_BIAS_GELU) {
+                Z[(long)m * ldc + n] = v;
+                v = gelu(v);
+            }
+            C[(long)m * ldc + n] = v;
+        }
+    }
+}
+
+// θ (FP64, N x p) -> x = 2 (θ - lo)/(hi - lo) - 1 (FP32); optional index list
+__global__ void normalize_kernel(const double* __restrict__ theta, int n, int p,
+                                 const double* __restrict__ lo, const double* __restrict__ hi,
+                                 float* __restrict__ x) {
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n * p) return;
+    const int j = e % p;
+    x[e] = (float)(2.0 * (theta[e] - lo[j]) / (hi[j] - lo[j]) - 1.0);
+}
+
+// dZ = dY ⊙ GELU'(Z)
+__global__ void gelu_back_kernel(long n, const float* __restrict__ Z, float* __restrict__ dY) {
+    long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < n) dY[e] *= gelu_grad(Z[e]);
+}
+
+// db[j] = Σ_i dZ[i, j] (fixed order: one thread per column, strided rows)
+__global__ void colsum_kernel(int rows, int cols, const float* __restrict__ dZ, float* __restrict__ db) {
+    __shared__ float part[256];
+    const int j = blockIdx.x;
+    float s = 0.f;
+    for (int i = threadIdx.x; i < rows; i += blockDim.x) s += dZ[(long)i * cols + j];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) part[threadIdx.x] += part[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) db[j] = part[0];
+}
+
+// mean-squared error: dY = (out - y)/n, per-row squared error for the loss
+__global__ void mse_kernel(int n, int k, const float* __restrict__ out, const float* __restrict__ y,
+                           float* __restrict__ dY, float* __restrict__ row_loss) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float s = 0.f;
+    for (int j = 0; j < k; ++j) {
+        const float d = out[(long)i * k + j] - y[(long)i * k + j];
+        dY[(long)i * k + j] = d / (float)n;
+        s = fmaf(d, d, s);
+    }
+    if (row_loss) row_loss[i] = 0.5f * s;
+}
+
+// Adam with bias correction (Kingma & Ba 2015); refreshes the BF16 weight copy
+__global__ void adam_kernel(long count, float* __restrict__ p, const float* __restrict__ g,
+                            float* __restrict__ m, float* __restrict__ v, float lr, float b1, float b2,
+                            float eps, float c1, float c2, __nv_bfloat16* __restrict__ pbf) {
+    long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= count) return;
+    const float gi = g[e];
+    const float mi = b1 * m[e] + (1.f - b1) * gi;
+    const float vi = b2 * v[e] + (1.f - b2) * gi * gi;
+    m[e] = mi;
+    v[e] = vi;
+    const float w = p[e] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    p[e] = w;
+    if (pbf) pbf[e] = __float2bfloat16_rn(w);
+}
+
+__global__ void to_bf16_kernel(long count, const float* __restrict__ p, __nv_bfloat16* __restrict__ q) {
+    long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < count) q[e] = __float2bfloat16_rn(p[e]);
+}
+
+// llk_s = norm - ½ (q0 - 2 hᵀ c̃ + c̃ᵀ G c̃), c̃ = scale ⊙ c ; one warp per chain
+__global__ void surrogate_llk_kernel(int n, int k, const float* __restrict__ coeff,
+                                     const float* __restrict__ scale, const float* __restrict__ G,
+                                     const float* __restrict__ h, double q0, double norm,
+                                     double* __restrict__ llk) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= n) return;
+    const float* c = coeff + (long)warp * k;
+    double acc = 0.0;
+    for (int a = lane; a < k; a += 32) {
+        const float ca = c[a] * scale[a];
+        float row = 0.f;
+        for (int b = 0; b < k; ++b) row = fmaf(G[a * k + b], c[b] * scale[b], row);
+        acc += (double)ca * (double)row - 2.0 * (double)h[a] * (double)ca;
+    }
+    acc = warp_sum(acc);
+    if (lane == 0) llk[warp] = norm - 0.5 * (q0 + acc);
+}
+
+// Stage 1 of delayed acceptance: surrogate Metropolis test and compaction of survivors
+__global__ void da_screen_kernel(int n, const double* __restrict__ beta, uint64_t seed, uint32_t step,
+                                 const uint32_t* __restrict__ epoch, const uint32_t* __restrict__ mask,
+                                 const double* __restrict__ cprior, const double* __restrict__ csur,
+                                 const double* __restrict__ prior, const double* __restrict__ sur,
+                                 int32_t* __restrict__ pass, int32_t* __restrict__ index,
+                                 int32_t* __restrict__ count) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int ok = 0;
+    if (!mask[i]) {
+        const double b = *beta;
+        const double d1 = (cprior[i] + b * csur[i]) - (prior[i] + b * sur[i]);
+        u32x4 r = draw(seed, (uint32_t)i, 1u, STREAM_ACCEPT, step, *epoch);
+        ok = log(u01_open_closed(r.x, r.y)) <= d1;
+    }
+    pass[i] = ok;
+    if (ok) index[atomicAdd(count, 1)] = i;
+}
+
+// Stage 2: exact correction for the survivors; counters: accepted, rejected (support), unlikely
+__global__ void da_accept_kernel(int n, int p, const double* __restrict__ beta, uint64_t seed,
+                                 uint32_t step, const uint32_t* __restrict__ epoch,
+                                 const uint32_t* __restrict__ mask, const int32_t* __restrict__ pass,
+                                 const double* __restrict__ cand, const double* __restrict__ cprior,
+                                 const double* __restrict__ cdata, const double* __restrict__ csur,
+                                 double* __restrict__ theta, double* __restrict__ prior,
+                                 double* __restrict__ data, double* __restrict__ post,
+                                 double* __restrict__ sur, unsigned long long* __restrict__ counters,
+                                 unsigned long long* __restrict__ screened) {
+    __shared__ unsigned int s_cnt[4];
+    if (threadIdx.x < 4) s_cnt[threadIdx.x] = 0u;
+    __syncthreads();
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        if (mask[i]) {
+            atomicAdd(&s_cnt[1], 1u);
+        } else if (!pass[i]) {
+            atomicAdd(&s_cnt[2], 1u);
+        } else {
+            atomicAdd(&s_cnt[3], 1u);
+            const double b = *beta;
+            const double cp = cprior[i] + b * cdata[i];
+            const double dsur = (cprior[i] + b * csur[i]) - (prior[i] + b * sur[i]);
+            u32x4 r = draw(seed, (uint32_t)i, 2u, STREAM_ACCEPT, step, *epoch);
+            if (log(u01_open_closed(r.x, r.y)) > (cp - post[i]) - dsur) {
+                atomicAdd(&s_cnt[2], 1u);
+            } else {
+                atomicAdd(&s_cnt[0], 1u);
+                for (int j = 0; j < p; ++j) theta[(size_t)i * p + j] = cand[(size_t)i * p + j];
+                prior[i] = cprior[i];
+                data[i] = cdata[i];
+                post[i] = cp;
+                sur[i] = csur[i];
+            }
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 3 && s_cnt[threadIdx.x])
+        atomicAdd(&counters[threadIdx.x], (unsigned long long)s_cnt[threadIdx.x]);
+    if (threadIdx.x == 3 && s_cnt[3] && screened) atomicAdd(screened, (unsigned long long)s_cnt[3]);
+}
+
+}  // namespace ag
+
+// ---------------------------------------------------------------------------
+// C ABI
+using namespace ag;
+
+static inline int nblk(long n, int t) { return (int)((n + t - 1) / t); }
+
+static int check_net(const ag_mlp* net) {
+    AG_REQUIRE(net && net->nlayers >= 1 && net->nlayers <= kMaxLayers, "invalid network");
+    for (int l = 0; l <= net->nlayers; ++l) AG_REQUIRE(net->sizes[l] > 0, "layer size must be positive");
+    return AG_OK;
+}
+
+extern "C" int64_t ag_mlp_param_count(const ag_mlp* net) {
+    if (check_net(net)) return -1;
+    int64_t c = 0;
+    for (int l = 0; l < net->nlayers; ++l) c += (int64_t)net->sizes[l + 1] * net->sizes[l] + net->sizes[l + 1];
+    return c;
+}
+
+// parameter layout: for each layer W (out x in) then b (out)
+static void offsets(const ag_mlp* net, int64_t* w, int64_t* b) {
+    int64_t c = 0;
+    for (int l = 0; l < net->nlayers; ++l) {
+        w[l] = c;
+        c += (int64_t)net->sizes[l + 1] * net->sizes[l];
+        b[l] = c;
+        c += net->sizes[l + 1];
+    }
+}
+
+extern "C" int64_t ag_mlp_activation_floats(const ag_mlp* net, int32_t n) {
+    if (check_net(net) || n <= 0) return -1;
+    int64_t c = 0;
+    for (int l = 1; l <= net->nlayers; ++l) c += 2 * (int64_t)n * net->sizes[l];   // Z and Y per layer
+    return c;
+}
+
+static int gemm(cudaStream_t s, int M, int N, int K, const float* A, long sam, long sak, const void* B,
+                bool bbf16, long sbk, long sbn, float* C, long ldc, const float* bias, int epi, float* Z) {
+    dim3 grid(nblk(N, BN), nblk(M, BM));
+    if (bbf16)
+        gemm_kernel<true><<<grid, 256, 0, s>>>(M, N, K, A, sam, sak, B, sbk, sbn, C, ldc, bias, epi, Z);
+    else
+        gemm_kernel<false><<<grid, 256, 0, s>>>(M, N, K, A, sam, sak, B, sbk, sbn, C, ldc, bias, epi, Z);
+    return launch_status("gemm_kernel");
+}
+
+extern "C" int ag_normalize_inputs(const double* theta, int32_t n, int32_t p, const double* lo,
+                                   const double* hi, float* x, void* stream) {
+    AG_REQUIRE(theta && lo && hi && x && n > 0 && p > 0, "invalid arguments");
+    normalize_kernel<<<nblk((long)n * p, 256), 256, 0, as_stream(stream)>>>(theta, n, p, lo, hi, x);
+    return launch_status("normalize_kernel");
+}
+
+extern "C" int ag_mlp_forward(const ag_mlp* net, const float* params, const uint16_t* wbf16,
+                              const float* x, int32_t n, float* out, float* acts, void* stream) {
+    int rc = check_net(net);
+    if (rc) return rc;
+    AG_REQUIRE(params && wbf16 && x && out && acts && n > 0, "invalid arguments");
+    cudaStream_t s = as_stream(stream);
+    int64_t wo[kMaxLayers], bo[kMaxLayers];
+    offsets(net, wo, bo);
+    const float* in = x;
+    float* a = acts;
+    for (int l = 0; l < net->nlayers; ++l) {
+        const int fi = net->sizes[l], fo = net->sizes[l + 1];
+        const bool last = (l == net->nlayers - 1);
+        float* Z = a;
+        float* Y = last ? out : a + (int64_t)n * fo;
+        rc = gemm(s, n, fo, fi, in, fi, 1, wbf16 + wo[l], true, 1, fi, Y, fo, params + bo[l],
+                  last ? EPI_BIAS : EPI_BIAS_GELU, Z);
+        if (rc) return rc;
+        in = Y;
+        a += 2 * (int64_t)n * fo;
+    }
+    return AG_OK;
+}
+
+extern "C" int ag_mlp_backward(const ag_mlp* net, const float* params, const uint16_t* wbf16,
+                               const float* x, int32_t n, const float* acts, float* dout, float* grads,
+                               float* scratch, void* stream) {
+    int rc = check_net(net);
+    if (rc) return rc;
+    AG_REQUIRE(params && wbf16 && x && acts && dout && grads && scratch && n > 0, "invalid arguments");
+    cudaStream_t s = as_stream(stream);
+    int64_t wo[kMaxLayers], bo[kMaxLayers], ao[kMaxLayers];
+    offsets(net, wo, bo);
+    int64_t c = 0;
+    int maxw = 0;
+    for (int l = 0; l < net->nlayers; ++l) {
+        ao[l] = c;
+        c += 2 * (int64_t)n * net->sizes[l + 1];
+        maxw = max(maxw, net->sizes[l + 1]);
+        maxw = max(maxw, net->sizes[l]);
+    }
+    // dY of the current layer lives in dout (last layer) or in scratch (n x maxw, ping-pong)
+    float* cur = dout;
+    float* bufs[2] = {scratch, scratch + (int64_t)n * maxw};
+    for (int l = net->nlayers - 1; l >= 0; --l) {
+        const int fi = net->sizes[l], fo = net->sizes[l + 1];
+        const bool last = (l == net->nlayers - 1);
+        if (!last) {
+            gelu_back_kernel<<<nblk((long)n * fo, 256), 256, 0, s>>>((long)n * fo, acts + ao[l], cur);
+            rc = launch_status("gelu_back_kernel");
+            if (rc) return rc;
+        }
+        const float* hin = (l == 0) ? x : acts + ao[l - 1] + (int64_t)n * fi;   // Y of layer l-1
+        // dW (fo x fi) = dZᵀ (fo x n) · h (n x fi)
+        rc = gemm(s, fo, fi, n, cur, 1, fo, hin, false, fi, 1, grads + wo[l], fi, nullptr, EPI_NONE, nullptr);
+        if (rc) return rc;
+        colsum_kernel<<<fo, 256, 0, s>>>(n, fo, cur, grads + bo[l]);
+        rc = launch_status("colsum_kernel");
+        if (rc) return rc;
+        if (l > 0) {
+            float* nxt = bufs[l & 1];
+            // dX (n x fi) = dZ (n x fo) · W (fo x fi)
+            rc = gemm(s, n, fi, fo, cur, fo, 1, wbf16 + wo[l], true, fi, 1, nxt, fi, nullptr, EPI_NONE, nullptr);
+            if (rc) return rc;
+            cur = nxt;
+        }
+    }
+    return AG_OK;
+}
+
+extern "C" int ag_mse_grad(int32_t n, int32_t k, const float* out, const float* target, float* dout,
+                           float* row_loss, void* stream) {
+    AG_REQUIRE(n > 0 && k > 0 && out && target && dout, "invalid arguments");
+    mse_kernel<<<nblk(n, 256), 256, 0, as_stream(stream)>>>(n, k, out, target, dout, row_loss);
+    return launch_status("mse_kernel");
+}
+
+extern "C" int ag_adam_step(int64_t count, float* params, const float* grads, float* m, float* v,
+                            int32_t t, float lr, float b1, float b2, float eps, uint16_t* wbf16,
+                            void* stream) {
+    AG_REQUIRE(count > 0 && params && grads && m && v && t >= 1, "invalid arguments");
+    const float c1 = 1.f - powf(b1, (float)t), c2 = 1.f - powf(b2, (float)t);
+    adam_kernel<<<nblk(count, 256), 256, 0, as_stream(stream)>>>(
+        count, params, grads, m, v, lr, b1, b2, eps, c1, c2, reinterpret_cast<__nv_bfloat16*>(wbf16));
+    return launch_status("adam_kernel");
+}
+
+extern "C" int ag_to_bf16(int64_t count, const float* src, uint16_t* dst, void* stream) {
+    AG_REQUIRE(count > 0 && src && dst, "invalid arguments");
+    to_bf16_kernel<<<nblk(count, 256), 256, 0, as_stream(stream)>>>(count, src,
+                                                                     reinterpret_cast<__nv_bfloat16*>(dst));
+    return launch_status("to_bf16_kernel");
+}
+
+extern "C" int ag_surrogate_llk(int32_t n, int32_t k, const float* coeff, const float* scale,
+                                const float* gram, const float* h, double q0, double norm, double* llk,
+                                void* stream) {
+    AG_REQUIRE(n > 0 && k > 0 && coeff && scale && gram && h && llk, "invalid arguments");
+    surrogate_llk_kernel<<<nblk((long)n * 32, 256), 256, 0, as_stream(stream)>>>(n, k, coeff, scale, gram, h,
+                                                                               q0, norm, llk);
+    return launch_status("surrogate_llk_kernel");
+}
+
+extern "C" int ag_da_screen(const ag_stage_state* st, int32_t n, uint64_t seed, uint32_t step,
+                            const uint32_t* mask, const double* cprior, const double* csur,
+                            const double* prior, const double* sur, int32_t* pass, int32_t* index,
+                            int32_t* count, void* stream) {
+    AG_REQUIRE(st && n > 0 && mask && cprior && csur && prior && sur && pass && index && count,
+               "invalid arguments");
+    cudaStream_t s = as_stream(stream);
+    int rc = cuda_status(cudaMemsetAsync(count, 0, sizeof(int32_t), s), "memset count");
+    if (rc) return rc;
+    da_screen_kernel<<<nblk(n, 256), 256, 0, s>>>(n, st->beta, seed, step, st->epoch, mask, cprior, csur,
+                                                  prior, sur, pass, index, count);
+    return launch_status("da_screen_kernel");
+}
+
+extern "C" int ag_da_accept(const ag_stage_state* st, int32_t n, int32_t p, uint64_t seed, uint32_t step,
+                            const uint32_t* mask, const int32_t* pass, const double* cand,
+                            const double* cprior, const double* cdata, const double* csur, double* theta,
+                            double* prior, double* data, double* post, double* sur,
+                            unsigned long long* screened, void* stream) {
+    AG_REQUIRE(st && n > 0 && p > 0 && mask && pass && cand && cprior && cdata && csur && theta && prior &&
+                   data && post && sur,
+               "invalid arguments");
+    da_accept_kernel<<<nblk(n, 256), 256, 0, as_stream(stream)>>>(
+        n, p, st->beta, seed, step, st->epoch, mask, pass, cand, cprior, cdata, csur, theta, prior, data,
+        post, sur, st->counters, screened);
+    return launch_status("da_accept_kernel");
+}

@@ -114,6 +114,17 @@ int ag_forward_llk(int model, const ag_layout* layout, const double* theta, int3
                    void* workspace, size_t workspace_bytes, void* stream);
 
 /*
+ * ag_forward_llk restricted to the chains index[0 .. *count) (device-side
+ * count, e.g. the survivors of a delayed-acceptance screen); llk, chain_status
+ * and residual rows of the other chains are left untouched.  No counterpart in
+ * the reference (its likelihood always evaluates every chain).
+ */
+int ag_forward_llk_subset(int model, const ag_layout* layout, const double* theta, int32_t n,
+                          const ag_station_set* stations, double norm, const int32_t* index,
+                          const int32_t* count, double* llk, uint32_t* chain_status,
+                          float* residuals, void* workspace, size_t workspace_bytes, void* stream);
+
+/*
  * CDM geometry check only: chain_status[i] |= AG_CHAIN_ABOVE_SURFACE where a
  * corner of the CDM lies above the free surface (models/cdm/cdm/libcdm.py:219-224).
  */
@@ -230,6 +241,56 @@ int ag_adapt_scaling(const ag_stage_state* st, double aw, double rw, void* strea
 /* posterior = prior + β data (altar/altar/models/Bayesian.py:105-115). */
 int ag_posterior(const ag_stage_state* st, int32_t n, const double* prior, const double* data,
                  double* post, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Learned surrogate and delayed acceptance.  No counterpart in the reference:
+ * an MLP maps normalised source parameters to PCA coefficients of the LOS
+ * field; it screens proposals (stage 1) before the exact model (stage 2).
+ * Parameters: one FP32 buffer, per layer W (out x in, row-major) then b (out);
+ * a BF16 copy of the same buffer feeds the products (FP32 accumulation).
+ */
+#define AG_MLP_MAX_LAYERS 8
+typedef struct ag_mlp {
+    int32_t nlayers;                        /* dense layers; GELU after all but the last */
+    int32_t sizes[AG_MLP_MAX_LAYERS + 1];   /* input, hidden..., output widths */
+} ag_mlp;
+
+/* number of FP32 parameters (weights and biases) */
+int64_t ag_mlp_param_count(const ag_mlp* net);
+/* floats of activation storage ag_mlp_forward needs for n rows */
+int64_t ag_mlp_activation_floats(const ag_mlp* net, int32_t n);
+/* x = 2 (θ - lo)/(hi - lo) - 1 as FP32 (n x p) */
+int ag_normalize_inputs(const double* theta, int32_t n, int32_t p, const double* lo,
+                        const double* hi, float* x, void* stream);
+/* out (n x sizes[nlayers]) = MLP(x); acts keeps pre- and post-activations for the backward pass */
+int ag_mlp_forward(const ag_mlp* net, const float* params, const uint16_t* params_bf16,
+                   const float* x, int32_t n, float* out, float* acts, void* stream);
+/* gradients of the loss whose output gradient is dout (overwritten); scratch: 2 n max-width floats */
+int ag_mlp_backward(const ag_mlp* net, const float* params, const uint16_t* params_bf16,
+                    const float* x, int32_t n, const float* acts, float* dout, float* grads,
+                    float* scratch, void* stream);
+/* dout = (out - target)/n; row_loss[i] = 1/2 |out_i - target_i|² (optional) */
+int ag_mse_grad(int32_t n, int32_t k, const float* out, const float* target, float* dout,
+                float* row_loss, void* stream);
+/* one Adam step (step number t >= 1) on the FP32 parameters; refreshes the BF16 copy if given */
+int ag_adam_step(int64_t count, float* params, const float* grads, float* m, float* v, int32_t t,
+                 float lr, float b1, float b2, float eps, uint16_t* params_bf16, void* stream);
+/* BF16 copy of an FP32 buffer */
+int ag_to_bf16(int64_t count, const float* src, uint16_t* dst, void* stream);
+/* llk = norm - 1/2 (q0 - 2 hᵀ c̃ + c̃ᵀ G c̃) with c̃ = scale ⊙ coeff (n x k) */
+int ag_surrogate_llk(int32_t n, int32_t k, const float* coeff, const float* scale, const float* gram,
+                     const float* h, double q0, double norm, double* llk, void* stream);
+/* delayed-acceptance stage 1 (Christen & Fox 2005): surrogate Metropolis test; survivors are
+ * listed in index[0 .. *count) */
+int ag_da_screen(const ag_stage_state* st, int32_t n, uint64_t seed, uint32_t step,
+                 const uint32_t* mask, const double* cprior, const double* csur, const double* prior,
+                 const double* sur, int32_t* pass, int32_t* index, int32_t* count, void* stream);
+/* delayed-acceptance stage 2: exact correction of the survivors; counters as ag_accept,
+ * *screened (optional) counts the survivors */
+int ag_da_accept(const ag_stage_state* st, int32_t n, int32_t p, uint64_t seed, uint32_t step,
+                 const uint32_t* mask, const int32_t* pass, const double* cand, const double* cprior,
+                 const double* cdata, const double* csur, double* theta, double* prior, double* data,
+                 double* post, double* sur, unsigned long long* screened, void* stream);
 
 /* CUDA graph capture of a sequence of calls on one stream. */
 int ag_graph_begin(void* stream);
