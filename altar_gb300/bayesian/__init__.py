@@ -6,6 +6,7 @@ from .grid import Grid
 from .cov import COV
 from .annealing import CUDAAnnealing
 from .annealer import Annealer
+from .surrogate import DelayedAcceptance, Surrogate
 
 __all__ = ["CoolingStep", "StageState", "Notifier", "Profiler", "Metropolis", "Grid", "COV",
-           "CUDAAnnealing", "Annealer"]
+           "CUDAAnnealing", "Annealer", "DelayedAcceptance", "Surrogate"]

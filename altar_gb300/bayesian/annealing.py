@@ -75,7 +75,13 @@ class CUDAAnnealing:
         return self
 
     def walk(self, annealer):
-        self._phase("walk", lambda: annealer.sampler.samplePosterior(annealer=annealer, step=self.step))
+        sampler = annealer.sampler
+        sampler.prepare(annealer=annealer, step=self.step)
+        run = lambda: sampler.samplePosterior(annealer=annealer, step=self.step)
+        if sampler.capturable:
+            self._phase("walk:" + sampler.mode_key(), run)
+        else:
+            run()
         return self.step.state.counters
 
     def resample(self, annealer, statistics):
@@ -91,6 +97,7 @@ class CUDAAnnealing:
         rep = {"stage": self.iteration, "beta": float(scal[0]), "dbeta": float(scal[1]),
                "cov": float(scal[2]), "scaling": float(self.step.state.scaling.item()),
                "accepted": acc, "rejected": rej, "unlikely": unl, "flags": int(flags[0])}
+        rep.update(annealer.sampler.report())
         self.reports.append(rep)
         if rep["flags"] & _native.AG_DEV_ERR_TIMEOUT:
             raise RuntimeError("a device wait timed out during the stage")

@@ -34,6 +34,19 @@ class Metropolis:
                          torch.zeros(n, dtype=torch.int32, device=DEVICE))
         return self._buf
 
+    # hooks of the annealing worker: host-side decisions before a walk, and the
+    # key under which the walk's launch sequence is captured
+    capturable = True
+
+    def prepare(self, annealer, step):
+        return self
+
+    def mode_key(self):
+        return "mh"
+
+    def report(self):
+        return {}
+
     def prime(self, step):
         """Set the initial proposal scaling on the device."""
         step.state.scaling.fill_(self.scaling)

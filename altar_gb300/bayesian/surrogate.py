@@ -199,9 +199,20 @@ class DelayedAcceptance(Metropolis):
     def mode_key(self):
         return self.mode
 
-    def samplePosterior(self, annealer, step):
+    def prepare(self, annealer, step):
+        """Host-side decisions before a walk: train when collection ends, check the surrogate."""
         self._choose_mode(annealer, step)
-        return super().samplePosterior(annealer, step)
+        if self.screened is not None:
+            self.screened.zero_()
+        return self
+
+    def report(self):
+        rep = {"mode": self.mode, "samples": self.surrogate.count}
+        if self.rms_history and self.mode != "collect":
+            rep["rms_sigma"] = self.rms_history[-1]
+        if self.mode == "da" and self.screened is not None:
+            rep["screened"] = int(self.screened.item())
+        return rep
 
     def _choose_mode(self, annealer, step):
         sur = self.surrogate

@@ -180,6 +180,54 @@ def run_reference(args):
     return 0
 
 
+def cdm_psets():
+    from altar_gb300.distributions import Uniform
+    from altar_gb300.models import Contiguous
+    names = ["location", "depth", "opening", "a", "omega"]
+    counts = [2, 1, 1, 3, 3]
+    bounds = [PRIORS[0], PRIORS[2], PRIORS[3], PRIORS[4], PRIORS[7]]
+    return {nm: Contiguous(c, Uniform(b)) for nm, c, b in zip(names, counts, bounds)}
+
+
+def anneal(kind, X, Y, los, d, N, rank, args):
+    """One CATMIP run to β = 1 with the plain or the delayed-acceptance sampler."""
+    import torch
+    from altar_gb300 import Application
+    from altar_gb300.bayesian import Annealer, DelayedAcceptance, Surrogate
+    from altar_gb300.models import CDM
+    from altar_gb300.models.observations import Observations
+    from altar_gb300.simulations import RNG, Job
+    sampler = None
+    if kind == "da":
+        sampler = DelayedAcceptance(surrogate=Surrogate(seed=5), collect_until_beta=args.collect_beta,
+                                    max_samples=args.max_samples, rms_limit=args.rms_limit, epochs=args.epochs)
+    model = CDM(cdm_psets(), observations=Observations(X, Y, los, d, SIGMA ** 2))
+    app = Application(model, job=Job(chains=N, steps=5), rng=RNG(1234 + rank),
+                      controller=Annealer(sampler=sampler))
+    app.initialize()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    app.controller.posterior(model, max_stages=args.max_stages)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    worker = app.controller.worker
+    reps = worker.reports
+    th = worker.step.theta.cpu().numpy()
+    steps = sum(r["accepted"] + r["rejected"] + r["unlikely"] for r in reps)
+    res = {"time_s": dt, "stages": len(reps), "final_beta": reps[-1]["beta"] if reps else None,
+           "chain_steps": steps, "chain_steps_per_s": steps / dt,
+           "mean": th.mean(0).tolist(), "sd": th.std(0).tolist(),
+           "acceptance": [r["accepted"] / max(1, r["accepted"] + r["rejected"] + r["unlikely"]) for r in reps],
+           "betas": [r["beta"] for r in reps]}
+    if kind == "da":
+        res["modes"] = [r.get("mode") for r in reps]
+        res["rms_sigma"] = [r.get("rms_sigma") for r in reps]
+        res["screened"] = [r.get("screened") for r in reps]
+        res["train_losses"] = sampler.surrogate.losses
+        res["samples"] = sampler.surrogate.count
+    return res
+
+
 def run_ours(args):
     import torch
     rank, world, local, dist = dist_setup()
@@ -198,28 +246,34 @@ def run_ours(args):
     counts = [2, 1, 1, 3, 3]
     bounds = [PRIORS[0], PRIORS[2], PRIORS[3], PRIORS[4], PRIORS[7]]
     psets = {nm: Contiguous(c, Uniform(b)) for nm, c, b in zip(names, counts, bounds)}
+    if args.mode in ("anneal", "compare"):
+        runs = ["plain", "da"] if args.mode == "compare" else [args.sampler]
+        out = {}
+        for kind in runs:
+            out[kind] = anneal(kind, X, Y, los, d, N, rank, args)
+        line = {"metric": "CDM time-to-beta=1", "unit": "s", "n_gpus": world, "higher_is_better": False,
+                "config": {"workload": "cdm-40k-obs", "chains": N, "stations": X.size, "steps_per_stage": 5,
+                           "truth": truth.tolist()},
+                "runs": out}
+        if "plain" in out and "da" in out:
+            a, b = out["plain"], out["da"]
+            line["value"] = b["time_s"]
+            line["speedup_da_vs_plain"] = a["time_s"] / b["time_s"]
+            sd = np.array(a["sd"])
+            line["posterior_mean_diff_in_sd"] = (np.abs(np.array(a["mean"]) - np.array(b["mean"])) /
+                                                 np.where(sd > 0, sd, 1)).tolist()
+        else:
+            line["value"] = out[runs[0]]["time_s"]
+        if rank == 0:
+            print(json.dumps(line))
+        return 0
+
     model = CDM(psets, observations=Observations(X, Y, los, d, SIGMA ** 2))
     app = Application(model, job=Job(chains=N, steps=5), rng=RNG(1234 + rank))
     app.initialize()
     ann = app.controller
     worker = ann.worker
     stream = worker.stream
-
-    if args.mode == "anneal":
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        ann.posterior(model)
-        torch.cuda.synchronize()
-        dt = time.perf_counter() - t0
-        reps = worker.reports
-        steps = sum(r["accepted"] + r["rejected"] + r["unlikely"] for r in reps)
-        line = {"metric": "CDM time-to-beta=1", "value": dt, "unit": "s", "n_gpus": world,
-                "stages": len(reps), "chain_steps": steps, "chain_steps_per_s": steps / dt,
-                "higher_is_better": False, "final_beta": reps[-1]["beta"] if reps else None,
-                "config": {"workload": "cdm-40k-obs", "chains": N, "stations": X.size, "steps_per_stage": 5}}
-        if rank == 0:
-            print(json.dumps(line))
-        return 0
 
     samp = ann.sampler
     S = app.job.steps
@@ -348,7 +402,13 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--mode", default="walk", choices=["walk", "anneal"])
+    ap.add_argument("--mode", default="walk", choices=["walk", "anneal", "compare"])
+    ap.add_argument("--sampler", default="plain", choices=["plain", "da"])
+    ap.add_argument("--max-stages", type=int, default=400)
+    ap.add_argument("--collect-beta", type=float, default=0.05)
+    ap.add_argument("--max-samples", type=int, default=2_000_000)
+    ap.add_argument("--rms-limit", type=float, default=0.5)
+    ap.add_argument("--epochs", type=int, default=8)
     ap.add_argument("--chains", type=int, default=32768)
     ap.add_argument("--cpu-chains", type=int, default=128)
     args = ap.parse_args()
