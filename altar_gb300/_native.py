@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "_lib")
 LIBPATH = os.path.join(LIBDIR, "libaltar_gb300.so")
-SOURCES = ("forward.cu", "stage.cu", "surrogate.cu", "api.cu")
+SOURCES = ("forward.cu", "stage.cu", "surrogate.cu", "linear.cu", "api.cu")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 
@@ -98,6 +98,10 @@ class Layout(ctypes.Structure):
                 ("source_stride", c_int32), ("nu", c_double)]
 
 
+class LinearModel(ctypes.Structure):
+    _fields_ = [("a64", c_void_p), ("b64", c_void_p), ("a_split", c_void_p), ("m_obs", c_int32), ("p", c_int32)]
+
+
 class MLP(ctypes.Structure):
     _fields_ = [("nlayers", c_int32), ("sizes", c_int32 * 9)]
 
@@ -116,6 +120,11 @@ _SIGNATURES = {
     "ag_forward_llk": (c_int, [c_int, P, P, c_int32, P, c_double, P, P, P, P, P, c_size_t, P]),
     "ag_cdm_check": (c_int, [P, P, c_int32, P, P]),
     "ag_forward_llk_subset": (c_int, [c_int, P, P, c_int32, P, c_double, P, P, P, P, P, P, c_size_t, P]),
+    "ag_linear_kpad": (c_int32, [c_int32]),
+    "ag_linear_prepare": (c_int, [P, c_int32, c_int32, P, P]),
+    "ag_linear_workspace_bytes": (c_size_t, [c_int32, c_int32, c_int32]),
+    "ag_linear_llk": (c_int, [P, P, c_int32, c_double, P, P, c_size_t, P, P]),
+    "ag_linear_llk_fp64": (c_int, [P, P, c_int32, c_double, P, P]),
     "ag_mlp_param_count": (ctypes.c_int64, [P]),
     "ag_mlp_activation_floats": (ctypes.c_int64, [P, c_int32]),
     "ag_normalize_inputs": (c_int, [P, c_int32, c_int32, P, P, P, P]),

@@ -1,18 +1,23 @@
 """Learned surrogate of the forward field and the delayed-acceptance sampler.
 
-No counterpart in the reference.  The surrogate maps normalised source
-parameters to K PCA coefficients of the LOS displacement field:
+No counterpart in the reference.  The surrogate maps source parameters,
+normalised by the current population's mean and spread, to K PCA
+coefficients of the LOS displacement field:
   * the PCA basis (mean field μ, orthonormal B, per-component scales) comes
-    from exact fields the sampler evaluated in its first stages (Gram matrix
-    of a subset and its leading eigenvectors, computed once as set-up);
-  * training pairs (θ, Bᵀ(u(θ) - μ)/scale) are collected from every exact
-    evaluation while β is below ``collect_until_beta`` (up to ``max_samples``);
+    from exact fields of a subset of the current population (randomised range
+    finder: B from the leading right singular vectors of the centred fields);
+  * training pairs (θ, Bᵀ(u(θ) - μ)/scale) come from those exact evaluations;
   * the network (10 → 4×256 GELU → 64) is trained by the library's own
-    forward, backward and Adam kernels (``ag_mlp_*``, ``ag_adam_step``);
+    forward, backward and Adam kernels (``ag_mlp_*``, ``ag_adam_step``),
+    warm-started from the previous stage's weights;
   * its data log-likelihood is evaluated in PCA space (``ag_surrogate_llk``).
+A surrogate fitted once over the whole prior is far too coarse for the late,
+concentrated populations (measured RMS field error ~4σ on the CDM workload),
+so the fit is local to each stage's population and refreshed whenever the
+check below fails.
 
-``DelayedAcceptance`` is a Metropolis sampler that, once the surrogate is
-trained and its RMS field error on the current population is below
+``DelayedAcceptance`` is a Metropolis sampler that, when the surrogate's RMS
+field error on held-out chains of the current population is below
 ``rms_limit`` data standard deviations, screens every proposal on the
 surrogate posterior and evaluates the exact model only on the survivors
 (Christen & Fox 2005); otherwise it walks exactly like ``Metropolis``.
@@ -65,24 +70,42 @@ class Surrogate:
         _native.call("ag_to_bf16", self.params.numel(), ptr(self.params), ptr(self.pbf), stream_handle())
 
     # ---- PCA basis of the LOS fields
-    def fit_basis(self, fields, weight, d, norm, sample=4096):
-        """fields: (S, Mp) exact LOS fields (padding columns have weight 0)."""
-        F = fields[:sample].to(torch.float64)
+    def fit_basis(self, fields, weight, d, norm, oversample=8):
+        """Local PCA of exact fields (S, Mp) by a randomised range finder (set-up GEMMs).
+
+        The basis tensors keep their device addresses across refits, so captured
+        graphs that read them stay valid.
+        """
+        F = fields.to(torch.float32)
         mu = F.mean(0)
         Fc = F - mu
-        gram = Fc @ Fc.T
-        evals, evecs = torch.linalg.eigh(gram)
-        idx = torch.argsort(evals, descending=True)[: self.k]
-        lam = evals[idx].clamp_min(1e-300)
-        B = (Fc.T @ evecs[:, idx]) / torch.sqrt(lam)           # orthonormal columns
-        scale = torch.sqrt(lam / F.shape[0])                      # std of each coefficient
+        k = min(self.k, F.shape[0] - 1)
+        gen = torch.Generator(device=DEVICE)
+        gen.manual_seed(self.seed + 7)
+        omega = torch.randn(F.shape[1], k + oversample, device=DEVICE, generator=gen)
+        Q, _ = torch.linalg.qr(Fc @ omega)                         # (S, k+o) range of the fields
+        Bt = (Q.T @ Fc).double()                                   # (k+o, Mp)
+        evals, evecs = torch.linalg.eigh(Bt @ Bt.T)
+        idx = torch.argsort(evals, descending=True)[:k]
+        lam = evals[idx].clamp_min(1e-30)
+        B = (Bt.T @ evecs[:, idx]) / torch.sqrt(lam)              # orthonormal columns (Mp, k)
+        scale = torch.sqrt(lam / F.shape[0]).clamp_min(1e-12)     # std of each coefficient
+        if k < self.k:                                             # pad unused components
+            B = torch.cat([B, torch.zeros(B.shape[0], self.k - k, dtype=B.dtype, device=DEVICE)], 1)
+            scale = torch.cat([scale, torch.ones(self.k - k, dtype=scale.dtype, device=DEVICE)])
         w = weight.to(torch.float64)
         dd = d.to(torch.float64)
+        mu64 = mu.double()
         G = B.T @ (w[:, None] * B)
-        h = B.T @ (w * (dd - mu))
-        q0 = float(((mu - dd) ** 2 * w).sum())
-        self.basis = dict(mu=mu.float(), B=B.float(), scale=scale.float(), G=G.float(), h=h.float(), q0=q0,
-                          norm=float(norm), explained=float(lam.sum() / evals.clamp_min(0).sum()))
+        h = B.T @ (w * (dd - mu64))
+        q0 = float(((mu64 - dd) ** 2 * w).sum())
+        new = dict(mu=mu, B=B.float(), scale=scale.float(), G=G.float(), h=h.float())
+        if self.basis is None:
+            self.basis = {key: v.clone() for key, v in new.items()}
+        else:
+            for key, v in new.items():
+                self.basis[key].copy_(v)
+        self.basis.update(q0=q0, norm=float(norm))
         return self.basis
 
     def coefficients(self, fields):
@@ -172,126 +195,116 @@ class Surrogate:
 class DelayedAcceptance(Metropolis):
     """Metropolis with a surrogate screen (stage 1) before the exact model (stage 2)."""
 
-    def __init__(self, surrogate=None, collect_until_beta=0.05, max_samples=2_000_000, rms_limit=0.5,
-                 epochs=8, collect_per_step=8192, **kwds):
+    def __init__(self, surrogate=None, rms_limit=0.5, fit_chains=4096, check_chains=256, epochs=40,
+                 start_beta=0.0, retry_every=3, spread=3.0, **kwds):
         super().__init__(**kwds)
-        self.surrogate = surrogate if surrogate is not None else Surrogate()
-        self.collect_until_beta = collect_until_beta
-        self.max_samples = max_samples
-        self.rms_limit = rms_limit
-        self.epochs = epochs
-        self.collect_per_step = collect_per_step
-        self.mode = "collect"
-        self.rms_history = []
+        self.surrogate = surrogate if surrogate is not None else Surrogate(batch=1024)
+        self.rms_limit = float(rms_limit)
+        self.fit_chains, self.check_chains = int(fit_chains), int(check_chains)
+        self.epochs, self.start_beta = int(epochs), float(start_beta)
+        self.retry_every, self.spread = int(retry_every), float(spread)
+        self.mode = "plain"
+        self.rms = None
+        self.refits = 0
         self.screened = None
-        self._resid = None
+        self._stage = 0
+        self._last_try = -10 ** 9
+        self._bounds = None
         self._sbufs = None
 
-    @property
-    def capturable(self):
-        return self.mode != "collect"
-
-    def initialize(self, application):
-        super().initialize(application)
-        return self
-
-    # graphs: the worker keys captured walks by mode
     def mode_key(self):
         return self.mode
 
-    def prepare(self, annealer, step):
-        """Host-side decisions before a walk: train when collection ends, check the surrogate."""
-        self._choose_mode(annealer, step)
-        if self.screened is not None:
-            self.screened.zero_()
-        return self
-
     def report(self):
-        rep = {"mode": self.mode, "samples": self.surrogate.count}
-        if self.rms_history and self.mode != "collect":
-            rep["rms_sigma"] = self.rms_history[-1]
+        rep = {"mode": self.mode, "rms_sigma": self.rms, "refits": self.refits}
         if self.mode == "da" and self.screened is not None:
             rep["screened"] = int(self.screened.item())
         return rep
 
-    def _choose_mode(self, annealer, step):
+    # ---- per-stage host decisions (eager, before the walk graph)
+    def prepare(self, annealer, step):
+        self._stage += 1
+        if self.screened is not None:
+            self.screened.zero_()
+        if step.beta < self.start_beta:
+            self.mode = "plain"
+            return self
+        model, strat = annealer.model, annealer.model.strategy
         sur = self.surrogate
-        if self.mode == "collect":
-            beta = step.beta
-            if (beta >= self.collect_until_beta or sur.full) and sur.count > 0:
-                sur.train(epochs=self.epochs)
+        n, p = step.samples, step.parameters
+        fit = min(self.fit_chains, n // 2)
+        chk = min(self.check_chains, n - fit)
+        stride = max(1, n // (fit + chk))
+        rows = torch.arange(0, n, stride, device=DEVICE)[: fit + chk]
+        fit_rows, chk_rows = rows[:fit], rows[fit:fit + chk]
+        if sur.trained:
+            self.rms = self._check(annealer, step, chk_rows)
+            if self.rms <= self.rms_limit:
                 self.mode = "da"
-            else:
-                return
-        # per-stage check of the surrogate on the current population
-        rms = self.field_rms(annealer, step)
-        self.rms_history.append(rms)
-        self.mode = "da" if rms <= self.rms_limit else "plain"
+                return self
+            if self.rms > 4 * self.rms_limit and self._stage - self._last_try < self.retry_every:
+                self.mode = "plain"
+                return self
+        self._last_try = self._stage
+        self._refit(annealer, step, fit_rows)
+        self.rms = self._check(annealer, step, chk_rows)
+        self.mode = "da" if self.rms <= self.rms_limit else "plain"
+        return self
 
-    def field_rms(self, annealer, step, count=256):
-        """RMS of surrogate minus exact LOS field over stations, in data standard deviations."""
-        model = annealer.model
-        strat = model.strategy
-        th = step.theta[:count].contiguous()
-        n = th.shape[0]
-        mp = strat.stations.m_padded
-        res = torch.zeros(n, mp, dtype=torch.float32, device=DEVICE)
+    def _fields(self, strat, theta):
+        n = theta.shape[0]
+        res = torch.zeros(n, strat.stations.m_padded, dtype=torch.float32, device=DEVICE)
         out = torch.empty(n, dtype=torch.float64, device=DEVICE)
-        strat.forward(th, out, residuals=res)
-        exact = res + strat.stations.losd[:, 3]
-        bufs = self.surrogate.buffers(n, th.shape[1])
-        sur_llk = torch.empty(n, dtype=torch.float64, device=DEVICE)
-        self.surrogate.predict(th, model.lo, model.hi, sur_llk, bufs)
-        approx = self.surrogate.reconstruct(bufs[1])
+        strat.forward(theta, out, residuals=res)
+        return res + strat.stations.losd[:, 3]
+
+    def _set_bounds(self, step):
+        th = step.theta
+        mean = th.mean(0)
+        sd = th.std(0)
+        width = torch.maximum(self.spread * sd, 1e-9 * (mean.abs() + 1.0))
+        lo, hi = mean - width, mean + width
+        if self._bounds is None:
+            self._bounds = (lo.clone(), hi.clone())
+        else:
+            self._bounds[0].copy_(lo)
+            self._bounds[1].copy_(hi)
+
+    def _refit(self, annealer, step, rows):
+        model, strat, sur = annealer.model, annealer.model.strategy, self.surrogate
+        th = step.theta.index_select(0, rows).contiguous()
+        self._set_bounds(step)
+        fields = self._fields(strat, th)
+        sur.fit_basis(fields, strat.stations.weight, strat.stations.losd[:, 3], strat.norm)
+        p = step.parameters
+        x = torch.empty(th.shape[0], p, dtype=torch.float32, device=DEVICE)
+        _native.call("ag_normalize_inputs", ptr(th), th.shape[0], p, ptr(self._bounds[0]), ptr(self._bounds[1]),
+                     ptr(x), stream_handle())
+        if sur.params is None:
+            sur.init_params()
+        sur.reserve(th.shape[0], p)
+        sur.add(x, sur.coefficients(fields))
+        sur.train(epochs=self.epochs)
+        self.refits += 1
+
+    def _check(self, annealer, step, rows):
+        """RMS of surrogate minus exact LOS field over stations, in data standard deviations."""
+        strat, sur = annealer.model.strategy, self.surrogate
+        th = step.theta.index_select(0, rows).contiguous()
+        exact = self._fields(strat, th)
+        bufs = sur.buffers(th.shape[0], th.shape[1])
+        tmp = torch.empty(th.shape[0], dtype=torch.float64, device=DEVICE)
+        sur.predict(th, self._bounds[0], self._bounds[1], tmp, bufs)
+        approx = sur.reconstruct(bufs[1])
         w = strat.stations.weight
-        m = strat.stations.m
-        err2 = ((approx - exact) ** 2 * w).sum(1) / m
+        err2 = ((approx - exact) ** 2 * w).sum(1) / strat.stations.m
         return float(torch.sqrt(err2.mean()))
 
+    # ---- walks
     def walkChains(self, annealer, step):
-        if self.mode == "collect":
-            return self._walk_collect(annealer, step)
         if self.mode == "da":
             return self._walk_da(annealer, step)
         return super().walkChains(annealer, step)
-
-    def _walk_collect(self, annealer, step):
-        """Exact walk that also records (θ, PCA coefficients) pairs for training."""
-        model = annealer.model
-        strat = model.strategy
-        sur = self.surrogate
-        n, p = step.samples, step.parameters
-        cand, cprior, cdata, mask = self._buffers(n, p)
-        mp = strat.stations.m_padded
-        nc = min(n, self.collect_per_step)
-        if self._resid is None or self._resid.shape != (nc, mp):
-            self._resid = torch.zeros(nc, mp, dtype=torch.float32, device=DEVICE)
-        st = step.state.struct
-        s = stream_handle()
-        dobs = strat.stations.losd[:, 3]
-        for k in range(self.steps):
-            _native.call("ag_propose", st, ptr(step.theta), n, p, ptr(model.lo), ptr(model.hi), self.seed, k,
-                         ptr(cand), ptr(mask), ptr(cprior), s)
-            strat.forward(cand, cdata, mask=mask, status=mask)
-            # fields of the first nc candidates (a second pass over a slice keeps the buffer small)
-            sub = cand[:nc]
-            tmp = torch.empty(nc, dtype=torch.float64, device=DEVICE)
-            strat.forward(sub, tmp, mask=mask[:nc], residuals=self._resid)
-            valid = mask[:nc] == 0
-            fields = (self._resid + dobs)[valid]
-            if sur.basis is None:
-                sur.fit_basis(fields, strat.stations.weight, dobs, strat.norm)
-                sur.reserve(self.max_samples, p)
-                sur.init_params()
-            if not sur.full and fields.shape[0] > 0:
-                xb = torch.empty(fields.shape[0], p, dtype=torch.float32, device=DEVICE)
-                thv = sub[valid].contiguous()
-                _native.call("ag_normalize_inputs", ptr(thv), thv.shape[0], p, ptr(model.lo), ptr(model.hi),
-                             ptr(xb), s)
-                sur.add(xb, sur.coefficients(fields))
-            _native.call("ag_accept", st, n, p, self.seed, k, ptr(mask), ptr(cand), ptr(cprior), ptr(cdata),
-                         ptr(step.theta), ptr(step.prior), ptr(step.data), ptr(step.posterior), s)
-        return step.state.counters
 
     def _walk_da(self, annealer, step):
         model = annealer.model
@@ -299,7 +312,7 @@ class DelayedAcceptance(Metropolis):
         sur = self.surrogate
         n, p = step.samples, step.parameters
         cand, cprior, cdata, mask = self._buffers(n, p)
-        if self._sbufs is None or self._sbufs[0].shape[0] != n:
+        if self._sbufs is None or self._sbufs[1].shape[0] != n:
             self._sbufs = (sur.buffers(n, p), torch.empty(n, dtype=torch.float64, device=DEVICE),
                            torch.empty(n, dtype=torch.float64, device=DEVICE),
                            torch.empty(n, dtype=torch.int32, device=DEVICE),
@@ -308,16 +321,17 @@ class DelayedAcceptance(Metropolis):
                            torch.zeros(1, dtype=torch.int64, device=DEVICE))
         bufs, sur_cur, sur_cand, passed, index, count, screened = self._sbufs
         self.screened = screened
+        lo, hi = self._bounds
         st = step.state.struct
         s = stream_handle()
-        sur.predict(step.theta, model.lo, model.hi, sur_cur, bufs)
+        # the constant parts of the surrogate log-likelihood (q0, norm) cancel in both stages
+        sur.predict(step.theta, lo, hi, sur_cur, bufs)
         for k in range(self.steps):
             _native.call("ag_propose", st, ptr(step.theta), n, p, ptr(model.lo), ptr(model.hi), self.seed, k,
                          ptr(cand), ptr(mask), ptr(cprior), s)
-            sur.predict(cand, model.lo, model.hi, sur_cand, bufs)
+            sur.predict(cand, lo, hi, sur_cand, bufs)
             _native.call("ag_da_screen", st, n, self.seed, k, ptr(mask), ptr(cprior), ptr(sur_cand),
                          ptr(step.prior), ptr(sur_cur), ptr(passed), ptr(index), ptr(count), s)
-            strat.reserve(n)
             _native.call("ag_forward_llk_subset", strat.kind, ctypes.byref(strat.layout), ptr(cand), n,
                          strat.stations.struct, strat.norm, ptr(index), ptr(count), ptr(cdata), ptr(mask), None,
                          ptr(strat._ws), strat._ws_bytes, s)

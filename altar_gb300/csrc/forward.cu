@@ -310,65 +310,56 @@ AG_DEVICE_INLINE void side_pair(const SideC& S, float Xr, float Yr, float& ue, f
     const float dm4 = fmaf(dm2, m1B, m2A * dm1);
     const float dm5 = dm2 * (m2A + m2B);
     const float dm6 = dm1 * (m1A + m1B);
-    const float y1irA = y1A * irA, y1irB = y1B * irB, dy1ir = fmaf(dy1, irB, y1A * dir);
-    const float y2irA = y2 * irA, y2irB = y2 * irB, dy2ir = y2 * dir;
-    const float airA = aA * irA, airB = aB * irB, dair = fmaf(da, irB, aA * dir);
-    const float dm7 = fmaf(dy1ir, m1B, y1irA * dm1);
-    const float dm8 = fmaf(dy1ir, m2B, y1irA * dm2);
-    const float dm9 = fmaf(dy2ir, m1B, y2irA * dm1);
-    const float m10A = y2 * iqA, m10B = y2 * iqB, dm10 = y2 * diq;
-    const float m11A = z1A * iqA, m11B = z1B * iqB, dm11 = fmaf(dz1, iqB, z1A * diq);
-    const float dm12 = fmaf(dy1ir, m10B, y1irA * dm10);
-    const float dm13 = fmaf(dy1ir, m11B, y1irA * dm11);
-    const float dm14 = fmaf(dy2ir, m10B, y2irA * dm10);
-    const float dm15 = fmaf(dy2ir, m11B, y2irA * dm11);
-    const float dm16 = fmaf(dair, m1B, airA * dm1);
-    const float dm17 = fmaf(dair, m2B, airA * dm2);
-    const float dm18 = fmaf(dair, m10B, airA * dm10);
-    const float dm19 = fmaf(dair, m11B, airA * dm11);
-    (void)airB; (void)y2irB; (void)y1irB; (void)m10A; (void)m11A;
-    // combination (coefficients precomputed per side; configuration sign applied last)
+    const float y1irA = y1A * irA, dy1ir = fmaf(dy1, irB, y1A * dir);
+    const float y2irA = y2 * irA, dy2ir = y2 * dir;
+    const float airA = aA * irA, dair = fmaf(da, irB, aA * dir);
+    const float m10B = y2 * iqB, dm10 = y2 * diq;
+    const float m11B = z1B * iqB, dm11 = fmaf(dz1, iqB, z1A * diq);
+    // coefficients (precomputed per side; configuration sign applied here)
     const float C1F = q3.y, C2F = q3.z, C3F = q3.w;
     const float C1P = q4.x, C2P = q4.y, kc1 = q4.z, kc2 = q4.w;
     const float nb1 = q5.x, nb2 = q5.y, hb1 = q5.z, hb2 = q5.w;
     const float b1 = q6.x, b2 = q6.y, C1m10 = q6.z, C3m10 = q6.w;
     const float C1Q = q7.x, C2Q = q7.y, C3Q = q7.z, C1m11 = q7.w;
-    const float C3m11 = q8.x, C1m12 = q8.y;
+    const float C3m11 = q8.x;
+    const float c12 = sg * q8.y;                       // signed coefficient of the (m10 · r⁻¹) products
+    // The r⁻¹-weighted monomials share two brackets (distributivity of Δ(u v) = Δu v_B + u_A Δv):
+    //   v1: -b1 Δ(y1 r⁻¹ m1) + b2 Δ(y1 r⁻¹ m2) - b2 Δ(y1 r⁻¹ m11) + c12 Δ(y1 r⁻¹ m10)
+    //       = Δ(y1 r⁻¹)·X1 + (y1 r⁻¹)_A·ΔX1
+    //   v3: the same brackets with a r⁻¹ in place of y1 r⁻¹, negated
+    //   v2: b2 Δ(y1 r⁻¹ m1) + Δ(y2 r⁻¹)·X2 + (y2 r⁻¹)_A·ΔX2
+    const float X2 = fmaf(-b1, m1B, fmaf(-b2, m11B, c12 * m10B));
+    const float dX2 = fmaf(-b1, dm1, fmaf(-b2, dm11, c12 * dm10));
+    const float X1 = fmaf(b2, m2B, X2);
+    const float dX1 = fmaf(b2, dm2, dX2);
     float v1 = C1F * dF;
     v1 = fmaf(C1P, dLp, v1);
     v1 = fmaf(kc1, dm1, v1);
     v1 = fmaf(-kc2, dm2, v1);
     v1 = fmaf(-hb2, dm3 + dm5, v1);
     v1 = fmaf(hb1, dm4, v1);
-    v1 = fmaf(-b1, dm7, v1);
-    v1 = fmaf(b2, dm8 - dm13, v1);
     v1 = fmaf(C1m10, dm10, v1);
-    float w1 = C1Q * dLq;
-    w1 = fmaf(C1m11, dm11, w1);
-    w1 = fmaf(C1m12, dm12, w1);
-    v1 = fmaf(sg, w1, v1);
+    v1 = fmaf(dy1ir, X1, v1);
+    v1 = fmaf(y1irA, dX1, v1);
+    v1 = fmaf(sg, fmaf(C1Q, dLq, C1m11 * dm11), v1);
     float v2 = C2F * dF;
     v2 = fmaf(C2P, dLp, v2);
     v2 = fmaf(-kc2, dm1, v2);
     v2 = fmaf(-kc1, dm2, v2);
     v2 = fmaf(hb1, dm3 + dm6, v2);
     v2 = fmaf(-hb2, dm4, v2);
-    v2 = fmaf(b2, dm7 - dm15, v2);
-    v2 = fmaf(-b1, dm9, v2);
-    float w2 = C2Q * dLq;
-    w2 = fmaf(C1m12, dm14, w2);
-    v2 = fmaf(sg, w2, v2);
+    v2 = fmaf(b2, fmaf(dy1ir, m1B, y1irA * dm1), v2);
+    v2 = fmaf(dy2ir, X2, v2);
+    v2 = fmaf(y2irA, dX2, v2);
+    v2 = fmaf(sg * C2Q, dLq, v2);
     float v3 = C3F * dF;
     v3 = fmaf(-kc2, dLp, v3);
     v3 = fmaf(nb1, dm1, v3);
     v3 = fmaf(-nb2, dm2, v3);
     v3 = fmaf(C3m10, dm10, v3);
-    v3 = fmaf(b1, dm16, v3);
-    v3 = fmaf(b2, dm19 - dm17, v3);
-    float w3 = C3Q * dLq;
-    w3 = fmaf(C3m11, dm11, w3);
-    w3 = fmaf(-C1m12, dm18, w3);
-    v3 = fmaf(sg, w3, v3);
+    v3 = fmaf(-dair, X1, v3);
+    v3 = fmaf(-airA, dX1, v3);
+    v3 = fmaf(sg, fmaf(C3Q, dLq, C3m11 * dm11), v3);
     // back to EFCS: columns e1 = (c, s, 0), e2 = (s, -c, 0), e3 = (0, 0, -1)
     ue = fmaf(c, v1, fmaf(s, v2, ue));
     un = fmaf(s, v1, fmaf(-c, v2, un));

@@ -1,0 +1,379 @@
+// Linear Gaussian model on the 5th-generation tensor cores (tcgen05).
+//
+// The reference's linear model (models/linear/linear/Linear.py:152-185) forms
+// r = G θ - d with a dgemm and whitens each chain's residual.  Here the data
+// covariance is folded once into A = L⁻¹ G and b = L⁻¹ d (Cd = L Lᵀ), so that
+// rᵀ Cd⁻¹ r = |A θ - b|², and each chain's misfit is
+//     ρ = A (θ - θ₀) + ρ₀,   ρ₀ = A θ₀ - b  (FP64, the residual-correction pass),
+// with θ₀ the population mean: the tensor-core product only carries the
+// centred part.  A and δ = θ - θ₀ are split into BF16 pairs (x ≈ hi + lo) and
+// the product A δ is one GEMM over the concatenated K axis
+//     [δ_hi | δ_lo | δ_hi] · [A_hi | A_hi | A_lo]ᵀ
+// (three BF16 products, FP32 accumulation; the dropped lo·lo term is
+// ~2^-18 relative).  The GEMM is a tcgen05 kernel: TMA loads 128B-swizzled
+// K-major tiles into a 4-stage shared-memory ring guarded by mbarriers, one
+// thread issues tcgen05.mma (M = 128 chains, N = 256 observations, K = 16)
+// into a TMEM accumulator, and the epilogue reads TMEM with tcgen05.ld and
+// reduces Σ (acc + ρ₀)² per chain straight from registers.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "common.cuh"
+#include "internal.h"
+
+namespace ag {
+
+constexpr int TC_BM = 128;        // chains per tile (TMEM lanes)
+constexpr int TC_BN = 256;        // observations per tile (TMEM columns)
+constexpr int TC_BK = 64;         // K elements per stage (128 bytes of BF16: one swizzle row)
+constexpr int TC_STAGES = 4;
+constexpr uint32_t TC_A_BYTES = TC_BM * TC_BK * 2;   // 16 KB
+constexpr uint32_t TC_B_BYTES = TC_BN * TC_BK * 2;   // 32 KB
+constexpr uint32_t TC_STAGE_BYTES = TC_A_BYTES + TC_B_BYTES;
+constexpr uint32_t TC_SMEM = TC_STAGES * TC_STAGE_BYTES + 1024 /*align*/ + 1024 /*ρ₀*/ + 256 /*bars*/;
+constexpr uint32_t TC_WAIT = 1u << 26;
+
+// shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 B apart
+AG_DEVICE_INLINE uint64_t sw128_desc(uint32_t saddr) {
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+           ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+// instruction descriptor: D FP32, A and B BF16, both K-major, M x N
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+AG_DEVICE_INLINE void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+        ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar) : "memory");
+}
+
+AG_DEVICE_INLINE void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+        ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc) : "memory");
+}
+
+AG_DEVICE_INLINE void mma_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                 ::"r"(bar) : "memory");
+}
+
+AG_DEVICE_INLINE void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+AG_DEVICE_INLINE void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+AG_DEVICE_INLINE void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+          "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+          "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
+          "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// One CTA: 128 chains x 256 observations; partial[tile_n * n + chain] = Σ_obs (acc + ρ₀)²
+__global__ void __launch_bounds__(128, 1)
+linear_misfit_tc_kernel(const __grid_constant__ CUtensorMap map_a,   // chains  x K' (BF16)
+                        const __grid_constant__ CUtensorMap map_b,   // obs     x K' (BF16)
+                        int n, int m_obs, int kblocks, const float* __restrict__ rho0,
+                        double* __restrict__ partial, uint32_t* __restrict__ flags) {
+    extern __shared__ uint8_t smem_raw[];
+    const uint32_t raw = smem_addr(smem_raw);
+    const uint32_t base = (raw + 1023u) & ~1023u;
+    uint8_t* gbase = smem_raw + (base - raw);
+    float* s_rho = reinterpret_cast<float*>(gbase + TC_STAGES * TC_STAGE_BYTES);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(gbase + TC_STAGES * TC_STAGE_BYTES + 1024);
+    uint64_t* full = bars;                       // [TC_STAGES]
+    uint64_t* empty = bars + TC_STAGES;          // [TC_STAGES]
+    uint64_t* done = bars + 2 * TC_STAGES;       // [1]
+    __shared__ uint32_t s_tmem;
+    __shared__ int s_abort;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m0 = blockIdx.x * TC_BM;           // first chain
+    const int n0 = blockIdx.y * TC_BN;           // first observation
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < TC_STAGES; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(done, 1);
+        fence_mbar_init();
+        s_abort = 0;
+    }
+    for (int j = threadIdx.x; j < TC_BN; j += blockDim.x) s_rho[j] = (n0 + j < m_obs) ? rho0[n0 + j] : 0.f;
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     ::"r"(smem_addr(&s_tmem)), "r"(TC_BN) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = s_tmem;
+
+    if (threadIdx.x == 32) {
+        // TMA producer
+        for (int kb = 0; kb < kblocks; ++kb) {
+            const int s = kb % TC_STAGES;
+            if (kb >= TC_STAGES && !mbar_wait_bounded(&empty[s], ((kb / TC_STAGES) - 1) & 1, TC_WAIT)) {
+                atomicExch(&s_abort, 1);
+                break;
+            }
+            if (*(volatile int*)&s_abort) break;
+            const uint32_t sa = base + s * TC_STAGE_BYTES;
+            mbar_arrive_expect_tx(&full[s], TC_STAGE_BYTES);
+            tma_load_2d(sa, &map_a, kb * TC_BK, m0, smem_addr(&full[s]));
+            tma_load_2d(sa + TC_A_BYTES, &map_b, kb * TC_BK, n0, smem_addr(&full[s]));
+        }
+    } else if (threadIdx.x == 64) {
+        // MMA issuer
+        const uint32_t idesc = idesc_bf16(TC_BM, TC_BN);
+        int kb = 0;
+        for (; kb < kblocks; ++kb) {
+            const int s = kb % TC_STAGES;
+            if (!mbar_wait_bounded(&full[s], (kb / TC_STAGES) & 1, TC_WAIT)) {
+                atomicExch(&s_abort, 1);
+                break;
+            }
+            tc_fence_after();
+            const uint32_t sa = base + s * TC_STAGE_BYTES;
+            const uint64_t adesc = sw128_desc(sa), bdesc = sw128_desc(sa + TC_A_BYTES);
+#pragma unroll
+            for (int k = 0; k < TC_BK / 16; ++k)   // K = 16 per instruction: +32 bytes
+                mma_bf16(tmem, adesc + 2 * k, bdesc + 2 * k, idesc, (kb > 0 || k > 0) ? 1u : 0u);
+            mma_commit(smem_addr(&empty[s]));
+        }
+        mma_commit(smem_addr(done));           // fires when every issued MMA has completed
+    }
+    __syncwarp();
+    // epilogue: thread = chain row (TMEM lane), sums over the tile's observations
+    const bool ok = mbar_wait_bounded(done, 0, TC_WAIT);
+    tc_fence_after();
+    const int chain = m0 + warp * 32 + lane;
+    double acc = 0.0;
+    if (ok && !s_abort) {
+        const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+#pragma unroll 1
+        for (int c0 = 0; c0 < TC_BN; c0 += 32) {
+            float v[32];
+            tmem_ld32(tmem + lane_base + (uint32_t)c0, v);
+            float s = 0.f;
+#pragma unroll
+            for (int i = 0; i < 32; ++i) {
+                const float r = v[i] + s_rho[c0 + i];
+                s = (n0 + c0 + i < m_obs) ? fmaf(r, r, s) : s;
+            }
+            acc += (double)s;
+        }
+        if (chain < n) partial[(size_t)blockIdx.y * n + chain] = acc;
+    } else if (threadIdx.x == 0) {
+        raise_flag(flags, DEV_ERR_TIMEOUT);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_BN) : "memory");
+    }
+}
+
+// θ₀ = column means of θ (one thread per parameter, fixed order)
+__global__ void column_mean_kernel(const double* __restrict__ theta, int n, int p, double* __restrict__ mean) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= p) return;
+    double s = 0.0;
+    for (int i = 0; i < n; ++i) s += theta[(size_t)i * p + j];
+    mean[j] = s / n;
+}
+
+// ρ₀ = A θ₀ - b in FP64 (one warp per observation)
+__global__ void rho0_kernel(const double* __restrict__ A, const double* __restrict__ b,
+                            const double* __restrict__ theta0, int m, int p, float* __restrict__ rho0) {
+    const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (row >= m) return;
+    double s = 0.0;
+    for (int j = lane; j < p; j += 32) s = fma(A[(size_t)row * p + j], theta0[j], s);
+    s = warp_sum(s);
+    if (lane == 0) rho0[row] = (float)(s - b[row]);
+}
+
+// δ = θ - θ₀ split as [hi | lo | hi] (BF16, row length kp3 = 3 kp, kp = p padded to 64)
+__global__ void split_theta_kernel(const double* __restrict__ theta, const double* __restrict__ theta0,
+                                   int n, int p, int kp, __nv_bfloat16* __restrict__ out) {
+    const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (long)n * kp) return;
+    const int i = (int)(e / kp), j = (int)(e % kp);
+    float d = 0.f;
+    if (j < p) d = (float)(theta[(size_t)i * p + j] - theta0[j]);
+    const __nv_bfloat16 hi = __float2bfloat16_rn(d);
+    const __nv_bfloat16 lo = __float2bfloat16_rn(d - __bfloat162float(hi));
+    __nv_bfloat16* row = out + (size_t)i * 3 * kp;
+    row[j] = hi;
+    row[kp + j] = lo;
+    row[2 * kp + j] = hi;
+}
+
+// A split as [hi | hi | lo]
+__global__ void split_a_kernel(const double* __restrict__ A, int m, int p, int kp,
+                               __nv_bfloat16* __restrict__ out) {
+    const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (long)m * kp) return;
+    const int i = (int)(e / kp), j = (int)(e % kp);
+    const float a = (j < p) ? (float)A[(size_t)i * p + j] : 0.f;
+    const __nv_bfloat16 hi = __float2bfloat16_rn(a);
+    const __nv_bfloat16 lo = __float2bfloat16_rn(a - __bfloat162float(hi));
+    __nv_bfloat16* row = out + (size_t)i * 3 * kp;
+    row[j] = hi;
+    row[kp + j] = hi;
+    row[2 * kp + j] = lo;
+}
+
+__global__ void linear_reduce_kernel(int n, int tiles, const double* __restrict__ partial, double norm,
+                                     double* __restrict__ llk) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double s = 0.0;
+    for (int t = 0; t < tiles; ++t) s += partial[(size_t)t * n + i];
+    llk[i] = norm - 0.5 * s;
+}
+
+// Exact FP64 reference path: ρ = A θ - b per chain (one warp per chain, observations strided)
+__global__ void linear_fp64_kernel(const double* __restrict__ A, const double* __restrict__ b,
+                                   const double* __restrict__ theta, int n, int m, int p, double norm,
+                                   double* __restrict__ llk) {
+    const int chain = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (chain >= n) return;
+    const double* th = theta + (size_t)chain * p;
+    double acc = 0.0;
+    for (int r = lane; r < m; r += 32) {
+        double s = -b[r];
+        for (int j = 0; j < p; ++j) s = fma(A[(size_t)r * p + j], th[j], s);
+        acc = fma(s, s, acc);
+    }
+    acc = warp_sum(acc);
+    if (lane == 0) llk[chain] = norm - 0.5 * acc;
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn() {
+    static EncodeTiledFn fn = nullptr;
+    if (!fn) {
+        cudaDriverEntryPointQueryResult q;
+        void* p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    }
+    return fn;
+}
+
+// 2-D BF16 tensor map over rows x cols (row-major), box = box_rows x 64 columns, 128B swizzle
+static int make_map(CUtensorMap* map, const void* ptr_, int rows, int cols, int box_rows) {
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) return set_error(AG_ERR_CUDA, "cuTensorMapEncodeTiled is unavailable");
+    cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)cols * 2};
+    cuuint32_t box[2] = {(cuuint32_t)TC_BK, (cuuint32_t)box_rows};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(ptr_), dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return set_error(AG_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return AG_OK;
+}
+
+}  // namespace ag
+
+using namespace ag;
+
+static inline int cdiv(long a, long b) { return (int)((a + b - 1) / b); }
+static inline size_t al256(size_t b) { return (b + 255) / 256 * 256; }
+
+extern "C" int32_t ag_linear_kpad(int32_t p) { return p > 0 ? cdiv(p, TC_BK) * TC_BK : 0; }
+
+extern "C" int ag_linear_prepare(const double* A, int32_t m, int32_t p, uint16_t* a_split, void* stream) {
+    AG_REQUIRE(A && a_split && m > 0 && p > 0, "invalid arguments");
+    const int kp = ag_linear_kpad(p);
+    split_a_kernel<<<cdiv((long)m * kp, 256), 256, 0, as_stream(stream)>>>(A, m, p, kp,
+                                                                         reinterpret_cast<__nv_bfloat16*>(a_split));
+    return launch_status("split_a_kernel");
+}
+
+extern "C" size_t ag_linear_workspace_bytes(int32_t m, int32_t p, int32_t n) {
+    if (m <= 0 || p <= 0 || n <= 0) return 0;
+    const size_t kp = ag_linear_kpad(p);
+    return al256(p * sizeof(double)) + al256((size_t)m * sizeof(float)) +
+           al256((size_t)n * 3 * kp * 2) + al256((size_t)cdiv(m, TC_BN) * n * sizeof(double));
+}
+
+extern "C" int ag_linear_llk(const ag_linear_model* lm, const double* theta, int32_t n, double norm,
+                             double* llk, void* workspace, size_t workspace_bytes, uint32_t* flags,
+                             void* stream) {
+    AG_REQUIRE(lm && lm->a64 && lm->b64 && lm->a_split && theta && llk && n > 0, "invalid arguments");
+    const int m = lm->m_obs, p = lm->p;
+    AG_REQUIRE(m > 0 && p > 0, "invalid linear model sizes");
+    const size_t need = ag_linear_workspace_bytes(m, p, n);
+    AG_REQUIRE(workspace && workspace_bytes >= need && aligned(workspace, 256),
+               "ag_linear_llk needs %zu bytes of 256-byte aligned workspace", need);
+    AG_REQUIRE(aligned(lm->a_split, 16), "a_split must be 16-byte aligned");
+    cudaStream_t s = as_stream(stream);
+    const int kp = ag_linear_kpad(p);
+    char* ws = static_cast<char*>(workspace);
+    double* theta0 = reinterpret_cast<double*>(ws); ws += al256(p * sizeof(double));
+    float* rho0 = reinterpret_cast<float*>(ws); ws += al256((size_t)m * sizeof(float));
+    __nv_bfloat16* tsplit = reinterpret_cast<__nv_bfloat16*>(ws); ws += al256((size_t)n * 3 * kp * 2);
+    double* partial = reinterpret_cast<double*>(ws);
+    const int tiles = cdiv(m, TC_BN);
+    column_mean_kernel<<<cdiv(p, 128), 128, 0, s>>>(theta, n, p, theta0);
+    rho0_kernel<<<cdiv((long)m * 32, 256), 256, 0, s>>>(lm->a64, lm->b64, theta0, m, p, rho0);
+    split_theta_kernel<<<cdiv((long)n * kp, 256), 256, 0, s>>>(theta, theta0, n, p, kp, tsplit);
+    int rc = launch_status("linear prologue kernels");
+    if (rc) return rc;
+    CUtensorMap ma, mb;
+    rc = make_map(&ma, tsplit, n, 3 * kp, TC_BM);
+    if (rc) return rc;
+    rc = make_map(&mb, lm->a_split, m, 3 * kp, TC_BN);
+    if (rc) return rc;
+    static bool attr = false;
+    if (!attr) {
+        rc = cuda_status(cudaFuncSetAttribute(linear_misfit_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)TC_SMEM),
+                         "cudaFuncSetAttribute(linear_misfit_tc_kernel)");
+        if (rc) return rc;
+        attr = true;
+    }
+    dim3 grid(cdiv(n, TC_BM), tiles);
+    linear_misfit_tc_kernel<<<grid, 128, TC_SMEM, s>>>(ma, mb, n, m, 3 * kp / TC_BK, rho0, partial, flags);
+    rc = launch_status("linear_misfit_tc_kernel");
+    if (rc) return rc;
+    linear_reduce_kernel<<<cdiv(n, 256), 256, 0, s>>>(n, tiles, partial, norm, llk);
+    return launch_status("linear_reduce_kernel");
+}
+
+extern "C" int ag_linear_llk_fp64(const ag_linear_model* lm, const double* theta, int32_t n, double norm,
+                                  double* llk, void* stream) {
+    AG_REQUIRE(lm && lm->a64 && lm->b64 && theta && llk && n > 0, "invalid arguments");
+    linear_fp64_kernel<<<cdiv((long)n * 32, 256), 256, 0, as_stream(stream)>>>(lm->a64, lm->b64, theta, n,
+                                                                             lm->m_obs, lm->p, norm, llk);
+    return launch_status("linear_fp64_kernel");
+}

@@ -3,5 +3,6 @@ from .bayesian import Bayesian
 from .contiguous import Contiguous
 from .cdm import CDM
 from .mogi import Mogi
+from .linear import Linear
 
-__all__ = ["Bayesian", "Contiguous", "CDM", "Mogi"]
+__all__ = ["Bayesian", "Contiguous", "CDM", "Mogi", "Linear"]

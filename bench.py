@@ -199,8 +199,8 @@ def anneal(kind, X, Y, los, d, N, rank, args):
     from altar_gb300.simulations import RNG, Job
     sampler = None
     if kind == "da":
-        sampler = DelayedAcceptance(surrogate=Surrogate(seed=5), collect_until_beta=args.collect_beta,
-                                    max_samples=args.max_samples, rms_limit=args.rms_limit, epochs=args.epochs)
+        sampler = DelayedAcceptance(surrogate=Surrogate(seed=5, batch=1024), rms_limit=args.rms_limit,
+                                    epochs=args.epochs, start_beta=args.da_start_beta)
     model = CDM(cdm_psets(), observations=Observations(X, Y, los, d, SIGMA ** 2))
     app = Application(model, job=Job(chains=N, steps=5), rng=RNG(1234 + rank),
                       controller=Annealer(sampler=sampler))
@@ -223,8 +223,8 @@ def anneal(kind, X, Y, los, d, N, rank, args):
         res["modes"] = [r.get("mode") for r in reps]
         res["rms_sigma"] = [r.get("rms_sigma") for r in reps]
         res["screened"] = [r.get("screened") for r in reps]
-        res["train_losses"] = sampler.surrogate.losses
-        res["samples"] = sampler.surrogate.count
+        res["refits"] = sampler.refits
+        res["train_losses_last"] = sampler.surrogate.losses[-3:]
     return res
 
 
@@ -405,10 +405,9 @@ def main():
     ap.add_argument("--mode", default="walk", choices=["walk", "anneal", "compare"])
     ap.add_argument("--sampler", default="plain", choices=["plain", "da"])
     ap.add_argument("--max-stages", type=int, default=400)
-    ap.add_argument("--collect-beta", type=float, default=0.05)
-    ap.add_argument("--max-samples", type=int, default=2_000_000)
+    ap.add_argument("--da-start-beta", type=float, default=0.0)
     ap.add_argument("--rms-limit", type=float, default=0.5)
-    ap.add_argument("--epochs", type=int, default=8)
+    ap.add_argument("--epochs", type=int, default=40)
     ap.add_argument("--chains", type=int, default=32768)
     ap.add_argument("--cpu-chains", type=int, default=128)
     args = ap.parse_args()

@@ -243,6 +243,38 @@ int ag_posterior(const ag_stage_state* st, int32_t n, const double* prior, const
                  double* post, void* stream);
 
 /* ---------------------------------------------------------------------------
+ * Linear Gaussian model (models/linear/linear/Linear.py:152-185) with the data
+ * covariance folded in: A = L⁻¹ G, b = L⁻¹ d for Cd = L Lᵀ, so that
+ * llk = norm - 1/2 |A θ - b|² (the correct Gaussian form; the reference takes
+ * norm - |L r|/2, Linear.py:182).
+ */
+typedef struct ag_linear_model {
+    const double* a64;        /* [m_obs][p] FP64 A */
+    const double* b64;        /* [m_obs] FP64 b */
+    const uint16_t* a_split;  /* [m_obs][3 kpad] BF16 [A_hi | A_hi | A_lo] from ag_linear_prepare */
+    int32_t m_obs;
+    int32_t p;
+} ag_linear_model;
+
+/* p rounded up to the tensor-core K tile (64) */
+int32_t ag_linear_kpad(int32_t p);
+/* build the split BF16 operand of A (m x 3 kpad) */
+int ag_linear_prepare(const double* A, int32_t m, int32_t p, uint16_t* a_split, void* stream);
+/* workspace of ag_linear_llk for n chains */
+size_t ag_linear_workspace_bytes(int32_t m, int32_t p, int32_t n);
+/*
+ * llk[i] = norm - 1/2 |A θ_i - b|² with A(θ - θ₀) on the tcgen05 tensor cores (split BF16,
+ * FP32 accumulation) and ρ₀ = A θ₀ - b in FP64 (θ₀ = mean of the chains).  Replaces the
+ * dgemm + per-chain norm loop of Linear.dataLikelihood.  flags receives AG_DEV_ERR_TIMEOUT.
+ */
+int ag_linear_llk(const ag_linear_model* model, const double* theta, int32_t n, double norm,
+                  double* llk, void* workspace, size_t workspace_bytes, uint32_t* flags,
+                  void* stream);
+/* the same log-likelihood entirely in FP64 CUDA cores (reference path for checks) */
+int ag_linear_llk_fp64(const ag_linear_model* model, const double* theta, int32_t n, double norm,
+                       double* llk, void* stream);
+
+/* ---------------------------------------------------------------------------
  * Learned surrogate and delayed acceptance.  No counterpart in the reference:
  * an MLP maps normalised source parameters to PCA coefficients of the LOS
  * field; it screens proposals (stage 1) before the exact model (stage 2).

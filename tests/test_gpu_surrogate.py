@@ -85,11 +85,12 @@ def test_training_reduces_loss(cuda):
     sur = Surrogate((10, 64, 64, 8), seed=1, batch=1024).init_params()
     rng = np.random.default_rng(4)
     x = rng.uniform(-1, 1, (16384, 10)).astype(np.float32)
-    y = np.stack([np.sin(x @ rng.normal(size=10)) for _ in range(8)], 1).astype(np.float32)
+    W = rng.normal(size=(10, 8)) / 3
+    y = (x @ W + 0.3 * (x @ W) ** 2).astype(np.float32)      # smooth, like a local forward field
     sur.reserve(16384, 10)
     sur.add(dev(x, torch.float32), dev(y, torch.float32))
-    losses = sur.train(epochs=6, lr=3e-3)
-    assert losses[-1] < 0.3 * losses[0], losses
+    losses = sur.train(epochs=10, lr=3e-3)
+    assert losses[-1] < 0.1 * losses[0], losses
 
 
 def test_surrogate_llk_formula(cuda):
@@ -201,9 +202,8 @@ def test_delayed_acceptance_posterior(cuda):
         return app.controller.worker
 
     plain = run(None, 7)
-    sur = Surrogate((4, 128, 128, 32), seed=2, batch=2048, lr=2e-3)
-    da = DelayedAcceptance(surrogate=sur, collect_until_beta=1e-3, max_samples=200_000, rms_limit=50.0,
-                           epochs=6)
+    sur = Surrogate((4, 128, 128, 32), seed=2, batch=512, lr=2e-3)
+    da = DelayedAcceptance(surrogate=sur, rms_limit=50.0, fit_chains=1024, check_chains=128, epochs=20)
     dw = run(da, 7)
     assert sur.trained and any(r.get("mode") == "da" for r in dw.reports)
     tp, td = plain.step.theta.cpu().numpy(), dw.step.theta.cpu().numpy()
