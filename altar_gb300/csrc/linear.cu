@@ -34,7 +34,7 @@ constexpr uint32_t TC_A_BYTES = TC_BM * TC_BK * 2;   // 16 KB
 constexpr uint32_t TC_B_BYTES = TC_BN * TC_BK * 2;   // 32 KB
 constexpr uint32_t TC_STAGE_BYTES = TC_A_BYTES + TC_B_BYTES;
 constexpr uint32_t TC_SMEM = TC_STAGES * TC_STAGE_BYTES + 1024 /*align*/ + 1024 /*ρ₀*/ + 256 /*bars*/;
-constexpr uint32_t TC_WAIT = 1u << 26;
+constexpr uint32_t TC_WAIT = 1u << 22;
 
 // shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 B apart
 AG_DEVICE_INLINE uint64_t sw128_desc(uint32_t saddr) {
@@ -163,11 +163,13 @@ linear_misfit_tc_kernel(const __grid_constant__ CUtensorMap map_a,   // chains  
     }
     __syncwarp();
     // epilogue: thread = chain row (TMEM lane), sums over the tile's observations
-    const bool ok = mbar_wait_bounded(done, 0, TC_WAIT);
+    const bool waited = mbar_wait_bounded(done, 0, TC_WAIT);
+    // tcgen05.ld is warp-collective: decide for the whole CTA
+    const int ok = __syncthreads_and(waited && !*(volatile int*)&s_abort);
     tc_fence_after();
     const int chain = m0 + warp * 32 + lane;
     double acc = 0.0;
-    if (ok && !s_abort) {
+    if (ok) {
         const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
 #pragma unroll 1
         for (int c0 = 0; c0 < TC_BN; c0 += 32) {
