@@ -95,7 +95,7 @@ class Layout(ctypes.Structure):
     _fields_ = [("nparams", c_int32), ("x_idx", c_int32), ("depth_idx", c_int32),
                 ("strength_idx", c_int32), ("axes_idx", c_int32), ("omega_idx", c_int32),
                 ("offset_idx", c_int32), ("log_strength", c_int32), ("nsources", c_int32),
-                ("source_stride", c_int32), ("nu", c_double)]
+                ("source_stride", c_int32), ("variant", c_int32), ("reserved", c_int32), ("nu", c_double)]
 
 
 class LinearModel(ctypes.Structure):
@@ -117,6 +117,7 @@ _SIGNATURES = {
     "ag_last_error": (c_int, [c_char_p, c_size_t]),
     "ag_version": (c_char_p, []),
     "ag_forward_workspace_bytes": (c_size_t, [c_int, c_int32]),
+    "ag_forward_variants": (c_int32, [c_int]),
     "ag_forward_llk": (c_int, [c_int, P, P, c_int32, P, c_double, P, P, P, P, P, c_size_t, P]),
     "ag_cdm_check": (c_int, [P, P, c_int32, P, P]),
     "ag_forward_llk_subset": (c_int, [c_int, P, P, c_int32, P, c_double, P, P, P, P, P, P, c_size_t, P]),
@@ -136,6 +137,7 @@ _SIGNATURES = {
     "ag_to_bf16": (c_int, [ctypes.c_int64, P, P, P]),
     "ag_surrogate_llk": (c_int, [c_int32, c_int32, P, P, P, P, c_double, c_double, P, P]),
     "ag_da_screen": (c_int, [P, c_int32, c_uint64, c_uint32, P, P, P, P, P, P, P, P, P]),
+    "ag_da_moved": (c_int, [c_int32, c_int32, P, P, P, P, P, P]),
     "ag_da_accept": (c_int, [P, c_int32, c_int32, c_uint64, c_uint32, P, P, P, P, P, P, P, P, P, P, P,
                              P, P]),
     "ag_prior_sample": (c_int, [c_int32, c_int32, P, P, c_uint64, c_uint32, P, P, P]),

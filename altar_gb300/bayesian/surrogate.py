@@ -89,7 +89,10 @@ class Surrogate:
         idx = torch.argsort(evals, descending=True)[:k]
         lam = evals[idx].clamp_min(1e-30)
         B = (Bt.T @ evecs[:, idx]) / torch.sqrt(lam)              # orthonormal columns (Mp, k)
-        scale = torch.sqrt(lam / F.shape[0]).clamp_min(1e-12)     # std of each coefficient
+        # one common scale (the leading component's spread): the training loss in
+        # normalised coefficients is then proportional to the field-space error, so
+        # noise-level components cannot dominate it
+        scale = torch.full_like(lam, float(torch.sqrt(lam[0] / F.shape[0]).clamp_min(1e-12)))
         if k < self.k:                                             # pad unused components
             B = torch.cat([B, torch.zeros(B.shape[0], self.k - k, dtype=B.dtype, device=DEVICE)], 1)
             scale = torch.cat([scale, torch.ones(self.k - k, dtype=scale.dtype, device=DEVICE)])
@@ -196,8 +199,14 @@ class DelayedAcceptance(Metropolis):
     """Metropolis with a surrogate screen (stage 1) before the exact model (stage 2)."""
 
     def __init__(self, surrogate=None, rms_limit=0.5, fit_chains=4096, check_chains=256, epochs=40,
-                 start_beta=0.0, retry_every=3, spread=3.0, **kwds):
+                 start_beta=0.0, retry_every=3, spread=3.0, inner=1, outer=None, **kwds):
+        """inner: surrogate Metropolis moves per exact correction (1 = two-stage delayed
+        acceptance; k > 1 = surrogate-transition proposals, Liu 2001, corrected by the same
+        exact second stage); outer: exact corrections per stage in the surrogate mode
+        (default: the job's steps)."""
         super().__init__(**kwds)
+        self.inner = int(inner)
+        self.outer = None if outer is None else int(outer)
         self.surrogate = surrogate if surrogate is not None else Surrogate(batch=1024)
         self.rms_limit = float(rms_limit)
         self.fit_chains, self.check_chains = int(fit_chains), int(check_chains)
@@ -211,6 +220,7 @@ class DelayedAcceptance(Metropolis):
         self._last_try = -10 ** 9
         self._bounds = None
         self._sbufs = None
+        self._chain = None
 
     def mode_key(self):
         return self.mode
@@ -303,8 +313,62 @@ class DelayedAcceptance(Metropolis):
     # ---- walks
     def walkChains(self, annealer, step):
         if self.mode == "da":
+            if self.inner > 1:
+                return self._walk_transition(annealer, step)
             return self._walk_da(annealer, step)
         return super().walkChains(annealer, step)
+
+    def _walk_transition(self, annealer, step):
+        """k surrogate Metropolis moves, then one exact correction of where they ended."""
+        model = annealer.model
+        strat = model.strategy
+        sur = self.surrogate
+        n, p = step.samples, step.parameters
+        cand, cprior, cdata, mask = self._buffers(n, p)
+        if self._sbufs is None or self._sbufs[1].shape[0] != n:
+            self._sbufs = (sur.buffers(n, p), torch.empty(n, dtype=torch.float64, device=DEVICE),
+                           torch.empty(n, dtype=torch.float64, device=DEVICE),
+                           torch.empty(n, dtype=torch.int32, device=DEVICE),
+                           torch.empty(n, dtype=torch.int32, device=DEVICE),
+                           torch.zeros(1, dtype=torch.int32, device=DEVICE),
+                           torch.zeros(1, dtype=torch.int64, device=DEVICE))
+        if self._chain is None or self._chain[0].shape != (n, p):
+            f64 = dict(dtype=torch.float64, device=DEVICE)
+            st = step.state
+            counters = torch.zeros(3, dtype=torch.int64, device=DEVICE)
+            sst = _native.StageState(*(t.data_ptr() for t in (st.beta, st.dbeta_cov, st.scaling, st.sigma,
+                                                             st.chol, st.w, counters, st.epoch, st.flags)))
+            self._chain = (torch.zeros(n, p, **f64), torch.zeros(n, **f64), torch.zeros(n, **f64),
+                           torch.zeros(n, **f64), torch.zeros(n, dtype=torch.int32, device=DEVICE), sst, counters)
+        bufs, sur_cur, sur_cand, passed, index, count, screened = self._sbufs
+        th_s, pr_s, su_s, po_s, mask2, sst, _ = self._chain
+        self.screened = screened
+        lo, hi = self._bounds
+        st = step.state.struct
+        s = stream_handle()
+        sur.predict(step.theta, lo, hi, sur_cur, bufs)
+        outer = self.outer if self.outer is not None else self.steps
+        for o in range(outer):
+            th_s.copy_(step.theta)
+            pr_s.copy_(step.prior)
+            su_s.copy_(sur_cur)
+            _native.call("ag_posterior", st, n, ptr(pr_s), ptr(su_s), ptr(po_s), s)
+            for j in range(self.inner):
+                sid = 1000 + o * self.inner + j
+                _native.call("ag_propose", st, ptr(th_s), n, p, ptr(model.lo), ptr(model.hi), self.seed, sid,
+                             ptr(cand), ptr(mask), ptr(cprior), s)
+                sur.predict(cand, lo, hi, sur_cand, bufs)
+                _native.call("ag_accept", ctypes.byref(sst), n, p, self.seed, sid, ptr(mask), ptr(cand),
+                             ptr(cprior), ptr(sur_cand), ptr(th_s), ptr(pr_s), ptr(su_s), ptr(po_s), s)
+            _native.call("ag_da_moved", n, p, ptr(step.theta), ptr(th_s), ptr(passed), ptr(index), ptr(count), s)
+            mask2.zero_()
+            _native.call("ag_forward_llk_subset", strat.kind, ctypes.byref(strat.layout), ptr(th_s), n,
+                         strat.stations.struct, strat.norm, ptr(index), ptr(count), ptr(cdata), ptr(mask2), None,
+                         ptr(strat._ws), strat._ws_bytes, s)
+            _native.call("ag_da_accept", st, n, p, self.seed, o, ptr(mask2), ptr(passed), ptr(th_s), ptr(pr_s),
+                         ptr(cdata), ptr(su_s), ptr(step.theta), ptr(step.prior), ptr(step.data),
+                         ptr(step.posterior), ptr(sur_cur), ptr(screened), s)
+        return step.state.counters
 
     def _walk_da(self, annealer, step):
         model = annealer.model

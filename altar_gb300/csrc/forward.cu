@@ -367,8 +367,8 @@ AG_DEVICE_INLINE void side_pair(const SideC& S, float Xr, float Yr, float& ue, f
 }
 
 // ---------------------------------------------------------------------------
-template <int WARPS>
-__global__ void __launch_bounds__(WARPS * 32, 2)
+template <int WARPS, int MINB>
+__global__ void __launch_bounds__(WARPS * 32, MINB)
 cdm_llk_kernel(const ChainC* __restrict__ chains, int n, const float4* __restrict__ xy,
                const float4* __restrict__ losd, const float* __restrict__ wt,
                const int32_t* __restrict__ oid, int m_padded, double norm,
@@ -571,8 +571,14 @@ mogi_llk_kernel(ag_layout L, const double* __restrict__ theta, int n,
 // C ABI
 using namespace ag;
 
-static constexpr int kCdmWarps = 8;
+// CDM launch variants: warps (= chains) per CTA and resident CTAs per SM the
+// register allocation targets; chosen per problem by the autotuner
+struct CdmVariant { int warps; };
+static constexpr CdmVariant kCdmVariants[] = {{8}, {4}, {4}, {16}};
+static constexpr int kCdmVariantCount = 4;
 static constexpr int kMogiChains = 16;
+
+extern "C" int32_t ag_forward_variants(int model) { return model == AG_MODEL_CDM ? kCdmVariantCount : 1; }
 
 extern "C" size_t ag_forward_workspace_bytes(int model, int32_t n) {
     if (model == AG_MODEL_CDM && n > 0) return (size_t)n * sizeof(ChainC);
@@ -626,10 +632,30 @@ static int forward_llk(int model, const ag_layout* layout, const double* theta, 
                                                          noffsets, index, count);
         rc = launch_status("cdm_setup_kernel");
         if (rc) return rc;
-        const int grid = (n + kCdmWarps - 1) / kCdmWarps;
-        cdm_llk_kernel<kCdmWarps><<<grid, kCdmWarps * 32, 0, s>>>(
-            chains, n, xy, ld, st->weight, st->oid, st->m_padded, norm, llk, residuals, nullptr, index,
-            count);
+        const int v = L.variant;
+        AG_REQUIRE(v >= 0 && v < kCdmVariantCount, "CDM variant %d out of range [0, %d)", v, kCdmVariantCount);
+        const int warps = kCdmVariants[v].warps;
+        const int grid = (n + warps - 1) / warps;
+        const float4* ld_ = ld;
+        switch (v) {
+            case 0:
+                cdm_llk_kernel<8, 2><<<grid, 8 * 32, 0, s>>>(chains, n, xy, ld_, st->weight, st->oid, st->m_padded,
+                                                             norm, llk, residuals, nullptr, index, count);
+                break;
+            case 1:
+                cdm_llk_kernel<4, 4><<<grid, 4 * 32, 0, s>>>(chains, n, xy, ld_, st->weight, st->oid, st->m_padded,
+                                                             norm, llk, residuals, nullptr, index, count);
+                break;
+            case 2:
+                cdm_llk_kernel<4, 5><<<grid, 4 * 32, 0, s>>>(chains, n, xy, ld_, st->weight, st->oid, st->m_padded,
+                                                             norm, llk, residuals, nullptr, index, count);
+                break;
+            default:
+                cdm_llk_kernel<16, 1><<<grid, 16 * 32, 0, s>>>(chains, n, xy, ld_, st->weight, st->oid,
+                                                               st->m_padded, norm, llk, residuals, nullptr, index,
+                                                               count);
+                break;
+        }
         return launch_status("cdm_llk_kernel");
     }
     if (model == AG_MODEL_MOGI) {

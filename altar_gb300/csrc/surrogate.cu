@@ -248,6 +248,19 @@ __global__ void da_accept_kernel(int n, int p, const double* __restrict__ beta, 
     if (threadIdx.x == 3 && s_cnt[3] && screened) atomicAdd(screened, (unsigned long long)s_cnt[3]);
 }
 
+// chains whose surrogate-chain state moved away from the exact state go to the exact
+// correction: pass[i] = (θ_s ≠ θ) and no support violation, compacted into index
+__global__ void da_moved_kernel(int n, int p, const double* __restrict__ theta,
+                                const double* __restrict__ theta_s, int32_t* __restrict__ pass,
+                                int32_t* __restrict__ index, int32_t* __restrict__ count) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int moved = 0;
+    for (int j = 0; j < p; ++j) moved |= (theta[(size_t)i * p + j] != theta_s[(size_t)i * p + j]);
+    pass[i] = moved;
+    if (moved) index[atomicAdd(count, 1)] = i;
+}
+
 }  // namespace ag
 
 // ---------------------------------------------------------------------------
@@ -255,6 +268,16 @@ __global__ void da_accept_kernel(int n, int p, const double* __restrict__ beta, 
 using namespace ag;
 
 static inline int nblk(long n, int t) { return (int)((n + t - 1) / t); }
+
+extern "C" int ag_da_moved(int32_t n, int32_t p, const double* theta, const double* theta_s, int32_t* pass,
+                           int32_t* index, int32_t* count, void* stream) {
+    AG_REQUIRE(n > 0 && p > 0 && theta && theta_s && pass && index && count, "invalid arguments");
+    cudaStream_t s = as_stream(stream);
+    int rc = cuda_status(cudaMemsetAsync(count, 0, sizeof(int32_t), s), "memset count");
+    if (rc) return rc;
+    da_moved_kernel<<<nblk(n, 256), 256, 0, s>>>(n, p, theta, theta_s, pass, index, count);
+    return launch_status("da_moved_kernel");
+}
 
 static int check_net(const ag_mlp* net) {
     AG_REQUIRE(net && net->nlayers >= 1 && net->nlayers <= kMaxLayers, "invalid network");

@@ -19,9 +19,12 @@ from .observations import Observations
 
 
 class CDM(Bayesian):
-    def __init__(self, psets, observations=None, case=None, nu=0.25, **kwds):
+    def __init__(self, psets, observations=None, case=None, nu=0.25, variant=0, autotune=False, **kwds):
         super().__init__(psets=psets, **kwds)
         self.nu = float(nu)
+        self.variant = int(variant)
+        self.autotune = bool(autotune)
+        self.tuning = None
         self.obs = observations if observations is not None else (
             Observations.read(case) if case is not None else None)
         self.strategy = None
@@ -43,7 +46,7 @@ class CDM(Bayesian):
         off = p["offsets"].offset if "offsets" in p else -1
         return _native.Layout(self.parameters, p["location"].offset, p["depth"].offset,
                               p["opening"].offset, p["a"].offset, p["omega"].offset, off, 0, 1, 0,
-                              self.nu)
+                              variant=self.variant, nu=self.nu)
 
     def initializeSample(self, step, max_attempts=1000):
         super().initializeSample(step)
@@ -54,6 +57,10 @@ class CDM(Bayesian):
             _native.call("ag_cdm_check", ctypes.byref(lay), ptr(step.theta), step.samples,
                          ptr(status), stream_handle())
             if int(torch.count_nonzero(status)) == 0:
+                if self.autotune:
+                    from ..autotune import tune
+                    self.tuning = tune(self.strategy, step.theta)
+                    self.variant = self.tuning["variant"]
                 return self
             super().initializeSample(step, attempt=attempt, redraw=status)
         raise RuntimeError("could not draw an initial sample with every CDM below the surface")

@@ -40,8 +40,7 @@ class Mogi(Bayesian):
         off = p["offsets"].offset if "offsets" in p else -1
         if self.sources == 1:
             return _native.Layout(self.parameters, p["location"].offset, p["depth"].offset,
-                                  p["source"].offset, -1, -1, off, int(self.log_strength), 1, 0,
-                                  self.nu)
+                                  p["source"].offset, -1, -1, off, int(self.log_strength), 1, 0, nu=self.nu)
         raise NotImplementedError("multi-source layouts are built with Mogi.layout_multi")
 
     def dataLikelihood(self, step):

@@ -200,8 +200,9 @@ def anneal(kind, X, Y, los, d, N, rank, args):
     sampler = None
     if kind == "da":
         sampler = DelayedAcceptance(surrogate=Surrogate(seed=5, batch=1024), rms_limit=args.rms_limit,
-                                    epochs=args.epochs, start_beta=args.da_start_beta)
-    model = CDM(cdm_psets(), observations=Observations(X, Y, los, d, SIGMA ** 2))
+                                    epochs=args.epochs, start_beta=args.da_start_beta, inner=args.da_inner,
+                                    outer=args.da_outer)
+    model = CDM(cdm_psets(), observations=Observations(X, Y, los, d, SIGMA ** 2), autotune=not args.no_autotune)
     app = Application(model, job=Job(chains=N, steps=5), rng=RNG(1234 + rank),
                       controller=Annealer(sampler=sampler))
     app.initialize()
@@ -251,6 +252,10 @@ def run_ours(args):
         out = {}
         for kind in runs:
             out[kind] = anneal(kind, X, Y, los, d, N, rank, args)
+        for extra in args.da_variants:
+            inner, outer = (int(v) for v in extra.split("x"))
+            args.da_inner, args.da_outer = inner, outer
+            out[f"da_{inner}x{outer}"] = anneal("da", X, Y, los, d, N, rank, args)
         line = {"metric": "CDM time-to-beta=1", "unit": "s", "n_gpus": world, "higher_is_better": False,
                 "config": {"workload": "cdm-40k-obs", "chains": N, "stations": X.size, "steps_per_stage": 5,
                            "truth": truth.tolist()},
@@ -268,7 +273,7 @@ def run_ours(args):
             print(json.dumps(line))
         return 0
 
-    model = CDM(psets, observations=Observations(X, Y, los, d, SIGMA ** 2))
+    model = CDM(psets, observations=Observations(X, Y, los, d, SIGMA ** 2), autotune=not args.no_autotune)
     app = Application(model, job=Job(chains=N, steps=5), rng=RNG(1234 + rank))
     app.initialize()
     ann = app.controller
@@ -374,6 +379,7 @@ def run_ours(args):
                    "step": "one annealing stage: COV beta + Sigma + resample, 5 Metropolis steps, scaling",
                    "l2": "flushed (256 MB write) between timed iterations",
                    "graphs": "one CUDA graph per phase (cool, walk, resample)",
+                   "cdm_variant": model.variant, "autotune": model.tuning,
                    "beta_range": [reps[0]["beta"], reps[-1]["beta"]] if reps else None},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved / fp32_peak, "traffic": profile_traffic,
@@ -406,6 +412,10 @@ def main():
     ap.add_argument("--sampler", default="plain", choices=["plain", "da"])
     ap.add_argument("--max-stages", type=int, default=400)
     ap.add_argument("--da-start-beta", type=float, default=0.0)
+    ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--da-inner", type=int, default=1)
+    ap.add_argument("--da-outer", type=int, default=None)
+    ap.add_argument("--da-variants", nargs="*", default=[], help="extra DA runs as INNERxOUTER, e.g. 5x2")
     ap.add_argument("--rms-limit", type=float, default=0.5)
     ap.add_argument("--epochs", type=int, default=40)
     ap.add_argument("--chains", type=int, default=32768)

@@ -80,8 +80,13 @@ typedef struct ag_layout {
     int32_t log_strength;   /* Mogi: 1 = θ holds log10(ΔV) as in the reference, 0 = ΔV */
     int32_t nsources;       /* Mogi: number of point sources (>= 1) */
     int32_t source_stride;  /* Mogi: parameter distance between consecutive sources */
+    int32_t variant;        /* CDM kernel launch variant (0 = default; see ag_forward_variants) */
+    int32_t reserved;
     double nu;              /* Poisson ratio */
 } ag_layout;
+
+/* number of launch variants of a forward model (autotuning candidates) */
+int32_t ag_forward_variants(int model);
 
 /* Last error message of the calling thread (NUL-terminated, truncated to len). */
 int ag_last_error(char* buf, size_t len);
@@ -323,6 +328,12 @@ int ag_da_accept(const ag_stage_state* st, int32_t n, int32_t p, uint64_t seed, 
                  const uint32_t* mask, const int32_t* pass, const double* cand, const double* cprior,
                  const double* cdata, const double* csur, double* theta, double* prior, double* data,
                  double* post, double* sur, unsigned long long* screened, void* stream);
+
+/* surrogate-transition variant: pass[i] = 1 where the surrogate chain θ_s moved away from θ;
+ * those chains are listed in index[0 .. *count) for the exact correction (ag_da_accept with
+ * θ_s as the candidate) */
+int ag_da_moved(int32_t n, int32_t p, const double* theta, const double* theta_s, int32_t* pass,
+                int32_t* index, int32_t* count, void* stream);
 
 /* CUDA graph capture of a sequence of calls on one stream. */
 int ag_graph_begin(void* stream);

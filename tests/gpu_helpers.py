@@ -51,16 +51,16 @@ class Shim:
         return self._layout
 
 
-def cdm_strategy(X, Y, los, d, var, oid=None, offset_idx=-1, nparams=10):
+def cdm_strategy(X, Y, los, d, var, oid=None, offset_idx=-1, nparams=10, variant=0):
     obs = Observations(X, Y, los, d, var, oid)
-    lay = _native.Layout(nparams, 0, 2, 3, 4, 7, offset_idx, 0, 1, 0, 0.25)
+    lay = _native.Layout(nparams, 0, 2, 3, 4, 7, offset_idx, 0, 1, 0, variant=variant, nu=0.25)
     return CUDA(_native.AG_MODEL_CDM).initialize(None, Shim(obs, lay)), obs
 
 
 def mogi_strategy(X, Y, los, d, var, log_strength=False, oid=None, offset_idx=-1, nparams=4,
                   nsources=1, stride=0):
     obs = Observations(X, Y, los, d, var, oid)
-    lay = _native.Layout(nparams, 0, 2, 3, -1, -1, offset_idx, int(log_strength), nsources, stride, 0.25)
+    lay = _native.Layout(nparams, 0, 2, 3, -1, -1, offset_idx, int(log_strength), nsources, stride, nu=0.25)
     return CUDA(_native.AG_MODEL_MOGI).initialize(None, Shim(obs, lay)), obs
 
 

@@ -211,3 +211,33 @@ def test_delayed_acceptance_posterior(cuda):
         sd = tp[:, j].std()
         assert abs(td[:, j].mean() - tp[:, j].mean()) < 4 * sd / np.sqrt(2048 / 8), j
         assert abs(td[:, j].std() - sd) < 0.5 * sd, j
+
+
+def test_surrogate_transition_posterior(cuda):
+    """k surrogate moves per exact correction still target the exact posterior."""
+    g = np.linspace(-15e3, 15e3, 32)
+    X, Y = [a.ravel() for a in np.meshgrid(g, g)]
+    los = np.tile(LOS, (X.size, 1))
+    rng = np.random.default_rng(0)
+    d = catmip.mogi_los(np.array([[0.0, 0.0, 3e3, 2e6]]), X, Y, los, 0.25, log_strength=False)[0]
+    d = d + rng.normal(0, 5e-3, X.size)
+
+    def run(sampler):
+        psets = {"location": Contiguous(2, Uniform((-1e4, 1e4))), "depth": Contiguous(1, Uniform((1e3, 8e3))),
+                 "source": Contiguous(1, Uniform((1e5, 1e7)))}
+        model = Mogi(psets, observations=Observations(X, Y, los, d, 2.5e-5), log_strength=False)
+        app = Application(model, job=Job(chains=2048, steps=5), rng=RNG(9), controller=Annealer(sampler=sampler))
+        app.run()
+        return app.controller.worker
+
+    plain = run(None)
+    sur = Surrogate((4, 128, 128, 32), seed=2, batch=512, lr=2e-3)
+    da = DelayedAcceptance(surrogate=sur, rms_limit=50.0, fit_chains=1024, check_chains=128, epochs=20,
+                           inner=3, outer=2)
+    dw = run(da)
+    assert any(r.get("mode") == "da" for r in dw.reports)
+    tp, td = plain.step.theta.cpu().numpy(), dw.step.theta.cpu().numpy()
+    for j in range(4):
+        sd = tp[:, j].std()
+        assert abs(td[:, j].mean() - tp[:, j].mean()) < 4 * sd / np.sqrt(2048 / 8), j
+        assert abs(td[:, j].std() - sd) < 0.5 * sd, j
