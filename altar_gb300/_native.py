@@ -146,6 +146,8 @@ _SIGNATURES = {
     "ag_accept": (c_int, [P, c_int32, c_int32, c_uint64, c_uint32, P, P, P, P, P, P, P, P, P]),
     "ag_cov_workspace_bytes": (c_size_t, [c_int32]),
     "ag_cov_schedule": (c_int, [P, P, c_int32, c_double, c_double, P, c_size_t, P]),
+    "ag_cov_schedule_noalloc": (c_int, [P, P, c_int32, c_double, c_double, P]),
+    "ag_cov_schedule_noalloc_max_chains": (c_int32, []),
     "ag_sigma_workspace_bytes": (c_size_t, [c_int32, c_int32]),
     "ag_weighted_cov": (c_int, [P, P, c_int32, c_int32, P, c_size_t, P]),
     "ag_cholesky_scaled": (c_int, [P, c_int32, P]),

@@ -11,6 +11,7 @@
 
 #include "common.cuh"
 #include "internal.h"
+#include <mutex>
 
 namespace ag {
 
@@ -831,4 +832,91 @@ extern "C" int ag_adapt_scaling(const ag_stage_state* st, double aw, double rw, 
     if (rc) return rc;
     adapt_kernel<<<1, 32, 0, as_stream(stream)>>>(aw, rw, st->counters, st->scaling, st->epoch);
     return launch_status("adapt_kernel");
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free COV β schedule.
+//
+// Some callers cannot call cudaMalloc when they run a stage: hosts whose
+// device memory is entirely reserved up front by another allocator or by a
+// fixed memory budget, embedders that must not change their device footprint
+// after start-up, and loops that must not enter the allocator at all because
+// cudaMalloc and cudaFree may synchronise the device.  This entry point
+// needs no caller workspace: its scratch (the schedule state and the
+// per-block partial moments) lives in a file-scope device array of fixed
+// size, reserved when the library is loaded on a device and held by every
+// device that loads the library until the process exits.
+//
+// * Limit: n <= kNoAllocMaxChains chains; larger n is rejected.
+// * All calls share the one array, and it keeps the last call's contents:
+//   calls whose work overlaps on the GPU (different streams, or a call made
+//   before the previous one finished on another stream) race on it; issue
+//   them in order on one stream.
+// * The first call on each device looks up the array's device address
+//   (cudaGetSymbolAddress) with that device current; make that first call
+//   before any stream capture.
+namespace {
+
+constexpr int32_t kNoAllocMaxChains = 1 << 18;
+constexpr size_t kNoAllocState = (sizeof(CovState) + 255) / 256 * 256;
+constexpr size_t kNoAllocBytes =
+    kNoAllocState + (size_t)((kNoAllocMaxChains + kEvalChunk - 1) / kEvalChunk) * kGridPoints * 2 * sizeof(double);
+constexpr int kNoAllocMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_cov_scratch[kNoAllocBytes];
+
+std::mutex g_scratch_mutex;
+void* g_scratch_addr[kNoAllocMaxDevices] = {};
+
+int scratch_address(void** out) {
+    int dev = 0;
+    int rc = cuda_status(cudaGetDevice(&dev), "cudaGetDevice");
+    if (rc) return rc;
+    if (dev < 0 || dev >= kNoAllocMaxDevices)
+        return set_error(AG_ERR_SIZE, "device %d is beyond the %d devices this entry point tracks", dev,
+                         kNoAllocMaxDevices);
+    std::lock_guard<std::mutex> lock(g_scratch_mutex);
+    if (!g_scratch_addr[dev]) {
+        void* p = nullptr;
+        rc = cuda_status(cudaGetSymbolAddress(&p, g_cov_scratch), "cudaGetSymbolAddress(g_cov_scratch)");
+        if (rc) return rc;
+        g_scratch_addr[dev] = p;
+    }
+    *out = g_scratch_addr[dev];
+    return AG_OK;
+}
+
+}  // namespace
+
+extern "C" int32_t ag_cov_schedule_noalloc_max_chains(void) { return kNoAllocMaxChains; }
+
+extern "C" int ag_cov_schedule_noalloc(const ag_stage_state* st, const double* data_llk, int32_t n,
+                                       double target, double tol, void* stream) {
+    int rc = check_state(st);
+    if (rc) return rc;
+    AG_REQUIRE(data_llk != nullptr, "data_llk is NULL");
+    if (n < 2 || n > kNoAllocMaxChains)
+        return set_error(AG_ERR_SIZE,
+                         "ag_cov_schedule_noalloc supports 2 to %d chains (got %d); use ag_cov_schedule "
+                         "with a caller workspace for more",
+                         kNoAllocMaxChains, n);
+    void* scratch = nullptr;
+    rc = scratch_address(&scratch);
+    if (rc) return rc;
+    cudaStream_t s = as_stream(stream);
+    // the state block starts from zero on every call; the partials are written before they are read
+    rc = cuda_status(cudaMemsetAsync(scratch, 0, kNoAllocState, s), "cudaMemsetAsync(scratch state)");
+    if (rc) return rc;
+    CovState* S = reinterpret_cast<CovState*>(scratch);
+    double* part = reinterpret_cast<double*>(static_cast<char*>(scratch) + kNoAllocState);
+    const int nblk = blocks(n, kEvalChunk);
+    cov_median_kernel<<<1, 1024, 0, s>>>(data_llk, n, st->beta, S);
+    for (int round = 0; round <= kGridLevels; ++round) {
+        cov_eval_kernel<<<dim3(nblk, kGridPoints), 256, 0, s>>>(data_llk, n, S, part);
+        cov_decide_kernel<<<1, 32, 0, s>>>(n, nblk, target, tol, part, S);
+    }
+    cov_final_sum_kernel<<<nblk, 256, 0, s>>>(data_llk, n, S, part);
+    cov_final_state_kernel<<<1, 32, 0, s>>>(n, nblk, part, S, st->beta, st->dbeta_cov);
+    cov_weights_kernel<<<blocks(n, 256), 256, 0, s>>>(data_llk, n, S, st->w);
+    return launch_status("cov schedule kernels (no-alloc)");
 }

@@ -203,6 +203,24 @@ int ag_cov_schedule(const ag_stage_state* st, const double* data_llk, int32_t n,
                     double target, double tol, void* workspace, size_t workspace_bytes,
                     void* stream);
 
+/*
+ * Allocation-free variant of ag_cov_schedule (no counterpart in the reference).
+ * For callers that cannot allocate device memory when they drive the schedule
+ * (a fixed pre-reserved device budget, a device footprint that must not change
+ * after start-up, or a loop that must not enter the allocator because cudaMalloc
+ * and cudaFree may synchronise the device).  Same inputs and
+ * results as ag_cov_schedule without the workspace: the scratch is a fixed
+ * device array inside the library (about 45 KB, held by every device that
+ * loads the library until exit).  Supports at most
+ * ag_cov_schedule_noalloc_max_chains() chains (262,144); more returns
+ * AG_ERR_SIZE.  All calls share that array: calls that overlap on the GPU
+ * race, so issue them in order on one stream.  The first call on a device
+ * looks up the array's address and should come before any stream capture.
+ */
+int ag_cov_schedule_noalloc(const ag_stage_state* st, const double* data_llk, int32_t n,
+                            double target, double tol, void* stream);
+int32_t ag_cov_schedule_noalloc_max_chains(void);
+
 /* Bytes of workspace ag_weighted_cov needs. */
 size_t ag_sigma_workspace_bytes(int32_t n, int32_t p);
 
