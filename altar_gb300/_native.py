@@ -102,6 +102,10 @@ class LinearModel(ctypes.Structure):
     _fields_ = [("a64", c_void_p), ("b64", c_void_p), ("a_split", c_void_p), ("m_obs", c_int32), ("p", c_int32)]
 
 
+class WhitenBlock(ctypes.Structure):
+    _fields_ = [("w64", c_void_p), ("w_split", c_void_p), ("col0", c_int32), ("m", c_int32)]
+
+
 class MLP(ctypes.Structure):
     _fields_ = [("nlayers", c_int32), ("sizes", c_int32 * 9)]
 
@@ -126,6 +130,8 @@ _SIGNATURES = {
     "ag_linear_workspace_bytes": (c_size_t, [c_int32, c_int32, c_int32]),
     "ag_linear_llk": (c_int, [P, P, c_int32, c_double, P, P, c_size_t, P, P]),
     "ag_linear_llk_fp64": (c_int, [P, P, c_int32, c_double, P, P]),
+    "ag_whiten_workspace_bytes": (c_size_t, [c_int32, c_int32]),
+    "ag_whiten_llk": (c_int, [P, P, c_int32, c_int32, P, P, c_size_t, P, P]),
     "ag_mlp_param_count": (ctypes.c_int64, [P]),
     "ag_mlp_activation_floats": (ctypes.c_int64, [P, c_int32]),
     "ag_normalize_inputs": (c_int, [P, c_int32, c_int32, P, P, P, P]),
@@ -146,6 +152,7 @@ _SIGNATURES = {
     "ag_accept": (c_int, [P, c_int32, c_int32, c_uint64, c_uint32, P, P, P, P, P, P, P, P, P]),
     "ag_cov_workspace_bytes": (c_size_t, [c_int32]),
     "ag_cov_schedule": (c_int, [P, P, c_int32, c_double, c_double, P, c_size_t, P]),
+    "ag_cov_schedule_brent": (c_int, [P, P, c_int32, c_double, c_double, c_int32, P, c_size_t, P]),
     "ag_cov_schedule_noalloc": (c_int, [P, P, c_int32, c_double, c_double, P]),
     "ag_cov_schedule_noalloc_max_chains": (c_int32, []),
     "ag_sigma_workspace_bytes": (c_size_t, [c_int32, c_int32]),

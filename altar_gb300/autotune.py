@@ -40,8 +40,8 @@ def _save(table):
         pass
 
 
-def key(kind, m, n):
-    return f"model={kind} m={m} n={n} gpu={torch.cuda.get_device_name()}"
+def key(kind, m, n, nvar):
+    return f"model={kind} m={m} n={n} variants={nvar} gpu={torch.cuda.get_device_name()}"
 
 
 def tune(strategy, theta, reps=3, sample=8192, use_cache=True):
@@ -50,7 +50,7 @@ def tune(strategy, theta, reps=3, sample=8192, use_cache=True):
     kind = strategy.kind
     nvar = lib.ag_forward_variants(kind)
     n_full = theta.shape[0]
-    k = key(kind, strategy.stations.m, n_full)
+    k = key(kind, strategy.stations.m, n_full, nvar)
     table = _load() if use_cache else {}
     if k in table:
         strategy.layout.variant = int(table[k]["variant"])

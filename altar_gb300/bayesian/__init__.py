@@ -3,10 +3,11 @@ from .coolingstep import CoolingStep, StageState
 from .notifier import Notifier, Profiler
 from .metropolis import Metropolis
 from .grid import Grid
+from .brent import Brent
 from .cov import COV
 from .annealing import CUDAAnnealing
 from .annealer import Annealer
 from .surrogate import DelayedAcceptance, Surrogate
 
-__all__ = ["CoolingStep", "StageState", "Notifier", "Profiler", "Metropolis", "Grid", "COV",
+__all__ = ["CoolingStep", "StageState", "Notifier", "Profiler", "Metropolis", "Grid", "Brent", "COV",
            "CUDAAnnealing", "Annealer", "DelayedAcceptance", "Surrogate"]

@@ -12,12 +12,17 @@ from .notifier import Notifier
 
 
 class Annealer:
-    def __init__(self, sampler=None, scheduler=None, dispatcher=None, archiver=None, graphs=True):
+    def __init__(self, sampler=None, scheduler=None, dispatcher=None, archiver=None, graphs=True,
+                 checkpoint=None, resume=None):
+        """checkpoint: a simulations.Checkpoint written after every ``every`` stages;
+        resume: path of a checkpoint to continue from instead of sampling the prior."""
         self.sampler = sampler if sampler is not None else Metropolis()
         self.scheduler = scheduler if scheduler is not None else COV()
         self.dispatcher = dispatcher if dispatcher is not None else Notifier()
         self.archiver = archiver
         self.graphs = graphs
+        self.checkpoint = checkpoint
+        self.resume = resume
         self.worker = None
         self.model = None
 

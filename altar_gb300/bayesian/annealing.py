@@ -40,6 +40,13 @@ class CUDAAnnealing:
 
     def start(self, annealer):
         self.iteration = 0
+        if annealer.resume is not None:
+            from ..simulations.checkpoint import Checkpoint
+            model = annealer.model
+            self.step = CoolingStep.alloc(samples=model.job.chains, parameters=model.parameters)
+            arrays = Checkpoint.load(annealer.resume, model.job.chains, model.parameters)
+            self.iteration = Checkpoint.restore(self.step, arrays)
+            return self                            # the checkpoint carries the proposal scaling
         self.step = CoolingStep.start(annealer)
         annealer.sampler.prime(self.step)
         return self
@@ -105,6 +112,9 @@ class CUDAAnnealing:
             log.warning("stage %d: scaled Σ not positive definite; diagonal proposal used", self.iteration)
         log.info("stage %(stage)d beta %(beta).6g cov %(cov).4g accepted %(accepted)d", rep)
         annealer.model.bottom(step=self.step)
+        ck = annealer.checkpoint
+        if ck is not None and ck.due(self.iteration):
+            ck.save(ck.path, self.step, self.iteration)
         return self
 
     def finish(self, annealer):

@@ -198,13 +198,22 @@ class Surrogate:
 class DelayedAcceptance(Metropolis):
     """Metropolis with a surrogate screen (stage 1) before the exact model (stage 2)."""
 
-    def __init__(self, surrogate=None, rms_limit=0.5, fit_chains=4096, check_chains=256, epochs=40,
-                 start_beta=0.0, retry_every=3, spread=3.0, inner=1, outer=None, **kwds):
-        """inner: surrogate Metropolis moves per exact correction (1 = two-stage delayed
+    def __init__(self, surrogate=None, rms_limit=0.5, delta_limit=1.0, fit_chains=4096, check_chains=256,
+                 epochs=40, start_beta=0.0, retry_every=3, spread=3.0, inner=1, outer=None, **kwds):
+        """rms_limit: largest RMS field error (data standard deviations) of a usable surrogate;
+        delta_limit: largest spread (standard deviation over trial proposals) of the error of
+        the surrogate's tempered log-posterior ratio, β[(s(y) - s(x)) - (l(y) - l(x))].  Delayed
+        acceptance stays exact whatever the surrogate, but its mixing needs the surrogate's
+        accept decisions to follow the exact ones: with 40,000 observations a field error far
+        below the noise can still move the log-likelihood ratio by tens of units near β = 1.
+        inner: surrogate Metropolis moves per exact correction (1 = two-stage delayed
         acceptance; k > 1 = surrogate-transition proposals, Liu 2001, corrected by the same
         exact second stage); outer: exact corrections per stage in the surrogate mode
         (default: the job's steps)."""
         super().__init__(**kwds)
+        self.delta_limit = float(delta_limit)
+        self.delta = None
+        self._backoff = 0
         self.inner = int(inner)
         self.outer = None if outer is None else int(outer)
         self.surrogate = surrogate if surrogate is not None else Surrogate(batch=1024)
@@ -226,7 +235,7 @@ class DelayedAcceptance(Metropolis):
         return self.mode
 
     def report(self):
-        rep = {"mode": self.mode, "rms_sigma": self.rms, "refits": self.refits}
+        rep = {"mode": self.mode, "rms_sigma": self.rms, "delta_sd": self.delta, "refits": self.refits}
         if self.mode == "da" and self.screened is not None:
             rep["screened"] = int(self.screened.item())
         return rep
@@ -249,17 +258,51 @@ class DelayedAcceptance(Metropolis):
         fit_rows, chk_rows = rows[:fit], rows[fit:fit + chk]
         if sur.trained:
             self.rms = self._check(annealer, step, chk_rows)
-            if self.rms <= self.rms_limit:
+            self.delta = self._delta_check(annealer, step, chk_rows)
+            if self._usable():
                 self.mode = "da"
                 return self
-            if self.rms > 4 * self.rms_limit and self._stage - self._last_try < self.retry_every:
+            # after a fit that failed its own check, wait before fitting again (doubling the wait)
+            if self._backoff and self._stage - self._last_try < self.retry_every * (1 << (self._backoff - 1)):
                 self.mode = "plain"
                 return self
         self._last_try = self._stage
         self._refit(annealer, step, fit_rows)
         self.rms = self._check(annealer, step, chk_rows)
-        self.mode = "da" if self.rms <= self.rms_limit else "plain"
+        self.delta = self._delta_check(annealer, step, chk_rows)
+        # a fresh fit that still fails waits longer before the next attempt
+        self._backoff = 0 if self._usable() else min(self._backoff + 1, 4)
+        self.mode = "da" if self._usable() else "plain"
         return self
+
+    def _usable(self):
+        return self.rms <= self.rms_limit and self.delta <= self.delta_limit
+
+    def _delta_check(self, annealer, step, rows):
+        """Spread of β[(s(y) - s(x)) - (l(y) - l(x))] over one trial proposal per check chain."""
+        model, strat, sur = annealer.model, annealer.model.strategy, self.surrogate
+        th = step.theta.index_select(0, rows).contiguous()
+        ex_x = step.data.index_select(0, rows)
+        c, p = th.shape
+        f64 = dict(dtype=torch.float64, device=DEVICE)
+        cand, cprior = torch.empty(c, p, **f64), torch.empty(c, **f64)
+        mask = torch.zeros(c, dtype=torch.int32, device=DEVICE)
+        s = stream_handle()
+        st = step.state.struct
+        _native.call("ag_cholesky_scaled", st, p, s)
+        _native.call("ag_propose", st, ptr(th), c, p, ptr(model.lo), ptr(model.hi), self.seed, 900000 + self._stage,
+                     ptr(cand), ptr(mask), ptr(cprior), s)
+        ex_y = torch.empty(c, **f64)
+        strat.forward(cand, ex_y, mask=mask, status=mask)
+        bufs = sur.buffers(c, p)
+        sx, sy = torch.empty(c, **f64), torch.empty(c, **f64)
+        sur.predict(th, self._bounds[0], self._bounds[1], sx, bufs)
+        sur.predict(cand, self._bounds[0], self._bounds[1], sy, bufs)
+        ok = mask == 0
+        if int(ok.sum()) < 2:
+            return float("inf")
+        eps = step.beta * ((sy - sx) - (ex_y - ex_x))[ok]
+        return float(eps.std())
 
     def _fields(self, strat, theta):
         n = theta.shape[0]

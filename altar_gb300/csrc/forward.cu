@@ -244,139 +244,248 @@ __global__ void cdm_check_kernel(ag_layout L, const double* __restrict__ theta, 
 }
 
 // ---------------------------------------------------------------------------
-// one angular-dislocation pair in difference arithmetic
-AG_DEVICE_INLINE float frcp(float x) { return fast_rcp(x); }
+// Scalar and two-station arithmetic.  side_pair is written once over a value
+// type V: float (one station per lane) or F2 (two stations per lane, every
+// add, multiply and FMA issued as one packed FP32x2 instruction, which halves
+// the issue slots of the FMA-pipe work).  Every product that feeds a sum is
+// written as an explicit FMA and the remaining adds and multiplies use the
+// non-contracting round-to-nearest forms, so both value types round every
+// operation identically and give bit-identical results.
+struct B2 { bool x, y; };
+struct F2 {
+    float2 v;
+    AG_DEVICE_INLINE F2() {}
+    AG_DEVICE_INLINE F2(float a) : v(make_float2(a, a)) {}
+    AG_DEVICE_INLINE F2(float a, float b) : v(make_float2(a, b)) {}
+    AG_DEVICE_INLINE explicit F2(float2 a) : v(a) {}
+};
+AG_DEVICE_INLINE F2 operator+(F2 a, F2 b) { return F2(__fadd2_rn(a.v, b.v)); }
+AG_DEVICE_INLINE F2 operator*(F2 a, F2 b) { return F2(__fmul2_rn(a.v, b.v)); }
+AG_DEVICE_INLINE F2 operator-(F2 a) { return F2(__fmul2_rn(a.v, make_float2(-1.0f, -1.0f))); }
+AG_DEVICE_INLINE F2 operator-(F2 a, F2 b) { return F2(__ffma2_rn(b.v, make_float2(-1.0f, -1.0f), a.v)); }
+AG_DEVICE_INLINE F2 vfma(F2 a, F2 b, F2 c) { return F2(__ffma2_rn(a.v, b.v, c.v)); }
+AG_DEVICE_INLINE F2 vadd(F2 a, F2 b) { return a + b; }
+AG_DEVICE_INLINE F2 vsub(F2 a, F2 b) { return a - b; }
+AG_DEVICE_INLINE F2 vmul(F2 a, F2 b) { return a * b; }
+AG_DEVICE_INLINE F2 vneg(F2 a) { return -a; }
+AG_DEVICE_INLINE float vfma(float a, float b, float c) { return fmaf(a, b, c); }
+AG_DEVICE_INLINE float vadd(float a, float b) { return __fadd_rn(a, b); }
+AG_DEVICE_INLINE float vsub(float a, float b) { return __fsub_rn(a, b); }
+AG_DEVICE_INLINE float vmul(float a, float b) { return __fmul_rn(a, b); }
+AG_DEVICE_INLINE float vneg(float a) { return -a; }
 
-AG_DEVICE_INLINE void side_pair(const SideC& S, float Xr, float Yr, float& ue, float& un,
-                                float& uv) {
-    const float4 q0 = S.q[0], q1 = S.q[1], q2 = S.q[2], q3 = S.q[3], q4 = S.q[4], q5 = S.q[5],
-                 q6 = S.q[6], q7 = S.q[7], q8 = S.q[8];
-    const float c = q0.x, s = q0.y;
-    const float dy1 = q1.x, aA = q1.y, aB = q1.z, da = q1.w;
+AG_DEVICE_INLINE bool vge0(float a) { return a >= 0.0f; }
+AG_DEVICE_INLINE B2 vge0(F2 a) { return {a.v.x >= 0.0f, a.v.y >= 0.0f}; }
+AG_DEVICE_INLINE bool vgt0(float a) { return a > 0.0f; }
+AG_DEVICE_INLINE B2 vgt0(F2 a) { return {a.v.x > 0.0f, a.v.y > 0.0f}; }
+AG_DEVICE_INLINE bool vand(bool a, bool b) { return a && b; }
+AG_DEVICE_INLINE B2 vand(B2 a, B2 b) { return {a.x && b.x, a.y && b.y}; }
+AG_DEVICE_INLINE float vsel(bool c, float a, float b) { return c ? a : b; }
+AG_DEVICE_INLINE F2 vsel(B2 c, F2 a, F2 b) { return F2(c.x ? a.v.x : b.v.x, c.y ? a.v.y : b.v.y); }
+
+AG_DEVICE_INLINE float frcp(float x) { return fast_rcp(x); }
+AG_DEVICE_INLINE F2 frcp(F2 x) { return F2(fast_rcp(x.v.x), fast_rcp(x.v.y)); }
+AG_DEVICE_INLINE float vrsqrt(float x) { return rsqrtf(x); }
+AG_DEVICE_INLINE F2 vrsqrt(F2 x) { return F2(rsqrtf(x.v.x), rsqrtf(x.v.y)); }
+AG_DEVICE_INLINE float vlog1p(float x) { return log1p_series(x); }
+AG_DEVICE_INLINE F2 vlog1p(F2 x) { return F2(log1p_series(x.v.x), log1p_series(x.v.y)); }
+AG_DEVICE_INLINE float vatan2(float y, float x) { return atan2_poly(y, x); }
+AG_DEVICE_INLINE F2 vatan2(F2 y, F2 x) { return F2(atan2_poly(y.v.x, x.v.x), atan2_poly(y.v.y, x.v.y)); }
+
+// Per-side constants as the two value types read them.  Index = position in SideC
+// (q[i >> 2], component i & 3); a few are also needed negated.
+enum : int {
+    K_C = 0, K_S, K_K1, K_K2, K_DY1, K_AA, K_AB, K_DA, K_SB, K_CB, K_TB2, K_CTB2, K_DAS, K_C1F, K_C2F, K_C3F,
+    K_C1P, K_C2P, K_KC1, K_KC2, K_NB1, K_NB2, K_HB1, K_HB2, K_B1, K_B2, K_C1M10, K_C3M10, K_C1Q, K_C2Q, K_C3Q,
+    K_C1M11, K_C3M11, K_C1M12
+};
+// negated constants: entry k of this list sits at slot 36 + k of the pair table
+__host__ __device__ constexpr int neg_entry(int k) {
+    constexpr int list[] = {K_C,   K_K1,  K_K2,  K_CB,    K_TB2,   K_B1, K_B2, K_KC1, K_KC2,
+                            K_HB2, K_NB2, K_DY1, K_C1M10, K_C3M10, K_NB1, K_DA, K_AA};
+    return k < (int)(sizeof(list) / sizeof(int)) ? list[k] : -1;
+}
+constexpr int kNegCount = 17;
+static_assert(neg_entry(kNegCount - 1) >= 0 && neg_entry(kNegCount) < 0, "negated-constant count");
+constexpr int kPairSlots = (36 + kNegCount + 1) & ~1;   // even: whole float4 pairs of pairs
+__host__ __device__ constexpr int neg_slot(int i) {
+    int k = 0;
+    while (k < kNegCount && neg_entry(k) != i) ++k;
+    return 36 + k;
+}
+
+// one side's constants duplicated into (v, v) pairs, plain then negated (two-station kernels)
+struct __align__(16) SideP {
+    float2 v[kPairSlots];
+};
+
+struct ScalarSide {
+    float4 q[9];
+    AG_DEVICE_INLINE explicit ScalarSide(const SideC& S) {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) q[i] = S.q[i];
+    }
+    template <int I>
+    AG_DEVICE_INLINE float at() const {
+        const float4 t = q[I >> 2];
+        return (I & 3) == 0 ? t.x : (I & 3) == 1 ? t.y : (I & 3) == 2 ? t.z : t.w;
+    }
+    template <int I>
+    AG_DEVICE_INLINE float neg() const { return -at<I>(); }
+};
+
+struct PairSide {
+    const SideP& P;
+    AG_DEVICE_INLINE explicit PairSide(const SideP& p) : P(p) {}
+    template <int I>
+    AG_DEVICE_INLINE F2 at() const { return F2(P.v[I]); }
+    template <int I>
+    AG_DEVICE_INLINE F2 neg() const {
+        static_assert(neg_slot(I) < 36 + kNegCount, "constant missing from the negated table");
+        return F2(P.v[neg_slot(I)]);
+    }
+};
+
+AG_DEVICE_INLINE void expand_side(const SideC& S, SideP& P) {
+    const float* f = reinterpret_cast<const float*>(S.q);
+#pragma unroll
+    for (int i = 0; i < 36; ++i) P.v[i] = make_float2(f[i], f[i]);
+#pragma unroll
+    for (int k = 0; k < kNegCount; ++k) P.v[36 + k] = make_float2(-f[neg_entry(k)], -f[neg_entry(k)]);
+    P.v[kPairSlots - 1] = make_float2(0.f, 0.f);
+}
+
+#define KC(i) k.template at<i>()
+#define KN(i) k.template neg<i>()
+
+// ---------------------------------------------------------------------------
+// one angular-dislocation pair in difference arithmetic
+template <class V, class K>
+AG_DEVICE_INLINE void side_pair(const K& k, V Xr, V Yr, V& ue, V& un, V& uv) {
+    const V c = KC(K_C), s = KC(K_S);
+    const V dy1 = KC(K_DY1), aA = KC(K_AA), aB = KC(K_AB), da = KC(K_DA);
     // station in the angular-dislocation frame of vertex A; y2 is the same at B
-    const float y1A = fmaf(c, Xr, fmaf(s, Yr, -q0.z));
-    const float y2 = fmaf(s, Xr, fmaf(-c, Yr, -q0.w));
-    const float y1B = y1A + dy1;
+    const V y1A = vfma(c, Xr, vfma(s, Yr, KN(K_K1)));
+    const V y2 = vfma(s, Xr, vfma(KN(K_C), Yr, KN(K_K2)));
+    const V y1B = vadd(y1A, dy1);
     // artefact-free configuration (libcdm.py:342-362): I if y1A >= 0 (β - π), else II (β)
-    const bool conf1 = y1A >= 0.0f;
-    const float sg = conf1 ? -1.0f : 1.0f;
-    const float sB = sg * q2.x, cB = sg * q2.y;
-    const float ct2 = conf1 ? -q2.z : q2.w;
-    const float y22 = y2 * y2;
-    // r
-    const float r2A = fmaf(y1A, y1A, fmaf(aA, aA, y22));
-    const float r2B = fmaf(y1B, y1B, fmaf(aB, aB, y22));
-    const float irA = rsqrtf(r2A), irB = rsqrtf(r2B);
-    const float rA = r2A * irA, rB = r2B * irB;
-    const float dr = fmaf(dy1, y1A + y1B, q3.x) * frcp(rA + rB);
-    const float dir = -dr * irA * irB;
+    const auto conf1 = vge0(y1A);
+    const V sg = vsel(conf1, V(-1.0f), V(1.0f));
+    const V sB = vmul(sg, KC(K_SB)), cB = vmul(sg, KC(K_CB)), ncB = vmul(sg, KN(K_CB));
+    const V ct2 = vsel(conf1, KN(K_TB2), KC(K_CTB2));
+    const V y22 = vmul(y2, y2);
+    // r (rA = r2A·irA enters every sum through an FMA)
+    const V r2A = vfma(y1A, y1A, vfma(aA, aA, y22));
+    const V r2B = vfma(y1B, y1B, vfma(aB, aB, y22));
+    const V irA = vrsqrt(r2A), irB = vrsqrt(r2B);
+    const V rB = vmul(r2B, irB);
+    const V dr = vmul(vfma(dy1, vadd(y1A, y1B), KC(K_DAS)), frcp(vfma(r2A, irA, rB)));
+    const V ndir = vmul(vmul(dr, irA), irB);           // -Δ(1/r)
     // r + a
-    const float pA = rA + aA, pB = rB + aB, dp = dr + da;
-    const float ipA = frcp(pA), ipB = frcp(pB);
-    const float dip = -dp * ipA * ipB;
+    const V pA = vfma(r2A, irA, aA), pB = vfma(r2B, irB, aB), dp = vadd(dr, da);
+    const V ipA = frcp(pA), ipB = frcp(pB);
+    const V ndip = vmul(vmul(dp, ipA), ipB);           // -Δ(1/(r+a))
     // z1, z3
-    const float z1A = fmaf(y1A, cB, aA * sB);
-    const float dz1 = fmaf(dy1, cB, da * sB);
-    const float z1B = z1A + dz1;
-    const float z3A = fmaf(y1A, sB, -aA * cB);
-    const float dz3 = fmaf(dy1, sB, -da * cB);
-    const float z3B = z3A + dz3;
-    // r - z3, cancellation-free: (z1² + y2²)/(r + z3) when z3 > 0
-    const bool posA = z3A > 0.0f, posB = z3B > 0.0f;
-    const float NA = fmaf(z1A, z1A, y22), NB = fmaf(z1B, z1B, y22);
-    const float DA = rA + z3A, DB = rB + z3B;
-    const float uA = posA ? NA : rA - z3A, vA = posA ? DA : 1.0f;
-    const float uB = posB ? NB : rB - z3B, vB = posB ? DB : 1.0f;
-    const float iuA = frcp(uA), ivA = frcp(vA), iuB = frcp(uB), ivB = frcp(vB);
-    const float qA = uA * ivA;
-    const float iqA = vA * iuA, iqB = vB * iuB;
-    const float dN = dz1 * (z1A + z1B);
-    const float dq = (posA && posB) ? fmaf(dN, DA, -NA * (dr + dz3)) * ivA * ivB : dr - dz3;
-    const float diq = -dq * iqA * iqB;
+    const V z1A = vfma(y1A, cB, vmul(aA, sB));
+    const V dz1 = vfma(dy1, cB, vmul(da, sB));
+    const V z1B = vadd(z1A, dz1);
+    const V z3A = vfma(y1A, sB, vmul(aA, ncB));
+    const V dz3 = vfma(dy1, sB, vmul(da, ncB));
+    const V z3B = vadd(z3A, dz3);
+    // r - z3, cancellation-free: (z1² + y2²)/(r + z3) when z3 > 0, else (r + z3) - 2 z3
+    const auto posA = vgt0(z3A), posB = vgt0(z3B);
+    const V NA = vfma(z1A, z1A, y22), NB = vfma(z1B, z1B, y22);
+    const V DA = vfma(r2A, irA, z3A), DB = vfma(r2B, irB, z3B);
+    const V uA = vsel(posA, NA, vfma(V(-2.0f), z3A, DA)), vA = vsel(posA, DA, V(1.0f));
+    const V uB = vsel(posB, NB, vfma(V(-2.0f), z3B, DB)), vB = vsel(posB, DB, V(1.0f));
+    const V iuA = frcp(uA), ivA = frcp(vA), iuB = frcp(uB), ivB = frcp(vB);
+    const V iqA = vmul(vA, iuA), iqB = vmul(vB, iuB);
+    const V dN = vmul(dz1, vadd(z1A, z1B));
+    const V dq = vsel(vand(posA, posB), vmul(vmul(vfma(dN, DA, vneg(vmul(NA, vadd(dr, dz3)))), ivA), ivB),
+                      vsub(dr, dz3));
+    const V ndiq = vmul(vmul(dq, iqA), iqB);           // -Δ(1/q)
     // log differences
-    const float dLp = log1p_series(dp * ipA);
-    const float dLq = log1p_series(dq * iqA);
-    (void)qA;
+    const V dLp = vlog1p(vmul(dp, ipA));
+    const V dLq = vlog1p(vmul(dq, iqA));
     // Burgers function difference: rotation of (x, y2) from A to B; y2 keeps its sign so
     // the rotation never crosses atan2's cut
-    const float xA = fmaf(pA, ct2, -y1A);
-    const float dx = fmaf(dp, ct2, -dy1);
-    const float xB = xA + dx;
-    const float dF = 2.0f * atan2_poly(-y2 * dx, fmaf(xA, xB, y22));
+    const V xA = vfma(pA, ct2, vneg(y1A));
+    const V dx = vfma(dp, ct2, KN(K_DY1));
+    const V xB = vadd(xA, dx);
+    const V dF = vmul(V(2.0f), vatan2(vmul(vneg(y2), dx), vfma(xA, xB, y22)));
     // monomials: value at A, value at B, difference
-    const float m1A = y2 * ipA, m1B = y2 * ipB, dm1 = y2 * dip;
-    const float m2A = y1A * ipA, m2B = y1B * ipB, dm2 = fmaf(dy1, ipB, y1A * dip);
-    const float dm3 = fmaf(da, ipB, aA * dip);
-    const float dm4 = fmaf(dm2, m1B, m2A * dm1);
-    const float dm5 = dm2 * (m2A + m2B);
-    const float dm6 = dm1 * (m1A + m1B);
-    const float y1irA = y1A * irA, dy1ir = fmaf(dy1, irB, y1A * dir);
-    const float y2irA = y2 * irA, dy2ir = y2 * dir;
-    const float airA = aA * irA, dair = fmaf(da, irB, aA * dir);
-    const float m10B = y2 * iqB, dm10 = y2 * diq;
-    const float m11B = z1B * iqB, dm11 = fmaf(dz1, iqB, z1A * diq);
-    // coefficients (precomputed per side; configuration sign applied here)
-    const float C1F = q3.y, C2F = q3.z, C3F = q3.w;
-    const float C1P = q4.x, C2P = q4.y, kc1 = q4.z, kc2 = q4.w;
-    const float nb1 = q5.x, nb2 = q5.y, hb1 = q5.z, hb2 = q5.w;
-    const float b1 = q6.x, b2 = q6.y, C1m10 = q6.z, C3m10 = q6.w;
-    const float C1Q = q7.x, C2Q = q7.y, C3Q = q7.z, C1m11 = q7.w;
-    const float C3m11 = q8.x;
-    const float c12 = sg * q8.y;                       // signed coefficient of the (m10 · r⁻¹) products
+    const V m1B = vmul(y2, ipB), ndm1 = vmul(y2, ndip);
+    const V m2A = vmul(y1A, ipA), m2B = vmul(y1B, ipB);
+    const V dm2 = vfma(dy1, ipB, vneg(vmul(y1A, ndip)));
+    const V dm3 = vfma(da, ipB, vmul(KN(K_AA), ndip));
+    const V dm4 = vfma(dm2, m1B, vneg(vmul(m2A, ndm1)));
+    const V dm35 = vfma(dm2, vfma(y1A, ipA, m2B), dm3);          // dm3 + dm2 (m2A + m2B)
+    const V dm36 = vfma(ndm1, vneg(vfma(y2, ipA, m1B)), dm3);    // dm3 + dm1 (m1A + m1B)
+    const V y1irA = vmul(y1A, irA), dy1ir = vfma(dy1, irB, vneg(vmul(y1A, ndir)));
+    const V y2irA = vmul(y2, irA), ndy2ir = vmul(y2, ndir);
+    const V nairA = vmul(KN(K_AA), irA), ndair = vfma(KN(K_DA), irB, vmul(aA, ndir));
+    const V m10B = vmul(y2, iqB), ndm10 = vmul(y2, ndiq);
+    const V m11B = vmul(z1B, iqB), dm11 = vfma(dz1, iqB, vneg(vmul(z1A, ndiq)));
+    const V c12 = vmul(sg, KC(K_C1M12));              // signed coefficient of the (m10 · r⁻¹) products
     // The r⁻¹-weighted monomials share two brackets (distributivity of Δ(u v) = Δu v_B + u_A Δv):
     //   v1: -b1 Δ(y1 r⁻¹ m1) + b2 Δ(y1 r⁻¹ m2) - b2 Δ(y1 r⁻¹ m11) + c12 Δ(y1 r⁻¹ m10)
     //       = Δ(y1 r⁻¹)·X1 + (y1 r⁻¹)_A·ΔX1
     //   v3: the same brackets with a r⁻¹ in place of y1 r⁻¹, negated
     //   v2: b2 Δ(y1 r⁻¹ m1) + Δ(y2 r⁻¹)·X2 + (y2 r⁻¹)_A·ΔX2
-    const float X2 = fmaf(-b1, m1B, fmaf(-b2, m11B, c12 * m10B));
-    const float dX2 = fmaf(-b1, dm1, fmaf(-b2, dm11, c12 * dm10));
-    const float X1 = fmaf(b2, m2B, X2);
-    const float dX1 = fmaf(b2, dm2, dX2);
-    float v1 = C1F * dF;
-    v1 = fmaf(C1P, dLp, v1);
-    v1 = fmaf(kc1, dm1, v1);
-    v1 = fmaf(-kc2, dm2, v1);
-    v1 = fmaf(-hb2, dm3 + dm5, v1);
-    v1 = fmaf(hb1, dm4, v1);
-    v1 = fmaf(C1m10, dm10, v1);
-    v1 = fmaf(dy1ir, X1, v1);
-    v1 = fmaf(y1irA, dX1, v1);
-    v1 = fmaf(sg, fmaf(C1Q, dLq, C1m11 * dm11), v1);
-    float v2 = C2F * dF;
-    v2 = fmaf(C2P, dLp, v2);
-    v2 = fmaf(-kc2, dm1, v2);
-    v2 = fmaf(-kc1, dm2, v2);
-    v2 = fmaf(hb1, dm3 + dm6, v2);
-    v2 = fmaf(-hb2, dm4, v2);
-    v2 = fmaf(b2, fmaf(dy1ir, m1B, y1irA * dm1), v2);
-    v2 = fmaf(dy2ir, X2, v2);
-    v2 = fmaf(y2irA, dX2, v2);
-    v2 = fmaf(sg * C2Q, dLq, v2);
-    float v3 = C3F * dF;
-    v3 = fmaf(-kc2, dLp, v3);
-    v3 = fmaf(nb1, dm1, v3);
-    v3 = fmaf(-nb2, dm2, v3);
-    v3 = fmaf(C3m10, dm10, v3);
-    v3 = fmaf(-dair, X1, v3);
-    v3 = fmaf(-airA, dX1, v3);
-    v3 = fmaf(sg, fmaf(C3Q, dLq, C3m11 * dm11), v3);
+    // (ndm1, ndm10, ndy2ir: negated differences, folded into the coefficient signs)
+    const V X2 = vfma(KN(K_B1), m1B, vfma(KN(K_B2), m11B, vmul(c12, m10B)));
+    const V dX2 = vfma(KC(K_B1), ndm1, vfma(KN(K_B2), dm11, vneg(vmul(c12, ndm10))));
+    const V X1 = vfma(KC(K_B2), m2B, X2);
+    const V dX1 = vfma(KC(K_B2), dm2, dX2);
+    V v1 = vmul(KC(K_C1F), dF);
+    v1 = vfma(KC(K_C1P), dLp, v1);
+    v1 = vfma(KN(K_KC1), ndm1, v1);
+    v1 = vfma(KN(K_KC2), dm2, v1);
+    v1 = vfma(KN(K_HB2), dm35, v1);
+    v1 = vfma(KC(K_HB1), dm4, v1);
+    v1 = vfma(KN(K_C1M10), ndm10, v1);
+    v1 = vfma(dy1ir, X1, v1);
+    v1 = vfma(y1irA, dX1, v1);
+    v1 = vfma(sg, vfma(KC(K_C1Q), dLq, vmul(KC(K_C1M11), dm11)), v1);
+    V v2 = vmul(KC(K_C2F), dF);
+    v2 = vfma(KC(K_C2P), dLp, v2);
+    v2 = vfma(KC(K_KC2), ndm1, v2);
+    v2 = vfma(KN(K_KC1), dm2, v2);
+    v2 = vfma(KC(K_HB1), dm36, v2);
+    v2 = vfma(KN(K_HB2), dm4, v2);
+    v2 = vfma(KC(K_B2), vfma(dy1ir, m1B, vneg(vmul(y1irA, ndm1))), v2);
+    v2 = vfma(vneg(ndy2ir), X2, v2);
+    v2 = vfma(y2irA, dX2, v2);
+    v2 = vfma(vmul(sg, KC(K_C2Q)), dLq, v2);
+    V v3 = vmul(KC(K_C3F), dF);
+    v3 = vfma(KN(K_KC2), dLp, v3);
+    v3 = vfma(KN(K_NB1), ndm1, v3);
+    v3 = vfma(KN(K_NB2), dm2, v3);
+    v3 = vfma(KN(K_C3M10), ndm10, v3);
+    v3 = vfma(ndair, X1, v3);
+    v3 = vfma(nairA, dX1, v3);
+    v3 = vfma(sg, vfma(KC(K_C3Q), dLq, vmul(KC(K_C3M11), dm11)), v3);
     // back to EFCS: columns e1 = (c, s, 0), e2 = (s, -c, 0), e3 = (0, 0, -1)
-    ue = fmaf(c, v1, fmaf(s, v2, ue));
-    un = fmaf(s, v1, fmaf(-c, v2, un));
-    uv -= v3;
+    ue = vfma(c, v1, vfma(s, v2, ue));
+    un = vfma(s, v1, vfma(KN(K_C), v2, un));
+    uv = vsub(uv, v3);
 }
 
+#undef KC
+#undef KN
+
 // ---------------------------------------------------------------------------
-template <int WARPS, int MINB>
+template <int WARPS, int MINB, bool PAIRED>
 __global__ void __launch_bounds__(WARPS * 32, MINB)
 cdm_llk_kernel(const ChainC* __restrict__ chains, int n, const float4* __restrict__ xy,
                const float4* __restrict__ losd, const float* __restrict__ wt,
-               const int32_t* __restrict__ oid, int m_padded, double norm,
+               const int32_t* __restrict__ oid, int m, int m_padded, double norm,
                double* __restrict__ llk, float* __restrict__ resid, uint32_t* __restrict__ flags,
                const int32_t* __restrict__ index, const int32_t* __restrict__ count) {
     // with an index list, slots beyond the device-side count have nothing to do
     if (index && (int)(blockIdx.x * WARPS) >= *count) return;
     __shared__ ChainC s_chain[WARPS];
+    __shared__ SideP s_pair[PAIRED ? WARPS : 1][PAIRED ? kSides : 1];
     __shared__ float4 s_xy[2][kTile];
     __shared__ float4 s_ld[2][kTile];
     __shared__ __align__(16) float s_w[2][kTile];
@@ -404,6 +513,11 @@ cdm_llk_kernel(const ChainC* __restrict__ chains, int n, const float4* __restric
         fence_mbar_init();
     }
     __syncthreads();
+    if constexpr (PAIRED) {
+        // each warp duplicates its own chain's side constants into (v, v) pairs
+        if (lane < kSides) expand_side(s_chain[warp].side[lane], s_pair[warp][lane]);
+        __syncwarp();
+    }
     auto issue = [&](int t, int buf) {
         const size_t base = (size_t)t * kTile;
         mbar_arrive_expect_tx(&bar[buf], tile_bytes);
@@ -429,25 +543,49 @@ cdm_llk_kernel(const ChainC* __restrict__ chains, int n, const float4* __restric
         const bool ok = mbar_wait_bounded(&bar[buf], phase, kWaitLimit);
         if (__syncthreads_or(!ok)) { failed_at = t; break; }
         if (active) {
-            for (int j = lane; j < kTile; j += 32) {
-                const float4 A = s_xy[buf][j];
-                const float4 B = s_ld[buf][j];
-                const float w = s_w[buf][j];
-                const float Xr = (A.x - x0h) + (A.y - x0l);
-                const float Yr = (A.z - y0h) + (A.w - y0l);
-                float ue = 0.f, un = 0.f, uv = 0.f;
-                uint32_t m = smask & 0x0FFFu;
-#pragma unroll 1
-                while (m) {
-                    const int sidx = __ffs(m) - 1;
-                    m &= m - 1;
-                    side_pair(C.side[sidx], Xr, Yr, ue, un, uv);
-                }
-                const float u = fmaf(ue, B.x, fmaf(un, B.y, uv * B.z));
+            // u projected on the LOS, minus data and offset; accumulate w r² and store r
+            auto finish = [&](float e_, float n_, float v_, const float4& B, float w, int j) {
+                const float u = fmaf(e_, B.x, fmaf(n_, B.y, v_ * B.z));
                 float r = u - B.w;
                 if (with_oid) r -= C.off[s_oid[buf][j] & (kMaxOffsets - 1)];
                 if (w != 0.f) ff_add_wsq(acc, r, w);
-                if (resid) resid[(size_t)chain * m_padded + (size_t)t * kTile + j] = (w != 0.f) ? r : 0.f;
+                if (resid) {
+                    const int col = t * kTile + j;
+                    resid[(size_t)chain * m_padded + col] = (col < m) ? r : 0.f;
+                }
+            };
+            if constexpr (PAIRED) {
+                // stations j and j + 32 together; accumulation order as in the scalar loop
+                for (int j = lane; j < kTile; j += 64) {
+                    const float4 A0 = s_xy[buf][j], A1 = s_xy[buf][j + 32];
+                    const F2 Xr = (F2(A0.x, A1.x) - F2(x0h)) + (F2(A0.y, A1.y) - F2(x0l));
+                    const F2 Yr = (F2(A0.z, A1.z) - F2(y0h)) + (F2(A0.w, A1.w) - F2(y0l));
+                    F2 ue(0.f), un(0.f), uv(0.f);
+                    uint32_t msk = smask & 0x0FFFu;
+#pragma unroll 1
+                    while (msk) {
+                        const int sidx = __ffs(msk) - 1;
+                        msk &= msk - 1;
+                        side_pair<F2>(PairSide(s_pair[warp][sidx]), Xr, Yr, ue, un, uv);
+                    }
+                    finish(ue.v.x, un.v.x, uv.v.x, s_ld[buf][j], s_w[buf][j], j);
+                    finish(ue.v.y, un.v.y, uv.v.y, s_ld[buf][j + 32], s_w[buf][j + 32], j + 32);
+                }
+            } else {
+                for (int j = lane; j < kTile; j += 32) {
+                    const float4 A = s_xy[buf][j];
+                    const float Xr = (A.x - x0h) + (A.y - x0l);
+                    const float Yr = (A.z - y0h) + (A.w - y0l);
+                    float ue = 0.f, un = 0.f, uv = 0.f;
+                    uint32_t msk = smask & 0x0FFFu;
+#pragma unroll 1
+                    while (msk) {
+                        const int sidx = __ffs(msk) - 1;
+                        msk &= msk - 1;
+                        side_pair<float>(ScalarSide(C.side[sidx]), Xr, Yr, ue, un, uv);
+                    }
+                    finish(ue, un, uv, s_ld[buf][j], s_w[buf][j], j);
+                }
             }
         }
         __syncthreads();
@@ -481,7 +619,7 @@ __global__ void __launch_bounds__(256, 2)
 mogi_llk_kernel(ag_layout L, const double* __restrict__ theta, int n,
                 const uint32_t* __restrict__ mask_in, const float4* __restrict__ xy,
                 const float4* __restrict__ losd, const float* __restrict__ wt,
-                const int32_t* __restrict__ oid, int noffsets, int m_padded, double norm,
+                const int32_t* __restrict__ oid, int noffsets, int m, int m_padded, double norm,
                 double* __restrict__ llk, float* __restrict__ resid, const int32_t* __restrict__ index,
                 const int32_t* __restrict__ count) {
     if (index && (int)(blockIdx.x * CH) >= *count) return;
@@ -547,7 +685,7 @@ mogi_llk_kernel(ag_layout L, const double* __restrict__ theta, int n,
             float r = u - B.w;
             if (oid) r -= s_off[c][o];
             if (w != 0.f) ff_add_wsq(acc[c], r, w);
-            if (resid && s_chain[c] < n) resid[(size_t)s_chain[c] * m_padded + j] = (w != 0.f) ? r : 0.f;
+            if (resid && s_chain[c] < n) resid[(size_t)s_chain[c] * m_padded + j] = (j < m) ? r : 0.f;
         }
     }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -574,8 +712,8 @@ using namespace ag;
 // CDM launch variants: warps (= chains) per CTA and resident CTAs per SM the
 // register allocation targets; chosen per problem by the autotuner
 struct CdmVariant { int warps; };
-static constexpr CdmVariant kCdmVariants[] = {{8}, {4}, {4}, {16}};
-static constexpr int kCdmVariantCount = 4;
+static constexpr CdmVariant kCdmVariants[] = {{8}, {4}, {4}, {16}, {4}, {4}, {4}};
+static constexpr int kCdmVariantCount = 7;
 static constexpr int kMogiChains = 16;
 
 extern "C" int32_t ag_forward_variants(int model) { return model == AG_MODEL_CDM ? kCdmVariantCount : 1; }
@@ -639,20 +777,35 @@ static int forward_llk(int model, const ag_layout* layout, const double* theta, 
         const float4* ld_ = ld;
         switch (v) {
             case 0:
-                cdm_llk_kernel<8, 2><<<grid, 8 * 32, 0, s>>>(chains, n, xy, ld_, st->weight, st->oid, st->m_padded,
+                cdm_llk_kernel<8, 2, false><<<grid, 8 * 32, 0, s>>>(chains, n, xy, ld_, st->weight, st->oid, st->m, st->m_padded,
                                                              norm, llk, residuals, nullptr, index, count);
                 break;
             case 1:
-                cdm_llk_kernel<4, 4><<<grid, 4 * 32, 0, s>>>(chains, n, xy, ld_, st->weight, st->oid, st->m_padded,
+                cdm_llk_kernel<4, 4, false><<<grid, 4 * 32, 0, s>>>(chains, n, xy, ld_, st->weight, st->oid, st->m, st->m_padded,
                                                              norm, llk, residuals, nullptr, index, count);
                 break;
             case 2:
-                cdm_llk_kernel<4, 5><<<grid, 4 * 32, 0, s>>>(chains, n, xy, ld_, st->weight, st->oid, st->m_padded,
+                cdm_llk_kernel<4, 5, false><<<grid, 4 * 32, 0, s>>>(chains, n, xy, ld_, st->weight, st->oid, st->m, st->m_padded,
                                                              norm, llk, residuals, nullptr, index, count);
                 break;
+            case 4:
+                cdm_llk_kernel<4, 5, true><<<grid, 4 * 32, 0, s>>>(chains, n, xy, ld_, st->weight, st->oid, st->m,
+                                                                  st->m_padded, norm, llk, residuals, nullptr, index,
+                                                                  count);
+                break;
+            case 5:
+                cdm_llk_kernel<4, 3, true><<<grid, 4 * 32, 0, s>>>(chains, n, xy, ld_, st->weight, st->oid, st->m,
+                                                                  st->m_padded, norm, llk, residuals, nullptr, index,
+                                                                  count);
+                break;
+            case 6:
+                cdm_llk_kernel<4, 4, true><<<grid, 4 * 32, 0, s>>>(chains, n, xy, ld_, st->weight, st->oid, st->m,
+                                                                  st->m_padded, norm, llk, residuals, nullptr, index,
+                                                                  count);
+                break;
             default:
-                cdm_llk_kernel<16, 1><<<grid, 16 * 32, 0, s>>>(chains, n, xy, ld_, st->weight, st->oid,
-                                                               st->m_padded, norm, llk, residuals, nullptr, index,
+                cdm_llk_kernel<16, 1, false><<<grid, 16 * 32, 0, s>>>(chains, n, xy, ld_, st->weight, st->oid,
+                                                               st->m, st->m_padded, norm, llk, residuals, nullptr, index,
                                                                count);
                 break;
         }
@@ -663,11 +816,11 @@ static int forward_llk(int model, const ag_layout* layout, const double* theta, 
         const int grid = (n + kMogiChains - 1) / kMogiChains;
         if (L.nsources == 1)
             mogi_llk_kernel<kMogiChains, 1><<<grid, 256, 0, s>>>(
-                L, theta, n, mask_in, xy, ld, st->weight, st->oid, noffsets, st->m_padded, norm, llk,
+                L, theta, n, mask_in, xy, ld, st->weight, st->oid, noffsets, st->m, st->m_padded, norm, llk,
                 residuals, index, count);
         else
             mogi_llk_kernel<kMogiChains, 2><<<grid, 256, 0, s>>>(
-                L, theta, n, mask_in, xy, ld, st->weight, st->oid, noffsets, st->m_padded, norm, llk,
+                L, theta, n, mask_in, xy, ld, st->weight, st->oid, noffsets, st->m, st->m_padded, norm, llk,
                 residuals, index, count);
         return launch_status("mogi_llk_kernel");
     }

@@ -195,6 +195,17 @@ linear_misfit_tc_kernel(const __grid_constant__ CUtensorMap map_a,   // chains  
     }
 }
 
+// ρ₀ = W r̄ in FP64 (one warp per whitened observation)
+__global__ void whiten_rho0_kernel(const double* __restrict__ W, const double* __restrict__ mean, int m,
+                                   float* __restrict__ rho0) {
+    const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (row >= m) return;
+    double s = 0.0;
+    for (int j = lane; j < m; j += 32) s = fma(W[(size_t)row * m + j], mean[j], s);
+    s = warp_sum(s);
+    if (lane == 0) rho0[row] = (float)s;
+}
+
 // θ₀ = column means of θ (one thread per parameter, fixed order)
 __global__ void column_mean_kernel(const double* __restrict__ theta, int n, int p, double* __restrict__ mean) {
     int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -247,13 +258,41 @@ __global__ void split_a_kernel(const double* __restrict__ A, int m, int p, int k
 }
 
 __global__ void linear_reduce_kernel(int n, int tiles, const double* __restrict__ partial, double norm,
-                                     double* __restrict__ llk) {
+                                     double* __restrict__ llk, int accumulate) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     double s = 0.0;
     for (int t = 0; t < tiles; ++t) s += partial[(size_t)t * n + i];
-    llk[i] = norm - 0.5 * s;
+    llk[i] = (accumulate ? llk[i] : norm) - 0.5 * s;
 }
+
+// column means of an FP32 block (n rows, m columns from col0, row stride ld), FP64 accumulation
+__global__ void block_mean_kernel(const float* __restrict__ r, int ld, int col0, int n, int m,
+                                  double* __restrict__ mean) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= m) return;
+    double s = 0.0;
+    for (int i = 0; i < n; ++i) s += (double)r[(size_t)i * ld + col0 + j];
+    mean[j] = s / n;
+}
+
+// δ = r - r̄ split as [hi | lo | hi] (BF16), rows of length 3 kp
+__global__ void split_block_kernel(const float* __restrict__ r, int ld, int col0, const double* __restrict__ mean,
+                                   int n, int m, int kp, __nv_bfloat16* __restrict__ out) {
+    const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (long)n * kp) return;
+    const int i = (int)(e / kp), j = (int)(e % kp);
+    float d = 0.f;
+    if (j < m) d = (float)((double)r[(size_t)i * ld + col0 + j] - mean[j]);
+    const __nv_bfloat16 hi = __float2bfloat16_rn(d);
+    const __nv_bfloat16 lo = __float2bfloat16_rn(d - __bfloat162float(hi));
+    __nv_bfloat16* row = out + (size_t)i * 3 * kp;
+    row[j] = hi;
+    row[kp + j] = lo;
+    row[2 * kp + j] = hi;
+}
+
+
 
 // Exact FP64 reference path: ρ = A θ - b per chain (one warp per chain, observations strided)
 __global__ void linear_fp64_kernel(const double* __restrict__ A, const double* __restrict__ b,
@@ -368,8 +407,61 @@ extern "C" int ag_linear_llk(const ag_linear_model* lm, const double* theta, int
     linear_misfit_tc_kernel<<<grid, 128, TC_SMEM, s>>>(ma, mb, n, m, 3 * kp / TC_BK, rho0, partial, flags);
     rc = launch_status("linear_misfit_tc_kernel");
     if (rc) return rc;
-    linear_reduce_kernel<<<cdiv(n, 256), 256, 0, s>>>(n, tiles, partial, norm, llk);
+    linear_reduce_kernel<<<cdiv(n, 256), 256, 0, s>>>(n, tiles, partial, norm, llk, 0);
     return launch_status("linear_reduce_kernel");
+}
+
+extern "C" size_t ag_whiten_workspace_bytes(int32_t m, int32_t n) {
+    if (m <= 0 || n <= 0) return 0;
+    const size_t kp = ag_linear_kpad(m);
+    return al256(m * sizeof(double)) + al256(sizeof(double)) + al256((size_t)m * sizeof(float)) +
+           al256((size_t)n * 3 * kp * 2) + al256((size_t)cdiv(m, TC_BN) * n * sizeof(double));
+}
+
+extern "C" int ag_whiten_llk(const ag_whiten_block* blk, const float* resid, int32_t ldr, int32_t n,
+                             double* llk, void* workspace, size_t workspace_bytes, uint32_t* flags,
+                             void* stream) {
+    AG_REQUIRE(blk && blk->w64 && blk->w_split && resid && llk && n > 0, "invalid arguments");
+    const int m = blk->m, col0 = blk->col0;
+    AG_REQUIRE(m > 0 && col0 >= 0 && col0 + m <= ldr, "block columns [%d, %d) outside rows of %d", col0, col0 + m,
+               ldr);
+    const size_t need = ag_whiten_workspace_bytes(m, n);
+    AG_REQUIRE(workspace && workspace_bytes >= need && aligned(workspace, 256),
+               "ag_whiten_llk needs %zu bytes of 256-byte aligned workspace", need);
+    AG_REQUIRE(aligned(blk->w_split, 16), "w_split must be 16-byte aligned");
+    cudaStream_t s = as_stream(stream);
+    const int kp = ag_linear_kpad(m);
+    char* ws = static_cast<char*>(workspace);
+    double* mean = reinterpret_cast<double*>(ws); ws += al256(m * sizeof(double));
+    ws += al256(sizeof(double));
+    float* rho0 = reinterpret_cast<float*>(ws); ws += al256((size_t)m * sizeof(float));
+    __nv_bfloat16* rsplit = reinterpret_cast<__nv_bfloat16*>(ws); ws += al256((size_t)n * 3 * kp * 2);
+    double* partial = reinterpret_cast<double*>(ws);
+    const int tiles = cdiv(m, TC_BN);
+    block_mean_kernel<<<cdiv(m, 128), 128, 0, s>>>(resid, ldr, col0, n, m, mean);
+    int rc = launch_status("whitening prologue");
+    if (rc) return rc;
+    split_block_kernel<<<cdiv((long)n * kp, 256), 256, 0, s>>>(resid, ldr, col0, mean, n, m, kp, rsplit);
+    rc = launch_status("split_block_kernel");
+    if (rc) return rc;
+    CUtensorMap ma, mb;
+    rc = make_map(&ma, rsplit, n, 3 * kp, TC_BM);
+    if (rc) return rc;
+    rc = make_map(&mb, blk->w_split, m, 3 * kp, TC_BN);
+    if (rc) return rc;
+    rc = cuda_status(cudaFuncSetAttribute(linear_misfit_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)TC_SMEM),
+                     "cudaFuncSetAttribute(linear_misfit_tc_kernel)");
+    if (rc) return rc;
+    whiten_rho0_kernel<<<cdiv((long)m * 32, 256), 256, 0, s>>>(blk->w64, mean, m, rho0);
+    rc = launch_status("whiten_rho0_kernel");
+    if (rc) return rc;
+    dim3 grid(cdiv(n, TC_BM), tiles);
+    linear_misfit_tc_kernel<<<grid, 128, TC_SMEM, s>>>(ma, mb, n, m, 3 * kp / TC_BK, rho0, partial, flags);
+    rc = launch_status("linear_misfit_tc_kernel (whitening)");
+    if (rc) return rc;
+    linear_reduce_kernel<<<cdiv(n, 256), 256, 0, s>>>(n, tiles, partial, 0.0, llk, 1);
+    return launch_status("linear_reduce_kernel (whitening)");
 }
 
 extern "C" int ag_linear_llk_fp64(const ag_linear_model* lm, const double* theta, int32_t n, double norm,

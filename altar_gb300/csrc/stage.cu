@@ -9,14 +9,16 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <mutex>
+
 #include "common.cuh"
 #include "internal.h"
-#include <mutex>
 
 namespace ag {
 
 constexpr int kMaxP = 32;          // largest parameter count of the stage kernels
 constexpr int kGridPoints = 11;    // COV.cc:276 Nbeta = 10 -> 11 points per level
+constexpr int kBrentMaxIter = 128;   // Brent iterations run on the device per stage
 constexpr int kGridLevels = 11;    // COV.cc:313 Nloop <= Nbeta
 constexpr int kEvalChunk = 1024;   // chains per CTA in a COV evaluation
 constexpr int kSigmaChunk = 256;   // chains per CTA in the covariance
@@ -150,6 +152,10 @@ struct CovState {
     int level;             // levels done (Nloop)
     int done;
     int skip;              // jumped straight to β = 1
+    // Brent's method (minimisation of (COV - target)² on [low, high])
+    double a, b, x, w, v, fx, fw, fv, d, e, u;
+    int iter;
+    int phase;             // 0: evaluating the initial point, 1: iterating
 };
 
 // order-preserving map of a double onto uint64
@@ -328,6 +334,124 @@ __global__ void cov_decide_kernel(int n, int nblk, double target, double tol,
         g += step;
     }
     S->npts = kGridPoints;
+}
+
+// Brent's minimiser for δβ (COV.cc:58-219).  The reference minimises f(δβ) = (COV − target)²
+// with GSL's Brent minimiser, primed with the guess δβ = 5e-5 inside [0, 1 − β], and stops
+// when the COV at the latest evaluated point is within tol of the target (or after maxiter
+// iterations), returning the best point found.  GSL is not part of the reference, so the
+// iteration itself is Brent's published method (R. P. Brent, "Algorithms for Minimization
+// without Derivatives", 1973, ch. 5, procedure localmin: parabolic interpolation through the
+// three best points, golden-section steps when the parabola is unacceptable) restated here.
+// One call per evaluation round: the COVs of the points of the previous round come in through
+// the partial moments, the next point goes out through S->pts.
+__device__ inline double brent_metric(double cov, double target) {
+    return (cov >= 1e100) ? 1e100 : (cov - target) * (cov - target);
+}
+
+__global__ void cov_brent_kernel(int n, int nblk, double target, double tol, int maxiter,
+                                 const double* __restrict__ part, CovState* __restrict__ S) {
+    if (threadIdx.x != 0 || S->done) return;
+    double cov[2];
+    for (int pt = 0; pt < S->npts && pt < 2; ++pt) {
+        double a = 0.0, b = 0.0;
+        for (int k = 0; k < nblk; ++k) {
+            a += part[((size_t)pt * nblk + k) * 2 + 0];
+            b += part[((size_t)pt * nblk + k) * 2 + 1];
+        }
+        cov[pt] = cov_from_moments(a, b, S->pts[pt] * (S->llk_max - S->median), n);
+    }
+    const double golden = 0.3819660112501051;      // (3 − √5) / 2
+    if (S->level == 0) {
+        // full remaining step first: skip straight to β = 1 if it meets the target (COV.cc:103-116)
+        S->cov_high = cov[0];
+        if (cov[0] < target || fabs(cov[0] - target) < tol) {
+            S->done = 1;
+            S->skip = 1;
+            S->dbeta = S->high;
+            return;
+        }
+        // bracket [0, 1 − β], first point the reference's guess, interior point v = w at the
+        // golden section of the bracket; both evaluated in the next round
+        S->level = 1;
+        S->a = 0.0;
+        S->b = S->high;
+        S->x = (5.0e-5 < S->high) ? 5.0e-5 : 0.5 * S->high;
+        S->v = S->w = S->a + golden * (S->b - S->a);
+        S->d = S->e = 0.0;
+        S->iter = 0;
+        S->phase = 0;
+        S->pts[0] = S->x;
+        S->pts[1] = S->v;
+        S->npts = 2;
+        return;
+    }
+    if (S->phase == 0) {
+        S->fx = brent_metric(cov[0], target);
+        S->fv = S->fw = brent_metric(cov[1], target);
+        S->phase = 1;
+    } else {
+        // fold the new point u into the bracket and the three best points
+        const double u = S->u, fu = brent_metric(cov[0], target);
+        if (fu <= S->fx) {
+            if (u < S->x) S->b = S->x; else S->a = S->x;
+            S->v = S->w; S->fv = S->fw;
+            S->w = S->x; S->fw = S->fx;
+            S->x = u; S->fx = fu;
+        } else {
+            if (u < S->x) S->a = u; else S->b = u;
+            if (fu <= S->fw || S->w == S->x) {
+                S->v = S->w; S->fv = S->fw;
+                S->w = u; S->fw = fu;
+            } else if (fu <= S->fv || S->v == S->x || S->v == S->w) {
+                S->v = u; S->fv = fu;
+            }
+        }
+        S->iter += 1;
+        // the reference's convergence test is on the COV of the latest point (COV.cc:182)
+        if (fabs(cov[0] - target) < tol || S->iter >= maxiter) {
+            S->done = 1;
+            S->dbeta = S->x;
+            return;
+        }
+    }
+    // next point
+    const double x = S->x, a = S->a, b = S->b;
+    const double xm = 0.5 * (a + b);
+    const double tol1 = 1.4901161193847656e-08 * fabs(x) + 1e-15;   // √ε·|x| plus an absolute floor
+    const double tol2 = 2.0 * tol1;
+    if (fabs(x - xm) <= tol2 - 0.5 * (b - a)) {                     // bracket down to the tolerance
+        S->done = 1;
+        S->dbeta = x;
+        return;
+    }
+    double d = S->d, e = S->e;
+    bool parabolic = false;
+    if (fabs(e) > tol1) {
+        double r = (x - S->w) * (S->fx - S->fv);
+        double q = (x - S->v) * (S->fx - S->fw);
+        double pp = (x - S->v) * q - (x - S->w) * r;
+        q = 2.0 * (q - r);
+        if (q > 0.0) pp = -pp; else q = -q;
+        const double e_prev = e;
+        e = d;
+        if (fabs(pp) < fabs(0.5 * q * e_prev) && pp > q * (a - x) && pp < q * (b - x)) {
+            d = pp / q;
+            const double u = x + d;
+            if (u - a < tol2 || b - u < tol2) d = (xm >= x) ? tol1 : -tol1;
+            parabolic = true;
+        }
+    }
+    if (!parabolic) {
+        e = (x >= xm) ? a - x : b - x;
+        d = golden * e;
+    }
+    const double u = (fabs(d) >= tol1) ? x + d : x + ((d >= 0.0) ? tol1 : -tol1);
+    S->d = d;
+    S->e = e;
+    S->u = u;
+    S->pts[0] = u;
+    S->npts = 1;
 }
 
 // final weights at the chosen δβ: sums first, then normalise
@@ -738,6 +862,32 @@ extern "C" int ag_cov_schedule(const ag_stage_state* st, const double* data_llk,
     cov_final_state_kernel<<<1, 32, 0, s>>>(n, nblk, part, S, st->beta, st->dbeta_cov);
     cov_weights_kernel<<<blocks(n, 256), 256, 0, s>>>(data_llk, n, S, st->w);
     return launch_status("cov schedule kernels");
+}
+
+extern "C" int ag_cov_schedule_brent(const ag_stage_state* st, const double* data_llk, int32_t n,
+                                     double target, double tol, int32_t maxiter, void* workspace,
+                                     size_t workspace_bytes, void* stream) {
+    int rc = check_state(st);
+    if (rc) return rc;
+    AG_REQUIRE(n > 1 && data_llk && maxiter > 0, "invalid arguments");
+    const size_t need = ag_cov_workspace_bytes(n);
+    AG_REQUIRE(workspace && workspace_bytes >= need && aligned(workspace, 256),
+               "ag_cov_schedule_brent needs %zu bytes of 256-byte aligned workspace", need);
+    cudaStream_t s = as_stream(stream);
+    CovState* S = reinterpret_cast<CovState*>(workspace);
+    double* part = reinterpret_cast<double*>(static_cast<char*>(workspace) + cov_part_offset());
+    const int nblk = blocks(n, kEvalChunk);
+    const int iters = maxiter < kBrentMaxIter ? maxiter : kBrentMaxIter;
+    cov_median_kernel<<<1, 1024, 0, s>>>(data_llk, n, st->beta, S);
+    // round 0: the full step; round 1: the guess and the interior point; then one point per iteration
+    for (int round = 0; round < iters + 2; ++round) {
+        cov_eval_kernel<<<dim3(nblk, 2), 256, 0, s>>>(data_llk, n, S, part);
+        cov_brent_kernel<<<1, 32, 0, s>>>(n, nblk, target, tol, iters, part, S);
+    }
+    cov_final_sum_kernel<<<nblk, 256, 0, s>>>(data_llk, n, S, part);
+    cov_final_state_kernel<<<1, 32, 0, s>>>(n, nblk, part, S, st->beta, st->dbeta_cov);
+    cov_weights_kernel<<<blocks(n, 256), 256, 0, s>>>(data_llk, n, S, st->w);
+    return launch_status("cov schedule kernels (Brent)");
 }
 
 extern "C" size_t ag_sigma_workspace_bytes(int32_t n, int32_t p) {

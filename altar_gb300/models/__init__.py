@@ -4,5 +4,6 @@ from .contiguous import Contiguous
 from .cdm import CDM
 from .mogi import Mogi
 from .linear import Linear
+from .densemogi import DenseMogi
 
-__all__ = ["Bayesian", "Contiguous", "CDM", "Mogi", "Linear"]
+__all__ = ["Bayesian", "Contiguous", "CDM", "Mogi", "Linear", "DenseMogi"]

@@ -2,5 +2,6 @@
 from .job import Job
 from .rng import RNG
 from .recorder import Recorder
+from .checkpoint import Checkpoint
 
-__all__ = ["Job", "RNG", "Recorder"]
+__all__ = ["Job", "RNG", "Recorder", "Checkpoint"]

@@ -151,6 +151,16 @@ def dist_setup():
     return rank, world, local, None
 
 
+def max_over_ranks(value, dist, device="cpu"):
+    """The slowest rank's time: each replica reports its own and rank 0 prints the max."""
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_reference(args):
     # under torchrun only rank 0 measures; the CPU arm needs no process group
     if int(os.environ.get("RANK", "0")) != 0:
@@ -200,7 +210,8 @@ def anneal(kind, X, Y, los, d, N, rank, args):
     sampler = None
     if kind == "da":
         sampler = DelayedAcceptance(surrogate=Surrogate(seed=5, batch=1024), rms_limit=args.rms_limit,
-                                    epochs=args.epochs, start_beta=args.da_start_beta, inner=args.da_inner,
+                                    delta_limit=args.delta_limit, epochs=args.epochs,
+                                    start_beta=args.da_start_beta, inner=args.da_inner,
                                     outer=args.da_outer)
     model = CDM(cdm_psets(), observations=Observations(X, Y, los, d, SIGMA ** 2), autotune=not args.no_autotune)
     app = Application(model, job=Job(chains=N, steps=5), rng=RNG(1234 + rank),
@@ -223,6 +234,7 @@ def anneal(kind, X, Y, los, d, N, rank, args):
     if kind == "da":
         res["modes"] = [r.get("mode") for r in reps]
         res["rms_sigma"] = [r.get("rms_sigma") for r in reps]
+        res["delta_sd"] = [r.get("delta_sd") for r in reps]
         res["screened"] = [r.get("screened") for r in reps]
         res["refits"] = sampler.refits
         res["train_losses_last"] = sampler.surrogate.losses[-3:]
@@ -273,7 +285,9 @@ def run_ours(args):
             print(json.dumps(line))
         return 0
 
-    model = CDM(psets, observations=Observations(X, Y, los, d, SIGMA ** 2), autotune=not args.no_autotune)
+    forced = args.variant is not None
+    model = CDM(psets, observations=Observations(X, Y, los, d, SIGMA ** 2),
+                autotune=not (args.no_autotune or forced), variant=args.variant if forced else 0)
     app = Application(model, job=Job(chains=N, steps=5), rng=RNG(1234 + rank))
     app.initialize()
     ann = app.controller
@@ -311,10 +325,7 @@ def run_ours(args):
             torch.cuda.synchronize()
         ms = [a.elapsed_time(b) for a, b in evs]
         t_stage = sum(ms) / len(ms) / 1e3
-        if dist is not None:
-            tt = torch.tensor([t_stage], device="cuda")
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            t_stage = float(tt.item())
+        t_stage = max_over_ranks(t_stage, dist, device="cuda")
         value = world * N * S / t_stage
         reps = worker.reports[-args.steps:]
         step = worker.step
@@ -413,10 +424,12 @@ def main():
     ap.add_argument("--max-stages", type=int, default=400)
     ap.add_argument("--da-start-beta", type=float, default=0.0)
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--variant", type=int, default=None, help="force one CDM launch variant (no autotuning)")
     ap.add_argument("--da-inner", type=int, default=1)
     ap.add_argument("--da-outer", type=int, default=None)
     ap.add_argument("--da-variants", nargs="*", default=[], help="extra DA runs as INNERxOUTER, e.g. 5x2")
     ap.add_argument("--rms-limit", type=float, default=0.5)
+    ap.add_argument("--delta-limit", type=float, default=1.0)
     ap.add_argument("--epochs", type=int, default=40)
     ap.add_argument("--chains", type=int, default=32768)
     ap.add_argument("--cpu-chains", type=int, default=128)

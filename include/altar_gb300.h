@@ -110,7 +110,8 @@ size_t ag_forward_workspace_bytes(int model, int32_t n);
  * for diagonal Cd.
  *   mask_in:    optional; chains with a non-zero word are skipped (llk untouched)
  *   chain_status: optional; receives AG_CHAIN_* bits (CDM geometry check)
- *   residuals:  optional N x m_padded FP32 output of the residuals (tests)
+ *   residuals:  optional N x m_padded FP32 residual rows (every station
+ *               below m, whatever its weight; 0 in the padding)
  *   workspace:  ag_forward_workspace_bytes(model, n) bytes, 256-byte aligned
  */
 int ag_forward_llk(int model, const ag_layout* layout, const double* theta, int32_t n,
@@ -202,6 +203,18 @@ size_t ag_cov_workspace_bytes(int32_t n);
 int ag_cov_schedule(const ag_stage_state* st, const double* data_llk, int32_t n,
                     double target, double tol, void* workspace, size_t workspace_bytes,
                     void* stream);
+
+/*
+ * δβ by Brent's minimiser (replaces altar.ext.altar.dbeta_brent,
+ * altar/ext/dbeta.cc:39-96 → COV::dbeta_brent, COV.cc:58-219): minimises
+ * (COV − target)² over [0, 1 − β] from the guess 5e-5, stops when the COV of
+ * the latest point is within tol of the target or after maxiter iterations
+ * (at most 128 run on the device), keeps the best point.  Same outputs and
+ * workspace (ag_cov_workspace_bytes) as ag_cov_schedule.
+ */
+int ag_cov_schedule_brent(const ag_stage_state* st, const double* data_llk, int32_t n,
+                          double target, double tol, int32_t maxiter, void* workspace,
+                          size_t workspace_bytes, void* stream);
 
 /*
  * Allocation-free variant of ag_cov_schedule (no counterpart in the reference).
@@ -296,6 +309,25 @@ int ag_linear_llk(const ag_linear_model* model, const double* theta, int32_t n, 
 /* the same log-likelihood entirely in FP64 CUDA cores (reference path for checks) */
 int ag_linear_llk_fp64(const ag_linear_model* model, const double* theta, int32_t n, double norm,
                        double* llk, void* stream);
+
+/*
+ * Dense-Cd whitening of one dataset's residual block (replaces the per-chain
+ * L2.withCovariance dtrmv loop, altar/altar/norms/L2.py:39-52, for dense Cd):
+ * llk[i] -= 1/2 |W (r_i - r̄) + W r̄|² over the block's columns, with W = L⁻¹
+ * (Cd = L Lᵀ), r̄ the mean residual over the chains, W (r - r̄) on the tcgen05
+ * tensor cores (split BF16, FP32 accumulation) and W r̄ in FP64.
+ */
+typedef struct ag_whiten_block {
+    const double* w64;        /* [m][m] FP64 W = L⁻¹ */
+    const uint16_t* w_split;  /* [m][3 kpad(m)] BF16 [W_hi | W_hi | W_lo] (ag_linear_prepare) */
+    int32_t col0;             /* first column of the block in the residual rows */
+    int32_t m;                /* observations in the block */
+} ag_whiten_block;
+
+size_t ag_whiten_workspace_bytes(int32_t m, int32_t n);
+/* resid: n rows of ldr FP32 residuals (ag_forward_llk's residual output) */
+int ag_whiten_llk(const ag_whiten_block* block, const float* resid, int32_t ldr, int32_t n, double* llk,
+                  void* workspace, size_t workspace_bytes, uint32_t* flags, void* stream);
 
 /* ---------------------------------------------------------------------------
  * Learned surrogate and delayed acceptance.  No counterpart in the reference:

@@ -127,6 +127,85 @@ def dbeta_grid(llk, beta, target=1.0, tol=0.01):
     return beta + guess, guess, cov, w
 
 
+def dbeta_brent(llk, beta, target=1.0, tol=0.01, maxiter=1000):
+    """δβ by Brent's minimiser of (cov - target)² (COV.cc:58-219). Returns (new β, δβ, cov, w).
+
+    Set-up as the reference: bracket [0, 1 - β], skip to β = 1 when the full step meets the
+    target (COV.cc:103-116), first point the guess 5e-5 (COV.cc:82), interior point at the
+    golden section of the bracket, stop when the cov of the latest point is within tol
+    (COV.cc:182) or after maxiter iterations, keep the best point (COV.cc:205).  The iteration
+    is Brent's published localmin (1973, ch. 5); the reference runs GSL's version of it, which
+    is not part of the reference, so the iterates themselves are not pinned to it.
+    """
+    median = median_gsl(llk)
+    high = 1.0 - beta
+    cov, w = cov_of(high, llk, median)
+    if cov < target or abs(cov - target) < tol:
+        return 1.0, high, cov, w
+
+    def f(x):
+        c, _ = cov_of(x, llk, median)
+        return (1e100 if c >= 1e100 else (c - target) ** 2), c
+
+    golden = 0.3819660112501051
+    a, b = 0.0, high
+    x = 5.0e-5 if 5.0e-5 < high else 0.5 * high
+    v = w_ = a + golden * (b - a)
+    fx, _ = f(x)
+    fv, _ = f(v)
+    fw = fv
+    d = e = 0.0
+    it = 0
+    while True:
+        xm = 0.5 * (a + b)
+        tol1 = 1.4901161193847656e-08 * abs(x) + 1e-15
+        tol2 = 2.0 * tol1
+        if abs(x - xm) <= tol2 - 0.5 * (b - a):
+            break
+        parabolic = False
+        if abs(e) > tol1:
+            r = (x - w_) * (fx - fv)
+            q = (x - v) * (fx - fw)
+            pp = (x - v) * q - (x - w_) * r
+            q = 2.0 * (q - r)
+            if q > 0.0:
+                pp = -pp
+            else:
+                q = -q
+            e_prev, e = e, d
+            if abs(pp) < abs(0.5 * q * e_prev) and pp > q * (a - x) and pp < q * (b - x):
+                d = pp / q
+                u = x + d
+                if u - a < tol2 or b - u < tol2:
+                    d = tol1 if xm >= x else -tol1
+                parabolic = True
+        if not parabolic:
+            e = (a - x) if x >= xm else (b - x)
+            d = golden * e
+        u = x + d if abs(d) >= tol1 else x + (tol1 if d >= 0.0 else -tol1)
+        fu, cu = f(u)
+        if fu <= fx:
+            if u < x:
+                b = x
+            else:
+                a = x
+            v, fv, w_, fw, x, fx = w_, fw, x, fx, u, fu
+        else:
+            if u < x:
+                a = u
+            else:
+                b = u
+            if fu <= fw or w_ == x:
+                v, fv, w_, fw = w_, fw, u, fu
+            elif fu <= fv or v == x or v == w_:
+                v, fv = u, fu
+        it += 1
+        if abs(cu - target) < tol or it >= maxiter:
+            break
+    cov, w = cov_of(x, llk, median)
+    return beta + x, x, cov, w
+
+
 # --------------------------------------------------------------------------- covariance and resampling
 def weighted_cov(theta, w):
     """θ̄ = Σwθ/Σw; Σ = Σ w θθᵀ - θ̄θ̄ᵀ (altar/altar/bayesian/COV.py:106-156)."""
@@ -185,8 +264,9 @@ class Annealing:
     """
 
     def __init__(self, data_llk, lo, hi, chains, steps=5, seed=0, tolerance=1e-3, target=1.0,
-                 grid_tol=0.01, scaling=0.1):
+                 grid_tol=0.01, scaling=0.1, solver="grid"):
         self.data_llk, self.lo, self.hi = data_llk, np.asarray(lo, float), np.asarray(hi, float)
+        self.solver = dbeta_brent if solver == "brent" else dbeta_grid
         self.n, self.p, self.steps, self.seed = chains, self.lo.size, steps, seed
         self.tolerance, self.target, self.grid_tol, self.scaling0 = tolerance, target, grid_tol, scaling
 
@@ -208,7 +288,7 @@ class Annealing:
         post = prior + beta * data
         stages = []
         while beta + self.tolerance < 1 and len(stages) < max_stages:
-            beta, dbeta, cov, w = dbeta_grid(data, beta, self.target, self.grid_tol)
+            beta, dbeta, cov, w = self.solver(data, beta, self.target, self.grid_tol)
             sigma = weighted_cov(theta, w)
             counts = multiplicities(w, philox.resample_uniforms(self.seed, n, epoch))
             src = rank_order(counts)

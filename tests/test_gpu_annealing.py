@@ -10,11 +10,11 @@ import pytest
 import torch
 
 from altar_gb300 import Application
-from altar_gb300.bayesian import Annealer
+from altar_gb300.bayesian import COV, Annealer, Brent
 from altar_gb300.distributions import Uniform
 from altar_gb300.models import CDM, Contiguous, Mogi
 from altar_gb300.models.observations import Observations
-from altar_gb300.simulations import RNG, Job
+from altar_gb300.simulations import RNG, Checkpoint, Job
 from oracle import catmip
 
 from gpu_helpers import cdm_los_oracle, cdm_prior_rows
@@ -34,13 +34,14 @@ def mogi_problem(seed=0):
     return X, Y, los, d
 
 
-def mogi_app(chains=1024, steps=5, seed=1, graphs=True):
+def mogi_app(chains=1024, steps=5, seed=1, graphs=True, scheduler=None, checkpoint=None, resume=None):
     X, Y, los, d = mogi_problem()
     psets = {"location": Contiguous(2, Uniform((-1e4, 1e4))), "depth": Contiguous(1, Uniform((1e3, 8e3))),
              "source": Contiguous(1, Uniform((1e5, 1e7)))}
     model = Mogi(psets, observations=Observations(X, Y, los, d, 2.5e-5), log_strength=False)
     return Application(model, job=Job(chains=chains, steps=steps), rng=RNG(seed),
-                       controller=Annealer(graphs=graphs))
+                       controller=Annealer(graphs=graphs, scheduler=scheduler, checkpoint=checkpoint,
+                                           resume=resume))
 
 
 def test_mogi_posterior_matches_oracle(cuda):
@@ -66,6 +67,50 @@ def test_mogi_posterior_matches_oracle(cuda):
         mcse = sd / np.sqrt(1024 / 8)      # resampled chains are strongly correlated
         assert abs(theta[:, j].mean() - rt[:, j].mean()) < 4 * mcse, j
         assert abs(theta[:, j].std() - sd) < 0.5 * sd, j
+
+
+def test_mogi_posterior_brent_matches_oracle(cuda):
+    """The same workload with the Brent δβ solver (Brent.py) on the device and in the oracle."""
+    app = mogi_app(scheduler=COV(solver=Brent()))
+    app.run()
+    step = app.controller.worker.step
+    theta = step.theta.cpu().numpy()
+    assert step.beta == 1.0
+    X, Y, los, d = mogi_problem()
+    lo = np.array([-1e4, -1e4, 1e3, 1e5])
+    hi = np.array([1e4, 1e4, 8e3, 1e7])
+
+    def llk(th):
+        u = catmip.mogi_los(th, X, Y, los, 0.25, log_strength=False)
+        return catmip.diag_llk(u, d, np.full(X.size, 2.5e-5))[0], np.zeros(th.shape[0], bool)
+
+    ref = catmip.Annealing(llk, lo, hi, chains=1024, steps=5, seed=1, solver="brent").run()
+    rt = ref["theta"]
+    reps = app.controller.worker.reports
+    assert abs(len(reps) - len(ref["stages"])) <= max(2, len(ref["stages"]) // 5)
+    assert all(abs(r["cov"] - 1.0) < 0.01 or r["beta"] == 1.0 for r in reps)
+    for j in range(4):
+        sd = rt[:, j].std()
+        mcse = sd / np.sqrt(1024 / 8)
+        assert abs(theta[:, j].mean() - rt[:, j].mean()) < 4 * mcse, j
+        assert abs(theta[:, j].std() - sd) < 0.5 * sd, j
+
+
+def test_checkpoint_resume_repeats_the_run(cuda, tmp_path):
+    """8 stages straight and 4 + 4 with a restart from the stage-4 checkpoint give the same
+    sample bit for bit (every draw is keyed by seed, epoch and step)."""
+    def stages(app, k):
+        app.initialize()
+        app.controller.posterior(app.model, max_stages=k)
+        w = app.controller.worker
+        return w.step.theta.cpu().numpy(), w.step.beta, len(w.reports)
+
+    straight, beta_s, _ = stages(mogi_app(seed=3), 8)
+    ck = Checkpoint(str(tmp_path / "stage.npz"))
+    stages(mogi_app(seed=3, checkpoint=ck), 4)
+    resumed, beta_r, n_r = stages(mogi_app(seed=3, resume=ck.path), 4)
+    assert n_r == 4 and beta_r == beta_s
+    np.testing.assert_array_equal(resumed, straight)
 
 
 def test_graph_replay_matches_eager(cuda):

@@ -122,6 +122,40 @@ def test_cov_schedule_matches_oracle(cuda, kind):
     np.testing.assert_allclose(st.w.cpu().numpy(), w_ref, rtol=1e-10, atol=1e-300)
 
 
+@pytest.mark.parametrize("kind", ["normal", "skip", "overflow", "wide"])
+def test_cov_schedule_brent_matches_oracle(cuda, kind):
+    """Brent δβ solver: same decisions as the oracle's restatement.  The device evaluates the
+    COV from shifted weight moments and the oracle from the normalised weights, so the
+    iterates may differ in the last bits: δβ within 1e-8 relative, COV within 1e-6."""
+    rng = np.random.default_rng(5)
+    n = 5000
+    beta0 = 0.0
+    if kind == "normal":
+        llk = rng.normal(-3e4, 1e3, n)
+    elif kind == "skip":
+        llk = rng.normal(-100.0, 1e-4, n)
+        beta0 = 0.4
+    elif kind == "overflow":
+        llk = np.concatenate([rng.normal(-1e6, 1e5, n - 10), rng.normal(0.0, 1.0, 10)])
+    else:
+        llk = -np.exp(rng.uniform(0, 14, n))
+    st = _state(n, 2)
+    st.beta.fill_(beta0)
+    ws = workspace(_native.load().ag_cov_workspace_bytes(n))
+    dllk = dev(llk)
+    _native.call("ag_cov_schedule_brent", st.struct, ptr(dllk), n, 1.0, 0.01, 1000, ptr(ws), ws.numel(),
+                 stream_handle())
+    _sync()
+    b_ref, db_ref, cov_ref, w_ref = catmip.dbeta_brent(llk, beta0, 1.0, 0.01, 1000)
+    b, db, cov = st.scalars.cpu().numpy()[:3]
+    assert abs(db - db_ref) <= 1e-8 * abs(db_ref), (db, db_ref)
+    assert abs(b - b_ref) <= 1e-8 * max(abs(b_ref), 1e-300) + 1e-15, (b, b_ref)
+    assert abs(cov - cov_ref) <= 1e-6 * max(1.0, cov_ref), (cov, cov_ref)
+    if kind != "skip":
+        assert abs(cov - 1.0) < 0.01 or cov < 1.0
+    np.testing.assert_allclose(st.w.cpu().numpy(), w_ref, rtol=1e-6, atol=1e-300)
+
+
 def test_weighted_cov_and_cholesky(cuda):
     rng = np.random.default_rng(6)
     n, p = 3000, 6

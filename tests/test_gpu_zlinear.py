@@ -71,3 +71,45 @@ def test_linear_llk_tensor_cores(cuda, m, p, n):
         model.tensor_cores = True
         torch.cuda.synchronize()
         assert np.max(np.abs(out.cpu().numpy() - ref) / np.abs(ref)) < 1e-10
+
+
+def test_dense_cd_two_source_mogi(cuda):
+    """Two Mogi sources, three datasets of uneven size with dense exponential Cd."""
+    from altar_gb300.models import DenseMogi
+    from oracle import catmip
+    rng = np.random.default_rng(3)
+    sizes, loss = (300, 520, 190), ([0.38, -0.08, 0.92], [-0.6, 0.1, 0.79], [0.1, 0.55, 0.83])
+    truth = np.array([-4e3, 1e3, 3e3, 6.3, 3e3, -2e3, 4e3, 6.1])
+    datasets = []
+    for m, l in zip(sizes, loss):
+        xy = rng.uniform(-25e3, 25e3, (m, 2))
+        dist = np.sqrt(((xy[:, None, :] - xy[None, :, :]) ** 2).sum(-1))
+        cd = 1.6e-5 * np.exp(-dist / 2e3) + 1e-9 * np.eye(m)
+        u = catmip.mogi_los(truth[None, :], xy[:, 0], xy[:, 1], np.tile(l, (m, 1)), 0.25, log_strength=True,
+                            nsources=2, stride=4)[0]
+        d = u + np.linalg.cholesky(cd) @ rng.normal(size=m)
+        datasets.append(dict(x=xy[:, 0], y=xy[:, 1], los=l, d=d, cd=cd))
+    psets = {}
+    for sidx in range(2):
+        psets[f"location{sidx}"] = Contiguous(2, Uniform((-1e4, 1e4)))
+        psets[f"depth{sidx}"] = Contiguous(1, Uniform((1e3, 8e3)))
+        psets[f"source{sidx}"] = Contiguous(1, Uniform((5.0, 7.0)))
+    model = DenseMogi(psets, datasets)
+    n = 384
+    app = _App()
+    app.job.chains = n
+    model.initialize(app)
+    theta = truth[None, :] + rng.normal(size=(n, 8)) * [200, 200, 100, 0.02, 200, 200, 100, 0.02]
+    out = torch.empty(n, dtype=torch.float64, device="cuda")
+    model.forward(torch.from_numpy(theta).cuda(), out)
+    torch.cuda.synchronize()
+    assert int(model.flags.item()) == 0
+    ref = np.zeros(n)
+    for ds, m in zip(datasets, sizes):
+        u = catmip.mogi_los(theta, ds["x"], ds["y"], np.tile(ds["los"], (m, 1)), 0.25, log_strength=True,
+                            nsources=2, stride=4)
+        r = u - ds["d"][None, :]
+        sign, logdet = np.linalg.slogdet(ds["cd"])
+        ref += -0.5 * (m * math.log(2 * math.pi) + logdet) - 0.5 * np.einsum("ij,ji->i", r, np.linalg.solve(ds["cd"], r.T))
+    err = np.abs(out.cpu().numpy() - ref)
+    assert np.all(err <= 1e-4 * np.abs(ref) + 0.5), (err.max(), np.abs(ref).min())

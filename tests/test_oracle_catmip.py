@@ -57,6 +57,22 @@ def test_cov_grid_hits_target():
     assert np.all(w >= 0) and math.isclose(w.sum(), 1.0, rel_tol=1e-12)
 
 
+def test_cov_brent_skip_and_target():
+    """Brent solver (COV.cc:58-219): skip to β = 1 like the grid, otherwise a δβ whose COV is
+    within tolerance of the target, close to the grid's answer, inside [0, 1 - β]."""
+    llk = np.linspace(-1.0, -0.999, 1000)
+    b, db, cov, w = catmip.dbeta_brent(llk, 0.25)
+    assert b == 1.0 and math.isclose(db, 0.75) and cov < 1.0
+    rng = np.random.default_rng(0)
+    for llk, beta in [(rng.normal(-5e4, 2e3, 4096), 0.0), (-np.exp(rng.uniform(0, 12, 3000)), 0.3)]:
+        b, db, cov, w = catmip.dbeta_brent(llk, beta)
+        assert 0 < db < 1 - beta and math.isclose(b, beta + db)
+        assert abs(cov - 1.0) < 0.01
+        _, dbg, covg, _ = catmip.dbeta_grid(llk, beta)
+        assert abs(db - dbg) < 0.25 * dbg      # both meet the tolerance; the COV is flat near it
+        assert np.all(w >= 0) and math.isclose(w.sum(), 1.0, rel_tol=1e-12)
+
+
 def test_cov_overflow_sentinel():
     llk = np.array([0.0, 0.0, 1e6, -1e6])
     c, _ = catmip.cov_of(1.0, llk, catmip.median_gsl(llk))
