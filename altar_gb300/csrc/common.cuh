@@ -233,6 +233,12 @@ AG_DEVICE_INLINE bool mbar_wait_bounded(uint64_t* bar, uint32_t phase, uint32_t 
     return false;
 }
 
+// order this thread's earlier shared-memory accesses (generic proxy) before the
+// asynchronous copies it issues next
+AG_DEVICE_INLINE void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
 // 1-D bulk copy global -> shared (16-byte aligned, size multiple of 16),
 // completion signalled on `bar` through the transaction count.
 AG_DEVICE_INLINE void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {

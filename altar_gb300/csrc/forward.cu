@@ -16,13 +16,15 @@
 // difference as a single atan2 of the rotation from A to B), so the
 // cancellation never happens in floating point.
 //
-// Work decomposition: one warp per chain, lanes over stations; a CTA holds
-// WARPS chains whose per-side constants (precomputed in FP64 by
-// cdm_setup_kernel) live in shared memory and are read with broadcast
-// vector loads; station tiles are staged into shared memory by 1-D bulk
-// copies (cp.async.bulk + mbarrier), double buffered, and shared by the
-// CTA's warps.  Each lane accumulates w·r² in float-float; the warp's sum is
-// reduced in FP64 in a fixed order.
+// Work decomposition: cdm_setup_kernel computes each chain's per-side
+// constants in FP64 and packs the chains that have work (not masked, not
+// above the free surface) into consecutive slots; the likelihood kernel runs
+// one warp per slot, lanes over stations; a CTA holds WARPS chains whose
+// constants live in shared memory and are read with broadcast vector loads;
+// station tiles stream through a ring of shared-memory buffers filled by 1-D
+// bulk copies (cp.async.bulk + mbarrier) and shared by the CTA's warps.  Each
+// lane accumulates w·r² in float-float; the warp's sum is reduced in FP64 in
+// a fixed order.
 #include <math.h>
 #include <stdint.h>
 
@@ -176,34 +178,41 @@ __device__ bool cdm_corners(const double* th, const ag_layout& L, Vec3 V[3][4]) 
     return above;
 }
 
+// One thread per requested chain (all n, or the first *count_in of index_in).  Chains that
+// are masked or lie above the free surface get their status and nothing else; every other
+// chain takes the next compacted slot (slot order is the order of the atomic, which does not
+// affect any chain's result) and writes its constants there, so the likelihood kernel's CTAs
+// hold only chains with work.
 __global__ void cdm_setup_kernel(ag_layout L, const double* __restrict__ theta, int n,
                                  const uint32_t* __restrict__ mask_in, ChainC* __restrict__ out,
                                  uint32_t* __restrict__ chain_status, int noffsets,
-                                 const int32_t* __restrict__ index, const int32_t* __restrict__ count) {
-    const int slot = blockIdx.x * blockDim.x + threadIdx.x;
-    if (slot >= n) return;
-    ChainC& C = out[slot];
-    int i = slot;
-    if (index) {
-        if (slot >= *count) { C.side_mask = 0u; return; }
-        i = index[slot];
+                                 const int32_t* __restrict__ index_in, const int32_t* __restrict__ count_in,
+                                 int32_t* __restrict__ index_out, int32_t* __restrict__ count_out) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    int i = t;
+    if (index_in) {
+        if (t >= *count_in) return;
+        i = index_in[t];
     }
+    if (mask_in && mask_in[i]) return;
     const double* th = theta + (size_t)i * L.nparams;
+    Vec3 V[3][4];
+    const bool above = cdm_corners(th, L, V);
+    if (above) {
+        if (chain_status) chain_status[i] |= CHAIN_ABOVE_SURFACE;
+        return;
+    }
+    const int slot = atomicAdd(count_out, 1);
+    index_out[slot] = i;
+    ChainC& C = out[slot];
     C.side_mask = 0u;
     C.status = 0u;
-    if (mask_in && mask_in[i]) return;
-    Vec3 V[3][4];
-    bool above = cdm_corners(th, L, V);
     const double x0 = th[L.x_idx], y0 = th[L.x_idx + 1];
     split_hilo(x0, C.hdr.x, C.hdr.y);
     split_hilo(y0, C.hdr.z, C.hdr.w);
     for (int k = 0; k < kMaxOffsets; ++k)
         C.off[k] = (k < noffsets) ? (float)th[L.offset_idx + k] : 0.f;
-    if (above) {
-        C.status = CHAIN_ABOVE_SURFACE;
-        if (chain_status) chain_status[i] |= CHAIN_ABOVE_SURFACE;
-        return;
-    }
     // which rectangles take part (libcdm.py:226-242)
     const double ax = th[L.axes_idx], ay = th[L.axes_idx + 1], az = th[L.axes_idx + 2];
     bool use[3];
@@ -244,79 +253,31 @@ __global__ void cdm_check_kernel(ag_layout L, const double* __restrict__ theta, 
 }
 
 // ---------------------------------------------------------------------------
-// Scalar and two-station arithmetic.  side_pair is written once over a value
-// type V: float (one station per lane) or F2 (two stations per lane, every
-// add, multiply and FMA issued as one packed FP32x2 instruction, which halves
-// the issue slots of the FMA-pipe work).  Every product that feeds a sum is
-// written as an explicit FMA and the remaining adds and multiplies use the
-// non-contracting round-to-nearest forms, so both value types round every
-// operation identically and give bit-identical results.
-struct B2 { bool x, y; };
-struct F2 {
-    float2 v;
-    AG_DEVICE_INLINE F2() {}
-    AG_DEVICE_INLINE F2(float a) : v(make_float2(a, a)) {}
-    AG_DEVICE_INLINE F2(float a, float b) : v(make_float2(a, b)) {}
-    AG_DEVICE_INLINE explicit F2(float2 a) : v(a) {}
-};
-AG_DEVICE_INLINE F2 operator+(F2 a, F2 b) { return F2(__fadd2_rn(a.v, b.v)); }
-AG_DEVICE_INLINE F2 operator*(F2 a, F2 b) { return F2(__fmul2_rn(a.v, b.v)); }
-AG_DEVICE_INLINE F2 operator-(F2 a) { return F2(__fmul2_rn(a.v, make_float2(-1.0f, -1.0f))); }
-AG_DEVICE_INLINE F2 operator-(F2 a, F2 b) { return F2(__ffma2_rn(b.v, make_float2(-1.0f, -1.0f), a.v)); }
-AG_DEVICE_INLINE F2 vfma(F2 a, F2 b, F2 c) { return F2(__ffma2_rn(a.v, b.v, c.v)); }
-AG_DEVICE_INLINE F2 vadd(F2 a, F2 b) { return a + b; }
-AG_DEVICE_INLINE F2 vsub(F2 a, F2 b) { return a - b; }
-AG_DEVICE_INLINE F2 vmul(F2 a, F2 b) { return a * b; }
-AG_DEVICE_INLINE F2 vneg(F2 a) { return -a; }
+// Arithmetic of side_pair.  Every product that feeds a sum is written as an
+// explicit FMA and the remaining adds and multiplies use the non-contracting
+// round-to-nearest forms, so the rounding of each operation is fixed by the
+// source rather than by the compiler's contraction choices.  (A two-station
+// form with packed FP32x2 instructions was measured 2-4% slower on this kernel:
+// the FMA pipe throttles the packed instructions, and it was removed.)
 AG_DEVICE_INLINE float vfma(float a, float b, float c) { return fmaf(a, b, c); }
 AG_DEVICE_INLINE float vadd(float a, float b) { return __fadd_rn(a, b); }
 AG_DEVICE_INLINE float vsub(float a, float b) { return __fsub_rn(a, b); }
 AG_DEVICE_INLINE float vmul(float a, float b) { return __fmul_rn(a, b); }
 AG_DEVICE_INLINE float vneg(float a) { return -a; }
-
 AG_DEVICE_INLINE bool vge0(float a) { return a >= 0.0f; }
-AG_DEVICE_INLINE B2 vge0(F2 a) { return {a.v.x >= 0.0f, a.v.y >= 0.0f}; }
 AG_DEVICE_INLINE bool vgt0(float a) { return a > 0.0f; }
-AG_DEVICE_INLINE B2 vgt0(F2 a) { return {a.v.x > 0.0f, a.v.y > 0.0f}; }
 AG_DEVICE_INLINE bool vand(bool a, bool b) { return a && b; }
-AG_DEVICE_INLINE B2 vand(B2 a, B2 b) { return {a.x && b.x, a.y && b.y}; }
 AG_DEVICE_INLINE float vsel(bool c, float a, float b) { return c ? a : b; }
-AG_DEVICE_INLINE F2 vsel(B2 c, F2 a, F2 b) { return F2(c.x ? a.v.x : b.v.x, c.y ? a.v.y : b.v.y); }
-
 AG_DEVICE_INLINE float frcp(float x) { return fast_rcp(x); }
-AG_DEVICE_INLINE F2 frcp(F2 x) { return F2(fast_rcp(x.v.x), fast_rcp(x.v.y)); }
 AG_DEVICE_INLINE float vrsqrt(float x) { return rsqrtf(x); }
-AG_DEVICE_INLINE F2 vrsqrt(F2 x) { return F2(rsqrtf(x.v.x), rsqrtf(x.v.y)); }
 AG_DEVICE_INLINE float vlog1p(float x) { return log1p_series(x); }
-AG_DEVICE_INLINE F2 vlog1p(F2 x) { return F2(log1p_series(x.v.x), log1p_series(x.v.y)); }
 AG_DEVICE_INLINE float vatan2(float y, float x) { return atan2_poly(y, x); }
-AG_DEVICE_INLINE F2 vatan2(F2 y, F2 x) { return F2(atan2_poly(y.v.x, x.v.x), atan2_poly(y.v.y, x.v.y)); }
 
-// Per-side constants as the two value types read them.  Index = position in SideC
-// (q[i >> 2], component i & 3); a few are also needed negated.
+// Per-side constant by its position in SideC (q[i >> 2], component i & 3)
 enum : int {
     K_C = 0, K_S, K_K1, K_K2, K_DY1, K_AA, K_AB, K_DA, K_SB, K_CB, K_TB2, K_CTB2, K_DAS, K_C1F, K_C2F, K_C3F,
     K_C1P, K_C2P, K_KC1, K_KC2, K_NB1, K_NB2, K_HB1, K_HB2, K_B1, K_B2, K_C1M10, K_C3M10, K_C1Q, K_C2Q, K_C3Q,
     K_C1M11, K_C3M11, K_C1M12
-};
-// negated constants: entry k of this list sits at slot 36 + k of the pair table
-__host__ __device__ constexpr int neg_entry(int k) {
-    constexpr int list[] = {K_C,   K_K1,  K_K2,  K_CB,    K_TB2,   K_B1, K_B2, K_KC1, K_KC2,
-                            K_HB2, K_NB2, K_DY1, K_C1M10, K_C3M10, K_NB1, K_DA, K_AA};
-    return k < (int)(sizeof(list) / sizeof(int)) ? list[k] : -1;
-}
-constexpr int kNegCount = 17;
-static_assert(neg_entry(kNegCount - 1) >= 0 && neg_entry(kNegCount) < 0, "negated-constant count");
-constexpr int kPairSlots = (36 + kNegCount + 1) & ~1;   // even: whole float4 pairs of pairs
-__host__ __device__ constexpr int neg_slot(int i) {
-    int k = 0;
-    while (k < kNegCount && neg_entry(k) != i) ++k;
-    return 36 + k;
-}
-
-// one side's constants duplicated into (v, v) pairs, plain then negated (two-station kernels)
-struct __align__(16) SideP {
-    float2 v[kPairSlots];
 };
 
 struct ScalarSide {
@@ -333,27 +294,6 @@ struct ScalarSide {
     template <int I>
     AG_DEVICE_INLINE float neg() const { return -at<I>(); }
 };
-
-struct PairSide {
-    const SideP& P;
-    AG_DEVICE_INLINE explicit PairSide(const SideP& p) : P(p) {}
-    template <int I>
-    AG_DEVICE_INLINE F2 at() const { return F2(P.v[I]); }
-    template <int I>
-    AG_DEVICE_INLINE F2 neg() const {
-        static_assert(neg_slot(I) < 36 + kNegCount, "constant missing from the negated table");
-        return F2(P.v[neg_slot(I)]);
-    }
-};
-
-AG_DEVICE_INLINE void expand_side(const SideC& S, SideP& P) {
-    const float* f = reinterpret_cast<const float*>(S.q);
-#pragma unroll
-    for (int i = 0; i < 36; ++i) P.v[i] = make_float2(f[i], f[i]);
-#pragma unroll
-    for (int k = 0; k < kNegCount; ++k) P.v[36 + k] = make_float2(-f[neg_entry(k)], -f[neg_entry(k)]);
-    P.v[kPairSlots - 1] = make_float2(0.f, 0.f);
-}
 
 #define KC(i) k.template at<i>()
 #define KN(i) k.template neg<i>()
@@ -475,77 +415,97 @@ AG_DEVICE_INLINE void side_pair(const K& k, V Xr, V Yr, V& ue, V& un, V& uv) {
 #undef KN
 
 // ---------------------------------------------------------------------------
-template <int WARPS, int MINB, bool PAIRED>
+// CDM likelihood.  One warp per compacted chain slot, lanes over stations.
+// Station tiles stream through a ring of kStages shared-memory buffers filled
+// by 1-D bulk copies: each warp waits on the buffer's full barrier, works
+// through the tile and counts itself done; the warp that finishes a tile last
+// refills that buffer with the tile kStages ahead.  No CTA-wide barrier is
+// taken per tile, so warps drift apart by up to kStages - 1 tiles instead of
+// waiting for the slowest one at every tile.
+constexpr int kStages = 4;
+
+template <int WARPS, int MINB>
 __global__ void __launch_bounds__(WARPS * 32, MINB)
-cdm_llk_kernel(const ChainC* __restrict__ chains, int n, const float4* __restrict__ xy,
+cdm_llk_kernel(const ChainC* __restrict__ chains, const int32_t* __restrict__ slot_chain,
+               const int32_t* __restrict__ nslots_ptr, int n, const float4* __restrict__ xy,
                const float4* __restrict__ losd, const float* __restrict__ wt,
                const int32_t* __restrict__ oid, int m, int m_padded, double norm,
-               double* __restrict__ llk, float* __restrict__ resid, uint32_t* __restrict__ flags,
-               const int32_t* __restrict__ index, const int32_t* __restrict__ count) {
-    // with an index list, slots beyond the device-side count have nothing to do
-    if (index && (int)(blockIdx.x * WARPS) >= *count) return;
+               double* __restrict__ llk, float* __restrict__ resid, uint32_t* __restrict__ flags) {
+    const int nslots = min(n, *nslots_ptr);
+    if ((int)(blockIdx.x * WARPS) >= nslots) return;       // whole CTA past the active chains
     __shared__ ChainC s_chain[WARPS];
-    __shared__ SideP s_pair[PAIRED ? WARPS : 1][PAIRED ? kSides : 1];
-    __shared__ float4 s_xy[2][kTile];
-    __shared__ float4 s_ld[2][kTile];
-    __shared__ __align__(16) float s_w[2][kTile];
-    __shared__ __align__(16) int32_t s_oid[2][kTile];
-    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ float4 s_xy[kStages][kTile];
+    __shared__ float4 s_ld[kStages][kTile];
+    __shared__ __align__(16) float s_w[kStages][kTile];
+    __shared__ __align__(16) int32_t s_oid[kStages][kTile];
+    __shared__ __align__(8) uint64_t full[kStages];
+    __shared__ int s_done[kStages];
+    __shared__ int s_issued;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int slot = blockIdx.x * WARPS + warp;
-    const int nslots = index ? min(n, *count) : n;
-    const int chain = (slot < nslots) ? (index ? index[slot] : slot) : n;
+    const bool active = slot < nslots;
+    const int chain = active ? slot_chain[slot] : n;
     const int ntiles = m_padded / kTile;
     const bool with_oid = (oid != nullptr);
     const uint32_t tile_bytes = kTile * (16u + 16u + 4u) + (with_oid ? kTile * 4u : 0u);
 
     // this warp's chain constants
-    {
-        const float4* src = reinterpret_cast<const float4*>(chains + (slot < nslots ? slot : 0));
+    if (active) {
+        const float4* src = reinterpret_cast<const float4*>(chains + slot);
         float4* dst = reinterpret_cast<float4*>(&s_chain[warp]);
         constexpr int nvec = sizeof(ChainC) / 16;
         for (int k = lane; k < nvec; k += 32) dst[k] = src[k];
     }
-    if (threadIdx.x == 0) {
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
-        fence_mbar_init();
-    }
-    __syncthreads();
-    if constexpr (PAIRED) {
-        // each warp duplicates its own chain's side constants into (v, v) pairs
-        if (lane < kSides) expand_side(s_chain[warp].side[lane], s_pair[warp][lane]);
-        __syncwarp();
-    }
     auto issue = [&](int t, int buf) {
         const size_t base = (size_t)t * kTile;
-        mbar_arrive_expect_tx(&bar[buf], tile_bytes);
-        bulk_g2s(&s_xy[buf][0], xy + base, kTile * 16u, &bar[buf]);
-        bulk_g2s(&s_ld[buf][0], losd + base, kTile * 16u, &bar[buf]);
-        bulk_g2s(&s_w[buf][0], wt + base, kTile * 4u, &bar[buf]);
-        if (with_oid) bulk_g2s(&s_oid[buf][0], oid + base, kTile * 4u, &bar[buf]);
+        mbar_arrive_expect_tx(&full[buf], tile_bytes);
+        bulk_g2s(&s_xy[buf][0], xy + base, kTile * 16u, &full[buf]);
+        bulk_g2s(&s_ld[buf][0], losd + base, kTile * 16u, &full[buf]);
+        bulk_g2s(&s_w[buf][0], wt + base, kTile * 4u, &full[buf]);
+        if (with_oid) bulk_g2s(&s_oid[buf][0], oid + base, kTile * 4u, &full[buf]);
     };
     if (threadIdx.x == 0) {
-        issue(0, 0);
-        if (ntiles > 1) issue(1, 1);
+        for (int b = 0; b < kStages; ++b) {
+            mbar_init(&full[b], 1);
+            s_done[b] = 0;
+        }
+        fence_mbar_init();
+        const int first = ntiles < kStages ? ntiles : kStages;
+        for (int t = 0; t < first; ++t) issue(t, t);
+        s_issued = first;
     }
+    __syncthreads();
     const ChainC& C = s_chain[warp];
-    const uint32_t smask = (chain < n) ? C.side_mask : 0u;
-    const bool active = smask != 0u;
+    const uint32_t smask = active ? C.side_mask : 0u;
     const float x0h = C.hdr.x, x0l = C.hdr.y, y0h = C.hdr.z, y0l = C.hdr.w;
     ff acc{0.f, 0.f};
-    int failed_at = -1;
-    int issued = (ntiles > 1) ? 2 : 1;
+    bool failed = false;
     for (int t = 0; t < ntiles; ++t) {
-        const int buf = t & 1;
-        const uint32_t phase = (t >> 1) & 1;
-        const bool ok = mbar_wait_bounded(&bar[buf], phase, kWaitLimit);
-        if (__syncthreads_or(!ok)) { failed_at = t; break; }
-        if (active) {
-            // u projected on the LOS, minus data and offset; accumulate w r² and store r
-            auto finish = [&](float e_, float n_, float v_, const float4& B, float w, int j) {
-                const float u = fmaf(e_, B.x, fmaf(n_, B.y, v_ * B.z));
+        const int buf = t % kStages;
+        const uint32_t phase = (uint32_t)(t / kStages) & 1u;
+        const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(&full[buf], phase, kWaitLimit));
+        if (!ok) {
+            failed = true;
+            break;
+        }
+        if (smask) {
+            for (int j = lane; j < kTile; j += 32) {
+                const float4 A = s_xy[buf][j];
+                const float Xr = (A.x - x0h) + (A.y - x0l);
+                const float Yr = (A.z - y0h) + (A.w - y0l);
+                float ue = 0.f, un = 0.f, uv = 0.f;
+                uint32_t msk = smask & 0x0FFFu;
+#pragma unroll 1
+                while (msk) {
+                    const int sidx = __ffs(msk) - 1;
+                    msk &= msk - 1;
+                    side_pair<float>(ScalarSide(C.side[sidx]), Xr, Yr, ue, un, uv);
+                }
+                // u projected on the LOS, minus data and offset; accumulate w r² and store r
+                const float4 B = s_ld[buf][j];
+                const float w = s_w[buf][j];
+                const float u = fmaf(ue, B.x, fmaf(un, B.y, uv * B.z));
                 float r = u - B.w;
                 if (with_oid) r -= C.off[s_oid[buf][j] & (kMaxOffsets - 1)];
                 if (w != 0.f) ff_add_wsq(acc, r, w);
@@ -553,53 +513,30 @@ cdm_llk_kernel(const ChainC* __restrict__ chains, int n, const float4* __restric
                     const int col = t * kTile + j;
                     resid[(size_t)chain * m_padded + col] = (col < m) ? r : 0.f;
                 }
-            };
-            if constexpr (PAIRED) {
-                // stations j and j + 32 together; accumulation order as in the scalar loop
-                for (int j = lane; j < kTile; j += 64) {
-                    const float4 A0 = s_xy[buf][j], A1 = s_xy[buf][j + 32];
-                    const F2 Xr = (F2(A0.x, A1.x) - F2(x0h)) + (F2(A0.y, A1.y) - F2(x0l));
-                    const F2 Yr = (F2(A0.z, A1.z) - F2(y0h)) + (F2(A0.w, A1.w) - F2(y0l));
-                    F2 ue(0.f), un(0.f), uv(0.f);
-                    uint32_t msk = smask & 0x0FFFu;
-#pragma unroll 1
-                    while (msk) {
-                        const int sidx = __ffs(msk) - 1;
-                        msk &= msk - 1;
-                        side_pair<F2>(PairSide(s_pair[warp][sidx]), Xr, Yr, ue, un, uv);
-                    }
-                    finish(ue.v.x, un.v.x, uv.v.x, s_ld[buf][j], s_w[buf][j], j);
-                    finish(ue.v.y, un.v.y, uv.v.y, s_ld[buf][j + 32], s_w[buf][j + 32], j + 32);
-                }
-            } else {
-                for (int j = lane; j < kTile; j += 32) {
-                    const float4 A = s_xy[buf][j];
-                    const float Xr = (A.x - x0h) + (A.y - x0l);
-                    const float Yr = (A.z - y0h) + (A.w - y0l);
-                    float ue = 0.f, un = 0.f, uv = 0.f;
-                    uint32_t msk = smask & 0x0FFFu;
-#pragma unroll 1
-                    while (msk) {
-                        const int sidx = __ffs(msk) - 1;
-                        msk &= msk - 1;
-                        side_pair<float>(ScalarSide(C.side[sidx]), Xr, Yr, ue, un, uv);
-                    }
-                    finish(ue, un, uv, s_ld[buf][j], s_w[buf][j], j);
+            }
+        }
+        // done with this buffer: the last warp of the CTA to get here refills it
+        __syncwarp();
+        if (lane == 0) {
+            __threadfence_block();
+            if (atomicAdd(&s_done[buf], 1) == WARPS - 1) {
+                __threadfence_block();
+                s_done[buf] = 0;
+                if (t + kStages < ntiles) {
+                    fence_proxy_async_smem();
+                    issue(t + kStages, buf);
+                    atomicAdd(&s_issued, 1);
                 }
             }
         }
-        __syncthreads();
-        if (threadIdx.x == 0 && t + 2 < ntiles) {
-            issue(t + 2, buf);
-            ++issued;
-        }
     }
-    if (failed_at >= 0) {
-        // drain the copies still in flight (bounded) before the CTA exits
+    if (__syncthreads_or(failed)) {
+        // a wait gave up: drain the copies still in flight (bounded) before the CTA exits
         if (threadIdx.x == 0) {
             raise_flag(flags, DEV_ERR_TIMEOUT);
-            for (int t = failed_at; t < issued; ++t)
-                mbar_wait_bounded(&bar[t & 1], (t >> 1) & 1, kWaitLimit);
+            const int last = s_issued;
+            for (int t = (last > kStages ? last - kStages : 0); t < last; ++t)
+                mbar_wait_bounded(&full[t % kStages], (uint32_t)(t / kStages) & 1u, kWaitLimit);
         }
         return;
     }
@@ -712,14 +649,18 @@ using namespace ag;
 // CDM launch variants: warps (= chains) per CTA and resident CTAs per SM the
 // register allocation targets; chosen per problem by the autotuner
 struct CdmVariant { int warps; };
-static constexpr CdmVariant kCdmVariants[] = {{8}, {4}, {4}, {16}, {4}, {4}, {4}};
-static constexpr int kCdmVariantCount = 7;
+static constexpr CdmVariant kCdmVariants[] = {{8}, {4}, {4}, {2}};
+static constexpr int kCdmVariantCount = 4;
 static constexpr int kMogiChains = 16;
 
 extern "C" int32_t ag_forward_variants(int model) { return model == AG_MODEL_CDM ? kCdmVariantCount : 1; }
 
+// CDM workspace: compacted chain constants, the chain of each slot, the slot count
+static size_t al256(size_t b) { return (b + 255) / 256 * 256; }
+
 extern "C" size_t ag_forward_workspace_bytes(int model, int32_t n) {
-    if (model == AG_MODEL_CDM && n > 0) return (size_t)n * sizeof(ChainC);
+    if (model == AG_MODEL_CDM && n > 0)
+        return al256((size_t)n * sizeof(ChainC)) + al256((size_t)n * sizeof(int32_t)) + 256;
     return 0;
 }
 
@@ -766,49 +707,30 @@ static int forward_llk(int model, const ag_layout* layout, const double* theta, 
         AG_REQUIRE(workspace != nullptr && workspace_bytes >= need && aligned(workspace, 256),
                    "CDM needs %zu bytes of 256-byte aligned workspace", need);
         ChainC* chains = reinterpret_cast<ChainC*>(workspace);
-        cdm_setup_kernel<<<(n + 127) / 128, 128, 0, s>>>(L, theta, n, mask_in, chains, chain_status,
-                                                         noffsets, index, count);
+        int32_t* slot_chain = reinterpret_cast<int32_t*>(static_cast<char*>(workspace) +
+                                                         al256((size_t)n * sizeof(ChainC)));
+        int32_t* nslots = reinterpret_cast<int32_t*>(reinterpret_cast<char*>(slot_chain) +
+                                                     al256((size_t)n * sizeof(int32_t)));
+        rc = cuda_status(cudaMemsetAsync(nslots, 0, sizeof(int32_t), s), "cudaMemsetAsync(slot count)");
+        if (rc) return rc;
+        cdm_setup_kernel<<<(n + 127) / 128, 128, 0, s>>>(L, theta, n, mask_in, chains, chain_status, noffsets,
+                                                         index, count, slot_chain, nslots);
         rc = launch_status("cdm_setup_kernel");
         if (rc) return rc;
         const int v = L.variant;
         AG_REQUIRE(v >= 0 && v < kCdmVariantCount, "CDM variant %d out of range [0, %d)", v, kCdmVariantCount);
         const int warps = kCdmVariants[v].warps;
         const int grid = (n + warps - 1) / warps;
-        const float4* ld_ = ld;
+#define AG_CDM_LAUNCH(W, B)                                                                                  \
+    cdm_llk_kernel<W, B><<<grid, W * 32, 0, s>>>(chains, slot_chain, nslots, n, xy, ld, st->weight, st->oid, \
+                                                 st->m, st->m_padded, norm, llk, residuals, nullptr)
         switch (v) {
-            case 0:
-                cdm_llk_kernel<8, 2, false><<<grid, 8 * 32, 0, s>>>(chains, n, xy, ld_, st->weight, st->oid, st->m, st->m_padded,
-                                                             norm, llk, residuals, nullptr, index, count);
-                break;
-            case 1:
-                cdm_llk_kernel<4, 4, false><<<grid, 4 * 32, 0, s>>>(chains, n, xy, ld_, st->weight, st->oid, st->m, st->m_padded,
-                                                             norm, llk, residuals, nullptr, index, count);
-                break;
-            case 2:
-                cdm_llk_kernel<4, 5, false><<<grid, 4 * 32, 0, s>>>(chains, n, xy, ld_, st->weight, st->oid, st->m, st->m_padded,
-                                                             norm, llk, residuals, nullptr, index, count);
-                break;
-            case 4:
-                cdm_llk_kernel<4, 5, true><<<grid, 4 * 32, 0, s>>>(chains, n, xy, ld_, st->weight, st->oid, st->m,
-                                                                  st->m_padded, norm, llk, residuals, nullptr, index,
-                                                                  count);
-                break;
-            case 5:
-                cdm_llk_kernel<4, 3, true><<<grid, 4 * 32, 0, s>>>(chains, n, xy, ld_, st->weight, st->oid, st->m,
-                                                                  st->m_padded, norm, llk, residuals, nullptr, index,
-                                                                  count);
-                break;
-            case 6:
-                cdm_llk_kernel<4, 4, true><<<grid, 4 * 32, 0, s>>>(chains, n, xy, ld_, st->weight, st->oid, st->m,
-                                                                  st->m_padded, norm, llk, residuals, nullptr, index,
-                                                                  count);
-                break;
-            default:
-                cdm_llk_kernel<16, 1, false><<<grid, 16 * 32, 0, s>>>(chains, n, xy, ld_, st->weight, st->oid,
-                                                               st->m, st->m_padded, norm, llk, residuals, nullptr, index,
-                                                               count);
-                break;
+            case 0: AG_CDM_LAUNCH(8, 2); break;
+            case 1: AG_CDM_LAUNCH(4, 4); break;
+            case 2: AG_CDM_LAUNCH(4, 5); break;
+            default: AG_CDM_LAUNCH(2, 8); break;
         }
+#undef AG_CDM_LAUNCH
         return launch_status("cdm_llk_kernel");
     }
     if (model == AG_MODEL_MOGI) {
