@@ -231,6 +231,16 @@ class DelayedAcceptance(Metropolis):
         self._sbufs = None
         self._chain = None
 
+    def initialize(self, application):
+        super().initialize(application)
+        # load the dense linear-algebra libraries the refits use (QR, symmetric eigensolver)
+        # now, so that their one-time start-up does not land inside the first refit
+        a = torch.eye(8, dtype=torch.float64, device=DEVICE)
+        torch.linalg.qr(a.float())
+        torch.linalg.eigh(a)
+        torch.cuda.synchronize()
+        return self
+
     def mode_key(self):
         return self.mode
 
@@ -262,16 +272,15 @@ class DelayedAcceptance(Metropolis):
             if self._usable():
                 self.mode = "da"
                 return self
-            # after a fit that failed its own check, wait before fitting again (doubling the wait)
-            if self._backoff and self._stage - self._last_try < self.retry_every * (1 << (self._backoff - 1)):
+            # after a fit that failed its own check, wait retry_every stages before fitting again
+            if self._backoff and self._stage - self._last_try < self.retry_every:
                 self.mode = "plain"
                 return self
         self._last_try = self._stage
         self._refit(annealer, step, fit_rows)
         self.rms = self._check(annealer, step, chk_rows)
         self.delta = self._delta_check(annealer, step, chk_rows)
-        # a fresh fit that still fails waits longer before the next attempt
-        self._backoff = 0 if self._usable() else min(self._backoff + 1, 4)
+        self._backoff = 0 if self._usable() else 1
         self.mode = "da" if self._usable() else "plain"
         return self
 

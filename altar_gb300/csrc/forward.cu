@@ -273,6 +273,46 @@ AG_DEVICE_INLINE float vrsqrt(float x) { return rsqrtf(x); }
 AG_DEVICE_INLINE float vlog1p(float x) { return log1p_series(x); }
 AG_DEVICE_INLINE float vatan2(float y, float x) { return atan2_poly(y, x); }
 
+// Several stations per lane as a group of scalars: every operation is the scalar one
+// on each element, so results are identical to the one-station form, while the
+// independent chains of dependent instructions interleave (instruction-level
+// parallelism for the MUFU and FMA latencies) and each side constant is loaded from
+// shared memory once for the whole group.
+template <int N>
+struct SV {
+    float v[N];
+    AG_DEVICE_INLINE SV() {}
+    AG_DEVICE_INLINE SV(float x) {
+#pragma unroll
+        for (int i = 0; i < N; ++i) v[i] = x;
+    }
+};
+template <int N>
+struct CV { bool v[N]; };
+#define AG_SV_MAP(expr)                  \
+    SV<N> r;                             \
+    _Pragma("unroll") for (int i = 0; i < N; ++i) r.v[i] = (expr); \
+    return r
+#define AG_CV_MAP(expr)                  \
+    CV<N> r;                             \
+    _Pragma("unroll") for (int i = 0; i < N; ++i) r.v[i] = (expr); \
+    return r
+template <int N> AG_DEVICE_INLINE SV<N> vfma(SV<N> x, SV<N> y, SV<N> z) { AG_SV_MAP(fmaf(x.v[i], y.v[i], z.v[i])); }
+template <int N> AG_DEVICE_INLINE SV<N> vadd(SV<N> x, SV<N> y) { AG_SV_MAP(__fadd_rn(x.v[i], y.v[i])); }
+template <int N> AG_DEVICE_INLINE SV<N> vsub(SV<N> x, SV<N> y) { AG_SV_MAP(__fsub_rn(x.v[i], y.v[i])); }
+template <int N> AG_DEVICE_INLINE SV<N> vmul(SV<N> x, SV<N> y) { AG_SV_MAP(__fmul_rn(x.v[i], y.v[i])); }
+template <int N> AG_DEVICE_INLINE SV<N> vneg(SV<N> x) { AG_SV_MAP(-x.v[i]); }
+template <int N> AG_DEVICE_INLINE CV<N> vge0(SV<N> x) { AG_CV_MAP(x.v[i] >= 0.0f); }
+template <int N> AG_DEVICE_INLINE CV<N> vgt0(SV<N> x) { AG_CV_MAP(x.v[i] > 0.0f); }
+template <int N> AG_DEVICE_INLINE CV<N> vand(CV<N> x, CV<N> y) { AG_CV_MAP(x.v[i] && y.v[i]); }
+template <int N> AG_DEVICE_INLINE SV<N> vsel(CV<N> c, SV<N> x, SV<N> y) { AG_SV_MAP(c.v[i] ? x.v[i] : y.v[i]); }
+template <int N> AG_DEVICE_INLINE SV<N> frcp(SV<N> x) { AG_SV_MAP(fast_rcp(x.v[i])); }
+template <int N> AG_DEVICE_INLINE SV<N> vrsqrt(SV<N> x) { AG_SV_MAP(rsqrtf(x.v[i])); }
+template <int N> AG_DEVICE_INLINE SV<N> vlog1p(SV<N> x) { AG_SV_MAP(log1p_series(x.v[i])); }
+template <int N> AG_DEVICE_INLINE SV<N> vatan2(SV<N> y, SV<N> x) { AG_SV_MAP(atan2_poly(y.v[i], x.v[i])); }
+#undef AG_SV_MAP
+#undef AG_CV_MAP
+
 // Per-side constant by its position in SideC (q[i >> 2], component i & 3)
 enum : int {
     K_C = 0, K_S, K_K1, K_K2, K_DY1, K_AA, K_AB, K_DA, K_SB, K_CB, K_TB2, K_CTB2, K_DAS, K_C1F, K_C2F, K_C3F,
@@ -295,8 +335,8 @@ struct ScalarSide {
     AG_DEVICE_INLINE float neg() const { return -at<I>(); }
 };
 
-#define KC(i) k.template at<i>()
-#define KN(i) k.template neg<i>()
+#define KC(i) V(k.template at<i>())
+#define KN(i) V(k.template neg<i>())
 
 // ---------------------------------------------------------------------------
 // one angular-dislocation pair in difference arithmetic
@@ -424,7 +464,7 @@ AG_DEVICE_INLINE void side_pair(const K& k, V Xr, V Yr, V& ue, V& un, V& uv) {
 // waiting for the slowest one at every tile.
 constexpr int kStages = 4;
 
-template <int WARPS, int MINB>
+template <int WARPS, int MINB, int SPL>
 __global__ void __launch_bounds__(WARPS * 32, MINB)
 cdm_llk_kernel(const ChainC* __restrict__ chains, const int32_t* __restrict__ slot_chain,
                const int32_t* __restrict__ nslots_ptr, int n, const float4* __restrict__ xy,
@@ -490,28 +530,54 @@ cdm_llk_kernel(const ChainC* __restrict__ chains, const int32_t* __restrict__ sl
             break;
         }
         if (smask) {
-            for (int j = lane; j < kTile; j += 32) {
-                const float4 A = s_xy[buf][j];
-                const float Xr = (A.x - x0h) + (A.y - x0l);
-                const float Yr = (A.z - y0h) + (A.w - y0l);
-                float ue = 0.f, un = 0.f, uv = 0.f;
-                uint32_t msk = smask & 0x0FFFu;
-#pragma unroll 1
-                while (msk) {
-                    const int sidx = __ffs(msk) - 1;
-                    msk &= msk - 1;
-                    side_pair<float>(ScalarSide(C.side[sidx]), Xr, Yr, ue, un, uv);
-                }
-                // u projected on the LOS, minus data and offset; accumulate w r² and store r
+            // u projected on the LOS, minus data and offset; accumulate w r² and store r
+            auto finish = [&](float e_, float n_, float v_, int j) {
                 const float4 B = s_ld[buf][j];
                 const float w = s_w[buf][j];
-                const float u = fmaf(ue, B.x, fmaf(un, B.y, uv * B.z));
+                const float u = fmaf(e_, B.x, fmaf(n_, B.y, v_ * B.z));
                 float r = u - B.w;
                 if (with_oid) r -= C.off[s_oid[buf][j] & (kMaxOffsets - 1)];
                 if (w != 0.f) ff_add_wsq(acc, r, w);
                 if (resid) {
                     const int col = t * kTile + j;
                     resid[(size_t)chain * m_padded + col] = (col < m) ? r : 0.f;
+                }
+            };
+            if constexpr (SPL > 1) {
+                // stations j, j + 32, ... together; accumulation order as in the one-station loop
+                for (int j0 = lane; j0 < kTile; j0 += 32 * SPL) {
+                    SV<SPL> Xr, Yr;
+#pragma unroll
+                    for (int q = 0; q < SPL; ++q) {
+                        const float4 A = s_xy[buf][j0 + 32 * q];
+                        Xr.v[q] = (A.x - x0h) + (A.y - x0l);
+                        Yr.v[q] = (A.z - y0h) + (A.w - y0l);
+                    }
+                    SV<SPL> ue(0.f), un(0.f), uv(0.f);
+                    uint32_t msk = smask & 0x0FFFu;
+#pragma unroll 1
+                    while (msk) {
+                        const int sidx = __ffs(msk) - 1;
+                        msk &= msk - 1;
+                        side_pair<SV<SPL>>(ScalarSide(C.side[sidx]), Xr, Yr, ue, un, uv);
+                    }
+#pragma unroll
+                    for (int q = 0; q < SPL; ++q) finish(ue.v[q], un.v[q], uv.v[q], j0 + 32 * q);
+                }
+            } else {
+                for (int j = lane; j < kTile; j += 32) {
+                    const float4 A = s_xy[buf][j];
+                    const float Xr = (A.x - x0h) + (A.y - x0l);
+                    const float Yr = (A.z - y0h) + (A.w - y0l);
+                    float ue = 0.f, un = 0.f, uv = 0.f;
+                    uint32_t msk = smask & 0x0FFFu;
+#pragma unroll 1
+                    while (msk) {
+                        const int sidx = __ffs(msk) - 1;
+                        msk &= msk - 1;
+                        side_pair<float>(ScalarSide(C.side[sidx]), Xr, Yr, ue, un, uv);
+                    }
+                    finish(ue, un, uv, j);
                 }
             }
         }
@@ -649,8 +715,8 @@ using namespace ag;
 // CDM launch variants: warps (= chains) per CTA and resident CTAs per SM the
 // register allocation targets; chosen per problem by the autotuner
 struct CdmVariant { int warps; };
-static constexpr CdmVariant kCdmVariants[] = {{8}, {4}, {4}, {2}};
-static constexpr int kCdmVariantCount = 4;
+static constexpr CdmVariant kCdmVariants[] = {{8}, {4}, {4}, {2}, {4}, {4}, {2}, {4}, {4}};
+static constexpr int kCdmVariantCount = 9;
 static constexpr int kMogiChains = 16;
 
 extern "C" int32_t ag_forward_variants(int model) { return model == AG_MODEL_CDM ? kCdmVariantCount : 1; }
@@ -721,14 +787,19 @@ static int forward_llk(int model, const ag_layout* layout, const double* theta, 
         AG_REQUIRE(v >= 0 && v < kCdmVariantCount, "CDM variant %d out of range [0, %d)", v, kCdmVariantCount);
         const int warps = kCdmVariants[v].warps;
         const int grid = (n + warps - 1) / warps;
-#define AG_CDM_LAUNCH(W, B)                                                                                  \
-    cdm_llk_kernel<W, B><<<grid, W * 32, 0, s>>>(chains, slot_chain, nslots, n, xy, ld, st->weight, st->oid, \
-                                                 st->m, st->m_padded, norm, llk, residuals, nullptr)
+#define AG_CDM_LAUNCH(W, B, SPL)                                                                    \
+    cdm_llk_kernel<W, B, SPL><<<grid, W * 32, 0, s>>>(chains, slot_chain, nslots, n, xy, ld, st->weight, \
+                                                      st->oid, st->m, st->m_padded, norm, llk, residuals, nullptr)
         switch (v) {
-            case 0: AG_CDM_LAUNCH(8, 2); break;
-            case 1: AG_CDM_LAUNCH(4, 4); break;
-            case 2: AG_CDM_LAUNCH(4, 5); break;
-            default: AG_CDM_LAUNCH(2, 8); break;
+            case 0: AG_CDM_LAUNCH(8, 2, 1); break;
+            case 1: AG_CDM_LAUNCH(4, 4, 1); break;
+            case 2: AG_CDM_LAUNCH(4, 5, 1); break;
+            case 3: AG_CDM_LAUNCH(2, 8, 1); break;
+            case 4: AG_CDM_LAUNCH(4, 3, 2); break;
+            case 5: AG_CDM_LAUNCH(4, 4, 2); break;
+            case 6: AG_CDM_LAUNCH(2, 6, 2); break;
+            case 7: AG_CDM_LAUNCH(4, 2, 4); break;
+            default: AG_CDM_LAUNCH(4, 3, 4); break;
         }
 #undef AG_CDM_LAUNCH
         return launch_status("cdm_llk_kernel");

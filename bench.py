@@ -243,6 +243,95 @@ def anneal(kind, X, Y, los, d, N, rank, args):
     return res
 
 
+def run_linear(args):
+    """Linear-Gaussian workload on the tcgen05 kernel: M = 4,096 observations, P = 256
+    parameters, N = 16,384 chains, dense exponential Cd (d = Gθ + Lξ).  Times one data
+    log-likelihood evaluation of all chains (ag_linear_llk: θ centring and BF16 split,
+    FP64 residual correction, tensor-core GEMM with the fused misfit, reduction) and
+    the whole annealing run to β = 1."""
+    import math
+    import torch
+    from altar_gb300 import Application
+    from altar_gb300.bayesian import Annealer
+    from altar_gb300.distributions import Uniform
+    from altar_gb300.models import Contiguous, Linear
+    from altar_gb300.simulations import RNG, Job
+    rank, world, local, dist = dist_setup()
+    torch.cuda.set_device(local)
+    M, P, N = 4096, 256, args.chains if args.chains != 32768 else 16384
+    rng = np.random.default_rng(7)
+    G = rng.normal(size=(M, P))
+    truth = rng.uniform(-1, 1, P)
+    xy = rng.uniform(0, 50e3, (M, 2))
+    dist_m = np.sqrt(((xy[:, None, :] - xy[None, :, :]) ** 2).sum(-1))
+    Cd = 1e-4 * np.exp(-dist_m / 2e3)
+    d = G @ truth + np.linalg.cholesky(Cd) @ rng.normal(size=M)
+    model = Linear({"theta": Contiguous(P, Uniform((-1, 1)))}, green=G, data=d, cd=Cd)
+    app = Application(model, job=Job(chains=N, steps=5), rng=RNG(99 + rank))
+    app.initialize()
+    theta = torch.from_numpy(rng.uniform(-1, 1, (N, P))).cuda()
+    out = torch.empty(N, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    for _ in range(max(3, args.warmup)):
+        model.forward(theta, out)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(local) as clk:
+        for a, b in evs:
+            flush.zero_()
+            a.record(stream)
+            model.forward(theta, out)
+            b.record(stream)
+        torch.cuda.synchronize()
+    t = sum(a.elapsed_time(b) for a, b in evs) / len(evs) / 1e3
+    t = max_over_ranks(t, dist, device="cuda")
+    assert int(model.flags.item()) == 0, "device wait timed out"
+    kp = (P + 63) // 64 * 64
+    alg = 2.0 * M * P * N                       # G·θ for every chain
+    executed = 2.0 * M * 3 * kp * N             # split BF16: three products per term
+    pk = peaks()
+    peak = float(pk.get("bf16_tflops", 1900.0))
+    # the same evaluation in FP64 on the CUDA cores, for the precision/speed trade
+    model.tensor_cores = False
+    model.forward(theta, out)
+    e64 = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(2)]
+    for a, b in e64:
+        a.record(stream)
+        model.forward(theta, out)
+        b.record(stream)
+    torch.cuda.synchronize()
+    t64 = sum(a.elapsed_time(b) for a, b in e64) / len(e64) / 1e3
+    model.tensor_cores = True
+    # whole run to β = 1
+    app2 = Application(model, job=Job(chains=N, steps=5), rng=RNG(199 + rank), controller=Annealer())
+    app2.initialize()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    app2.controller.posterior(model, max_stages=args.max_stages)
+    torch.cuda.synchronize()
+    t_run = time.perf_counter() - t0
+    reps = app2.controller.worker.reports
+    th = app2.controller.worker.step.theta.cpu().numpy()
+    err_mean = float(np.max(np.abs(th.mean(0) - truth)))
+    if rank == 0:
+        print(json.dumps({
+            "metric": "linear-model llk evaluations/s", "value": world * N / t, "unit": "chain-llk/s",
+            "n_gpus": world, "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": t * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16x3/f32/f64",
+            "data": "synthetic",
+            "config": {"workload": "linear-gaussian", "observations": M, "parameters": P, "chains": N,
+                       "cd": "dense exponential, 2 km correlation", "l2": "flushed (256 MB write)"},
+            "roofline": {"bound": "tensor", "achieved": alg / t / 1e12, "peak": peak, "unit": "TFLOP/s",
+                         "frac": alg / t / 1e12 / peak, "executed_tflops": executed / t / 1e12,
+                         "executed_frac": executed / t / 1e12 / peak,
+                         "note": "achieved counts 2·M·P·N; the split-BF16 GEMM executes 3x that"},
+            "fp64_cuda_cores_ms": t64 * 1e3,
+            "full_run": {"time_s": t_run, "stages": len(reps), "final_beta": reps[-1]["beta"] if reps else None,
+                         "max_abs_error_of_posterior_mean": err_mean},
+            "clocks": clk.summary()}))
+    return 0
+
+
 def run_ours(args):
     import torch
     rank, world, local, dist = dist_setup()
@@ -443,7 +532,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--mode", default="walk", choices=["walk", "anneal", "compare"])
+    ap.add_argument("--mode", default="walk", choices=["walk", "anneal", "compare", "linear"])
     ap.add_argument("--sampler", default="plain", choices=["plain", "da"])
     ap.add_argument("--max-stages", type=int, default=400)
     ap.add_argument("--da-start-beta", type=float, default=0.0)
@@ -463,6 +552,8 @@ def main():
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     if args.impl == "reference":
         return run_reference(args)
+    if args.mode == "linear":
+        return run_linear(args)
     return run_ours(args)
 
 
