@@ -207,12 +207,38 @@ __global__ void whiten_rho0_kernel(const double* __restrict__ W, const double* _
 }
 
 // θ₀ = column means of θ (one thread per parameter, fixed order)
-__global__ void column_mean_kernel(const double* __restrict__ theta, int n, int p, double* __restrict__ mean) {
-    int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= p) return;
+// Column means in two passes with a fixed summation order: block (c, ·) sums rows
+// [c·kMeanRows, (c+1)·kMeanRows) of its columns (threads over columns: coalesced rows),
+// then one thread per column adds the chunk sums in chunk order.
+constexpr int kMeanRows = 128;
+static inline int cdiv(long a, long b) { return (int)((a + b - 1) / b); }
+
+template <class T>
+__global__ void colsum_partial_kernel(const T* __restrict__ x, int ld, int col0, int n, int cols,
+                                      double* __restrict__ part) {
+    const int j = blockIdx.y * blockDim.x + threadIdx.x;
+    if (j >= cols) return;
+    const int r0 = blockIdx.x * kMeanRows, r1 = min(n, r0 + kMeanRows);
     double s = 0.0;
-    for (int i = 0; i < n; ++i) s += theta[(size_t)i * p + j];
+    for (int i = r0; i < r1; ++i) s += (double)x[(size_t)i * ld + col0 + j];
+    part[(size_t)blockIdx.x * cols + j] = s;
+}
+
+__global__ void colsum_final_kernel(const double* __restrict__ part, int nchunks, int cols, int n,
+                                    double* __restrict__ mean) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= cols) return;
+    double s = 0.0;
+    for (int c = 0; c < nchunks; ++c) s += part[(size_t)c * cols + j];
     mean[j] = s / n;
+}
+
+template <class T>
+static void column_means(const T* x, int ld, int col0, int n, int cols, double* part, double* mean,
+                         cudaStream_t s) {
+    const int nchunks = cdiv(n, kMeanRows);
+    colsum_partial_kernel<T><<<dim3(nchunks, cdiv(cols, 256)), 256, 0, s>>>(x, ld, col0, n, cols, part);
+    colsum_final_kernel<<<cdiv(cols, 256), 256, 0, s>>>(part, nchunks, cols, n, mean);
 }
 
 // ρ₀ = A θ₀ - b in FP64 (one warp per observation)
@@ -264,16 +290,6 @@ __global__ void linear_reduce_kernel(int n, int tiles, const double* __restrict_
     double s = 0.0;
     for (int t = 0; t < tiles; ++t) s += partial[(size_t)t * n + i];
     llk[i] = (accumulate ? llk[i] : norm) - 0.5 * s;
-}
-
-// column means of an FP32 block (n rows, m columns from col0, row stride ld), FP64 accumulation
-__global__ void block_mean_kernel(const float* __restrict__ r, int ld, int col0, int n, int m,
-                                  double* __restrict__ mean) {
-    int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= m) return;
-    double s = 0.0;
-    for (int i = 0; i < n; ++i) s += (double)r[(size_t)i * ld + col0 + j];
-    mean[j] = s / n;
 }
 
 // δ = r - r̄ split as [hi | lo | hi] (BF16), rows of length 3 kp
@@ -347,7 +363,6 @@ static int make_map(CUtensorMap* map, const void* ptr_, int rows, int cols, int 
 
 using namespace ag;
 
-static inline int cdiv(long a, long b) { return (int)((a + b - 1) / b); }
 static inline size_t al256(size_t b) { return (b + 255) / 256 * 256; }
 
 extern "C" int32_t ag_linear_kpad(int32_t p) { return p > 0 ? cdiv(p, TC_BK) * TC_BK : 0; }
@@ -364,7 +379,8 @@ extern "C" size_t ag_linear_workspace_bytes(int32_t m, int32_t p, int32_t n) {
     if (m <= 0 || p <= 0 || n <= 0) return 0;
     const size_t kp = ag_linear_kpad(p);
     return al256(p * sizeof(double)) + al256((size_t)m * sizeof(float)) +
-           al256((size_t)n * 3 * kp * 2) + al256((size_t)cdiv(m, TC_BN) * n * sizeof(double));
+           al256((size_t)n * 3 * kp * 2) + al256((size_t)cdiv(m, TC_BN) * n * sizeof(double)) +
+           al256((size_t)cdiv(n, kMeanRows) * p * sizeof(double));
 }
 
 extern "C" int ag_linear_llk(const ag_linear_model* lm, const double* theta, int32_t n, double norm,
@@ -383,9 +399,10 @@ extern "C" int ag_linear_llk(const ag_linear_model* lm, const double* theta, int
     double* theta0 = reinterpret_cast<double*>(ws); ws += al256(p * sizeof(double));
     float* rho0 = reinterpret_cast<float*>(ws); ws += al256((size_t)m * sizeof(float));
     __nv_bfloat16* tsplit = reinterpret_cast<__nv_bfloat16*>(ws); ws += al256((size_t)n * 3 * kp * 2);
-    double* partial = reinterpret_cast<double*>(ws);
+    double* partial = reinterpret_cast<double*>(ws); ws += al256((size_t)cdiv(m, TC_BN) * n * sizeof(double));
+    double* colpart = reinterpret_cast<double*>(ws);
     const int tiles = cdiv(m, TC_BN);
-    column_mean_kernel<<<cdiv(p, 128), 128, 0, s>>>(theta, n, p, theta0);
+    column_means(theta, p, 0, n, p, colpart, theta0, s);
     rho0_kernel<<<cdiv((long)m * 32, 256), 256, 0, s>>>(lm->a64, lm->b64, theta0, m, p, rho0);
     split_theta_kernel<<<cdiv((long)n * kp, 256), 256, 0, s>>>(theta, theta0, n, p, kp, tsplit);
     int rc = launch_status("linear prologue kernels");
@@ -415,7 +432,8 @@ extern "C" size_t ag_whiten_workspace_bytes(int32_t m, int32_t n) {
     if (m <= 0 || n <= 0) return 0;
     const size_t kp = ag_linear_kpad(m);
     return al256(m * sizeof(double)) + al256(sizeof(double)) + al256((size_t)m * sizeof(float)) +
-           al256((size_t)n * 3 * kp * 2) + al256((size_t)cdiv(m, TC_BN) * n * sizeof(double));
+           al256((size_t)n * 3 * kp * 2) + al256((size_t)cdiv(m, TC_BN) * n * sizeof(double)) +
+           al256((size_t)cdiv(n, kMeanRows) * m * sizeof(double));
 }
 
 extern "C" int ag_whiten_llk(const ag_whiten_block* blk, const float* resid, int32_t ldr, int32_t n,
@@ -436,9 +454,10 @@ extern "C" int ag_whiten_llk(const ag_whiten_block* blk, const float* resid, int
     ws += al256(sizeof(double));
     float* rho0 = reinterpret_cast<float*>(ws); ws += al256((size_t)m * sizeof(float));
     __nv_bfloat16* rsplit = reinterpret_cast<__nv_bfloat16*>(ws); ws += al256((size_t)n * 3 * kp * 2);
-    double* partial = reinterpret_cast<double*>(ws);
+    double* partial = reinterpret_cast<double*>(ws); ws += al256((size_t)cdiv(m, TC_BN) * n * sizeof(double));
+    double* colpart = reinterpret_cast<double*>(ws);
     const int tiles = cdiv(m, TC_BN);
-    block_mean_kernel<<<cdiv(m, 128), 128, 0, s>>>(resid, ldr, col0, n, m, mean);
+    column_means(resid, ldr, col0, n, m, colpart, mean, s);
     int rc = launch_status("whitening prologue");
     if (rc) return rc;
     split_block_kernel<<<cdiv((long)n * kp, 256), 256, 0, s>>>(resid, ldr, col0, mean, n, m, kp, rsplit);

@@ -16,7 +16,8 @@
 
 namespace ag {
 
-constexpr int kMaxP = 32;          // largest parameter count of the stage kernels
+constexpr int kMaxP = 32;          // parameter counts up to this use the one-thread-per-chain proposal
+constexpr int kMaxPLarge = 512;    // largest parameter count of the stage kernels
 constexpr int kGridPoints = 11;    // COV.cc:276 Nbeta = 10 -> 11 points per level
 constexpr int kBrentMaxIter = 128;   // Brent iterations run on the device per stage
 constexpr int kGridLevels = 11;    // COV.cc:313 Nloop <= Nbeta
@@ -90,6 +91,48 @@ __global__ void propose_kernel(const double* __restrict__ theta, int n, int p,
         for (int j = 0; j < p; ++j) c[j] = th[j];
     mask[i] = out ? CHAIN_OUT_OF_SUPPORT : 0u;
     cprior[i] = uniform_log_prior(p, lo, hi);
+}
+
+// The same proposal for many parameters: one warp per chain, the chain's normals in
+// shared memory, lane j computing the rows j, j + 32, ... of L z with the same
+// sequential k order as propose_kernel (identical results).
+constexpr int kProposeWarps = 8;
+__global__ void __launch_bounds__(kProposeWarps * 32)
+propose_warp_kernel(const double* __restrict__ theta, int n, int p, const double* __restrict__ chol,
+                    const double* __restrict__ lo, const double* __restrict__ hi, uint64_t seed,
+                    uint32_t step, const uint32_t* __restrict__ epoch, double* __restrict__ cand,
+                    uint32_t* __restrict__ mask, double* __restrict__ cprior) {
+    extern __shared__ double sz[];                 // [kProposeWarps][p] normals
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int i = blockIdx.x * kProposeWarps + warp;
+    if (i >= n) return;
+    double* z = sz + (size_t)warp * p;
+    const uint32_t ep = *epoch;
+    for (int q = lane; 2 * q < p; q += 32) {
+        double z0, z1;
+        normal_pair(draw(seed, (uint32_t)i, (uint32_t)q, STREAM_PROPOSAL, step, ep), z0, z1);
+        z[2 * q] = z0;
+        if (2 * q + 1 < p) z[2 * q + 1] = z1;
+    }
+    __syncwarp();
+    const double* th = theta + (size_t)i * p;
+    double* c = cand + (size_t)i * p;
+    bool out = false;
+    for (int j = lane; j < p; j += 32) {
+        const double* row = chol + (size_t)j * p;
+        double d = 0.0;
+        for (int k = 0; k <= j; ++k) d = fma(row[k], z[k], d);
+        const double v = th[j] + d;
+        c[j] = v;
+        out |= !(lo[j] <= v && v <= hi[j]);
+    }
+    out = __any_sync(0xffffffffu, out);
+    if (out)
+        for (int j = lane; j < p; j += 32) c[j] = th[j];
+    if (lane == 0) {
+        mask[i] = out ? CHAIN_OUT_OF_SUPPORT : 0u;
+        cprior[i] = uniform_log_prior(p, lo, hi);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -514,97 +557,128 @@ __global__ void cov_weights_kernel(const double* __restrict__ llk, int n,
 }
 
 // ---------------------------------------------------------------------------
-// weighted covariance (COV.py:106-156): per-chunk partial sums in fixed order
+// weighted covariance (COV.py:106-156): per-chunk partial sums in fixed order.  A chunk
+// holds as many chains as fit the shared-memory budget (256 for up to 32 parameters).
+constexpr size_t kSigmaSmem = 96 * 1024;
+static int sigma_chunk(int p) {
+    int c = kSigmaChunk;
+    while (c > 1 && (size_t)c * (p + 1) * sizeof(double) > kSigmaSmem) c >>= 1;
+    return c;
+}
+
+constexpr int kSigmaBlocks = 256;  // at most this many partial sums per entry
+
+// Block b sums the chunks [b·cpb, (b+1)·cpb) in order into part[b][e].
 __global__ void __launch_bounds__(256) sigma_partial_kernel(const double* __restrict__ theta,
                                                             const double* __restrict__ w, int n,
-                                                            int p, double* __restrict__ part) {
-    extern __shared__ double sm[];      // [kSigmaChunk][p] θ, then [kSigmaChunk] w
+                                                            int p, int chunk, int cpb,
+                                                            double* __restrict__ part) {
+    extern __shared__ double sm[];      // [chunk][p] θ, then [chunk] w
     double* sth = sm;
-    double* sw = sm + (size_t)kSigmaChunk * p;
-    const int begin = blockIdx.x * kSigmaChunk;
-    const int cnt = min(kSigmaChunk, n - begin);
-    for (int k = threadIdx.x; k < cnt * p; k += blockDim.x) sth[k] = theta[(size_t)begin * p + k];
-    for (int k = threadIdx.x; k < cnt; k += blockDim.x) sw[k] = w[begin + k];
-    __syncthreads();
+    double* sw = sm + (size_t)chunk * p;
     // entries: 0 = Σw, 1..p = Σ w θ_a, then lower triangle (a >= b) Σ w θ_a θ_b
     const int nent = 1 + p + p * (p + 1) / 2;
-    for (int e = threadIdx.x; e < nent; e += blockDim.x) {
-        int a = -1, b = -1;
-        if (e >= 1 && e <= p) {
-            a = e - 1;
-        } else if (e > p) {
-            int t = e - 1 - p;
-            a = 0;
-            while (t > a) { t -= a + 1; ++a; }
-            b = t;
+    const int c0 = blockIdx.x * cpb;
+    for (int c = c0; c < c0 + cpb; ++c) {
+        const int begin = c * chunk;
+        if (begin >= n) break;
+        const int cnt = min(chunk, n - begin);
+        __syncthreads();
+        for (int k = threadIdx.x; k < cnt * p; k += blockDim.x) sth[k] = theta[(size_t)begin * p + k];
+        for (int k = threadIdx.x; k < cnt; k += blockDim.x) sw[k] = w[begin + k];
+        __syncthreads();
+        for (int e = threadIdx.x; e < nent; e += blockDim.x) {
+            int a = -1, b = -1;
+            if (e >= 1 && e <= p) {
+                a = e - 1;
+            } else if (e > p) {
+                // row a of the lower triangle starts at entry a (a + 1) / 2
+                int t = e - 1 - p;
+                a = (int)((sqrt(8.0 * t + 1.0) - 1.0) * 0.5);
+                while ((a + 1) * (a + 2) / 2 <= t) ++a;
+                while (a * (a + 1) / 2 > t) --a;
+                b = t - a * (a + 1) / 2;
+            }
+            double acc = (c == c0) ? 0.0 : part[(size_t)blockIdx.x * nent + e];
+            for (int i = 0; i < cnt; ++i) {
+                double v = sw[i];
+                if (a >= 0) v *= sth[i * p + a];
+                if (b >= 0) v *= sth[i * p + b];
+                acc += v;
+            }
+            part[(size_t)blockIdx.x * nent + e] = acc;
         }
-        double acc = 0.0;
-        for (int i = 0; i < cnt; ++i) {
-            double v = sw[i];
-            if (a >= 0) v *= sth[i * p + a];
-            if (b >= 0) v *= sth[i * p + b];
-            acc += v;
-        }
-        part[(size_t)blockIdx.x * nent + e] = acc;
     }
 }
 
-__global__ void sigma_final_kernel(int p, int nblk, const double* __restrict__ part,
-                                   double* __restrict__ sigma) {
-    const int nent = 1 + p + p * (p + 1) / 2;
-    __shared__ double tot[1 + kMaxP + kMaxP * (kMaxP + 1) / 2];
-    for (int e = threadIdx.x; e < nent; e += blockDim.x) {
-        double acc = 0.0;
-        for (int k = 0; k < nblk; ++k) acc += part[(size_t)k * nent + e];
-        tot[e] = acc;
-    }
-    __syncthreads();
-    if (threadIdx.x != 0) return;
-    double mean[kMaxP];
-    for (int a = 0; a < p; ++a) mean[a] = tot[1 + a] / tot[0];   // weighted mean (gsl_stats_wmean)
-    int e = 1 + p;
-    for (int a = 0; a < p; ++a)
-        for (int b = 0; b <= a; ++b, ++e) {
-            const double v = tot[e] - mean[a] * mean[b];
-            sigma[a * p + b] = v;
-            sigma[b * p + a] = v;
-        }
+// totals over the chunks, in chunk order
+__global__ void sigma_total_kernel(int nent, int nblk, const double* __restrict__ part, double* __restrict__ tot) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nent) return;
+    double acc = 0.0;
+    for (int k = 0; k < nblk; ++k) acc += part[(size_t)k * nent + e];
+    tot[e] = acc;
 }
 
-// chol(scaling² Σ), lower triangle row-major (Metropolis.py:103-107)
+// Σ_ab = Σ w θ_a θ_b - θ̄_a θ̄_b with θ̄ = Σ w θ / Σ w (gsl_stats_wmean)
+__global__ void sigma_assemble_kernel(int p, const double* __restrict__ tot, double* __restrict__ sigma) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= p * (p + 1) / 2) return;
+    int a = (int)((sqrt(8.0 * e + 1.0) - 1.0) * 0.5);
+    while ((a + 1) * (a + 2) / 2 <= e) ++a;
+    while (a * (a + 1) / 2 > e) --a;
+    const int b = e - a * (a + 1) / 2;
+    const double ma = tot[1 + a] / tot[0], mb = tot[1 + b] / tot[0];
+    const double v = tot[1 + p + e] - ma * mb;
+    sigma[a * p + b] = v;
+    sigma[b * p + a] = v;
+}
+
+// chol(scaling² Σ), lower triangle row-major (Metropolis.py:103-107).  One CTA,
+// left-looking by columns in L itself: thread 0 forms the diagonal, then every
+// thread forms one entry below it; each entry sums over k in increasing order, as
+// the sequential Cholesky–Crout loop does.
 __global__ void cholesky_kernel(int p, const double* __restrict__ sigma,
                                 const double* __restrict__ scaling, double* __restrict__ L,
                                 uint32_t* __restrict__ flags) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    double A[kMaxP * kMaxP];
+    __shared__ double s_ljj;
+    __shared__ int s_ok;
     const double s2 = (*scaling) * (*scaling);
-    for (int k = 0; k < p * p; ++k) A[k] = s2 * sigma[k];
-    bool ok = true;
+    for (int k = threadIdx.x; k < p * p; k += blockDim.x) L[k] = s2 * sigma[k];
+    if (threadIdx.x == 0) s_ok = 1;
+    __syncthreads();
     for (int j = 0; j < p; ++j) {
-        double d = A[j * p + j];
-        for (int k = 0; k < j; ++k) d -= A[j * p + k] * A[j * p + k];
-        if (!(d > 0.0)) {
-            ok = false;
-            break;
+        if (threadIdx.x == 0) {
+            double d = L[j * p + j];
+            for (int k = 0; k < j; ++k) d -= L[j * p + k] * L[j * p + k];
+            if (!(d > 0.0)) {
+                s_ok = 0;
+            } else {
+                s_ljj = sqrt(d);
+                L[j * p + j] = s_ljj;
+            }
         }
-        const double ljj = sqrt(d);
-        A[j * p + j] = ljj;
-        for (int i = j + 1; i < p; ++i) {
-            double v = A[i * p + j];
-            for (int k = 0; k < j; ++k) v -= A[i * p + k] * A[j * p + k];
-            A[i * p + j] = v / ljj;
+        __syncthreads();
+        if (!s_ok) break;
+        const double ljj = s_ljj;
+        for (int i = j + 1 + threadIdx.x; i < p; i += blockDim.x) {
+            double v = L[i * p + j];
+            for (int k = 0; k < j; ++k) v -= L[i * p + k] * L[j * p + k];
+            L[i * p + j] = v / ljj;
         }
+        __syncthreads();
     }
-    if (!ok) {
+    if (!s_ok) {
         // keep the walk defined: fall back to the scaled diagonal and report
-        raise_flag(flags, DEV_ERR_NOT_SPD);
-        for (int i = 0; i < p; ++i)
-            for (int k = 0; k < p; ++k)
-                L[i * p + k] = (i == k) ? sqrt(fmax(s2 * sigma[i * p + i], 0.0)) : 0.0;
+        if (threadIdx.x == 0) raise_flag(flags, DEV_ERR_NOT_SPD);
+        for (int k = threadIdx.x; k < p * p; k += blockDim.x) {
+            const int i = k / p, c = k % p;
+            L[k] = (i == c) ? sqrt(fmax(s2 * sigma[k], 0.0)) : 0.0;
+        }
         return;
     }
-    for (int i = 0; i < p; ++i)
-        for (int k = 0; k < p; ++k) L[i * p + k] = (k <= i) ? A[i * p + k] : 0.0;
+    for (int k = threadIdx.x; k < p * p; k += blockDim.x)
+        if (k % p > k / p) L[k] = 0.0;              // clear the upper triangle
 }
 
 // ---------------------------------------------------------------------------
@@ -802,11 +876,24 @@ extern "C" int ag_propose(const ag_stage_state* st, const double* theta, int32_t
                           double* cand, uint32_t* mask, double* cprior, void* stream) {
     int rc = check_state(st);
     if (rc) return rc;
-    AG_REQUIRE(n > 0 && p > 0 && p <= kMaxP && theta && lo && hi && cand && mask && cprior,
-               "invalid arguments (p must be in 1..%d)", kMaxP);
-    propose_kernel<<<blocks(n, 128), 128, 0, as_stream(stream)>>>(theta, n, p, st->chol, lo, hi, seed,
-                                                                   step, st->epoch, cand, mask, cprior);
-    return launch_status("propose_kernel");
+    AG_REQUIRE(n > 0 && p > 0 && p <= kMaxPLarge && theta && lo && hi && cand && mask && cprior,
+               "invalid arguments (p must be in 1..%d)", kMaxPLarge);
+    cudaStream_t s = as_stream(stream);
+    if (p <= kMaxP) {
+        propose_kernel<<<blocks(n, 128), 128, 0, s>>>(theta, n, p, st->chol, lo, hi, seed, step, st->epoch, cand,
+                                                       mask, cprior);
+        return launch_status("propose_kernel");
+    }
+    const size_t smem = (size_t)kProposeWarps * p * sizeof(double);
+    if (smem > 48 * 1024) {
+        rc = cuda_status(cudaFuncSetAttribute(propose_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)smem),
+                         "cudaFuncSetAttribute(propose_warp_kernel)");
+        if (rc) return rc;
+    }
+    propose_warp_kernel<<<blocks(n, kProposeWarps), kProposeWarps * 32, smem, s>>>(
+        theta, n, p, st->chol, lo, hi, seed, step, st->epoch, cand, mask, cprior);
+    return launch_status("propose_warp_kernel");
 }
 
 extern "C" int ag_accept(const ag_stage_state* st, int32_t n, int32_t p, uint64_t seed,
@@ -890,22 +977,33 @@ extern "C" int ag_cov_schedule_brent(const ag_stage_state* st, const double* dat
     return launch_status("cov schedule kernels (Brent)");
 }
 
+static void sigma_grid(int n, int p, int* chunk, int* nblk, int* cpb) {
+    *chunk = sigma_chunk(p);
+    const int nchunks = blocks(n, *chunk);
+    *cpb = blocks(nchunks, kSigmaBlocks);
+    *nblk = blocks(nchunks, *cpb);
+}
+
 extern "C" size_t ag_sigma_workspace_bytes(int32_t n, int32_t p) {
-    if (n <= 0 || p <= 0) return 0;
+    if (n <= 0 || p <= 0 || p > kMaxPLarge) return 0;
+    int chunk, nblk, cpb;
+    sigma_grid(n, p, &chunk, &nblk, &cpb);
     const size_t nent = 1 + p + (size_t)p * (p + 1) / 2;
-    return (size_t)blocks(n, kSigmaChunk) * nent * sizeof(double);
+    return ((size_t)nblk + 1) * nent * sizeof(double);
 }
 
 extern "C" int ag_weighted_cov(const ag_stage_state* st, const double* theta, int32_t n, int32_t p,
                                void* workspace, size_t workspace_bytes, void* stream) {
     int rc = check_state(st);
     if (rc) return rc;
-    AG_REQUIRE(n > 0 && p > 0 && p <= kMaxP && theta, "invalid arguments (p <= %d)", kMaxP);
+    AG_REQUIRE(n > 0 && p > 0 && p <= kMaxPLarge && theta, "invalid arguments (p <= %d)", kMaxPLarge);
     const size_t need = ag_sigma_workspace_bytes(n, p);
     AG_REQUIRE(workspace && workspace_bytes >= need, "ag_weighted_cov needs %zu bytes", need);
     cudaStream_t s = as_stream(stream);
-    const int nblk = blocks(n, kSigmaChunk);
-    const size_t smem = (size_t)kSigmaChunk * (p + 1) * sizeof(double);
+    int chunk, nblk, cpb;
+    sigma_grid(n, p, &chunk, &nblk, &cpb);
+    const int nent = 1 + p + p * (p + 1) / 2;
+    const size_t smem = (size_t)chunk * (p + 1) * sizeof(double);
     if (smem > 48 * 1024) {
         rc = cuda_status(cudaFuncSetAttribute(sigma_partial_kernel,
                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
@@ -913,16 +1011,18 @@ extern "C" int ag_weighted_cov(const ag_stage_state* st, const double* theta, in
         if (rc) return rc;
     }
     double* part = reinterpret_cast<double*>(workspace);
-    sigma_partial_kernel<<<nblk, 256, smem, s>>>(theta, st->w, n, p, part);
-    sigma_final_kernel<<<1, 256, 0, s>>>(p, nblk, part, st->sigma);
+    double* tot = part + (size_t)nblk * nent;
+    sigma_partial_kernel<<<nblk, 256, smem, s>>>(theta, st->w, n, p, chunk, cpb, part);
+    sigma_total_kernel<<<blocks(nent, 256), 256, 0, s>>>(nent, nblk, part, tot);
+    sigma_assemble_kernel<<<blocks(p * (p + 1) / 2, 256), 256, 0, s>>>(p, tot, st->sigma);
     return launch_status("weighted covariance kernels");
 }
 
 extern "C" int ag_cholesky_scaled(const ag_stage_state* st, int32_t p, void* stream) {
     int rc = check_state(st);
     if (rc) return rc;
-    AG_REQUIRE(p > 0 && p <= kMaxP, "p must be in 1..%d", kMaxP);
-    cholesky_kernel<<<1, 32, 0, as_stream(stream)>>>(p, st->sigma, st->scaling, st->chol, st->dev_flags);
+    AG_REQUIRE(p > 0 && p <= kMaxPLarge, "p must be in 1..%d", kMaxPLarge);
+    cholesky_kernel<<<1, 256, 0, as_stream(stream)>>>(p, st->sigma, st->scaling, st->chol, st->dev_flags);
     return launch_status("cholesky_kernel");
 }
 

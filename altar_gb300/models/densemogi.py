@@ -57,7 +57,9 @@ class DenseMogi(Bayesian):
             l = np.asarray(ds_k["los"], float).reshape(-1, 3)
             los.append(np.repeat(l, m, 0) if l.shape[0] == 1 else l)
             ds.append(np.asarray(ds_k["d"], float))
-            cd = torch.as_tensor(np.asarray(ds_k["cd"], float), device=DEVICE)
+            cd = ds_k["cd"]
+            cd = (cd.to(device=DEVICE, dtype=torch.float64) if torch.is_tensor(cd)
+                  else torch.as_tensor(np.asarray(cd, float), device=DEVICE))
             L = torch.linalg.cholesky(cd)
             W = torch.linalg.solve_triangular(L, torch.eye(m, dtype=torch.float64, device=DEVICE), upper=False)
             logdet += 2.0 * float(torch.log(torch.diagonal(L)).sum())

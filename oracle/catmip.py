@@ -210,7 +210,7 @@ def dbeta_brent(llk, beta, target=1.0, tol=0.01, maxiter=1000):
 def weighted_cov(theta, w):
     """θ̄ = Σwθ/Σw; Σ = Σ w θθᵀ - θ̄θ̄ᵀ (altar/altar/bayesian/COV.py:106-156)."""
     mean = (w[:, None] * theta).sum(0) / w.sum()
-    S = (w[:, None, None] * theta[:, :, None] * theta[:, None, :]).sum(0)
+    S = (theta * w[:, None]).T @ theta
     return S - np.outer(mean, mean)
 
 
