@@ -715,8 +715,8 @@ using namespace ag;
 // CDM launch variants: warps (= chains) per CTA and resident CTAs per SM the
 // register allocation targets; chosen per problem by the autotuner
 struct CdmVariant { int warps; };
-static constexpr CdmVariant kCdmVariants[] = {{8}, {4}, {4}, {2}, {4}, {4}, {2}, {4}, {4}};
-static constexpr int kCdmVariantCount = 9;
+static constexpr CdmVariant kCdmVariants[] = {{8}, {4}, {4}, {2}, {4}, {4}, {2}, {4}, {4}, {4}, {4}};
+static constexpr int kCdmVariantCount = 11;
 static constexpr int kMogiChains = 16;
 
 extern "C" int32_t ag_forward_variants(int model) { return model == AG_MODEL_CDM ? kCdmVariantCount : 1; }
@@ -799,7 +799,9 @@ static int forward_llk(int model, const ag_layout* layout, const double* theta, 
             case 5: AG_CDM_LAUNCH(4, 4, 2); break;
             case 6: AG_CDM_LAUNCH(2, 6, 2); break;
             case 7: AG_CDM_LAUNCH(4, 2, 4); break;
-            default: AG_CDM_LAUNCH(4, 3, 4); break;
+            case 8: AG_CDM_LAUNCH(4, 3, 4); break;
+            case 9: AG_CDM_LAUNCH(4, 4, 4); break;
+            default: AG_CDM_LAUNCH(4, 5, 4); break;
         }
 #undef AG_CDM_LAUNCH
         return launch_status("cdm_llk_kernel");

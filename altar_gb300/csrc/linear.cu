@@ -10,11 +10,12 @@
 // the product A δ is one GEMM over the concatenated K axis
 //     [δ_hi | δ_lo | δ_hi] · [A_hi | A_hi | A_lo]ᵀ
 // (three BF16 products, FP32 accumulation; the dropped lo·lo term is
-// ~2^-18 relative).  The GEMM is a tcgen05 kernel: TMA loads 128B-swizzled
-// K-major tiles into a 4-stage shared-memory ring guarded by mbarriers, one
-// thread issues tcgen05.mma (M = 128 chains, N = 256 observations, K = 16)
-// into a TMEM accumulator, and the epilogue reads TMEM with tcgen05.ld and
-// reduces Σ (acc + ρ₀)² per chain straight from registers.
+// ~2^-18 relative).  The GEMM is a persistent tcgen05 kernel: TMA loads
+// 128B-swizzled K-major tiles into a 4-stage shared-memory ring guarded by
+// mbarriers, one thread issues tcgen05.mma (M = 128 chains, N = 256
+// observations, K = 16) into one of two TMEM accumulators, and four epilogue
+// warps read the other accumulator with tcgen05.ld and reduce Σ (acc + ρ₀)²
+// per chain straight from registers while the next tile's MMAs run.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -33,7 +34,6 @@ constexpr int TC_STAGES = 4;
 constexpr uint32_t TC_A_BYTES = TC_BM * TC_BK * 2;   // 16 KB
 constexpr uint32_t TC_B_BYTES = TC_BN * TC_BK * 2;   // 32 KB
 constexpr uint32_t TC_STAGE_BYTES = TC_A_BYTES + TC_B_BYTES;
-constexpr uint32_t TC_SMEM = TC_STAGES * TC_STAGE_BYTES + 1024 /*align*/ + 1024 /*ρ₀*/ + 256 /*bars*/;
 constexpr uint32_t TC_WAIT = 1u << 22;
 
 // shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 B apart
@@ -68,8 +68,12 @@ AG_DEVICE_INLINE void mma_commit(uint32_t bar) {
 AG_DEVICE_INLINE void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 AG_DEVICE_INLINE void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-AG_DEVICE_INLINE void tmem_ld32(uint32_t taddr, float (&v)[32]) {
-    uint32_t r[32];
+AG_DEVICE_INLINE void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
+// tcgen05.ld of 32 columns without the completion wait (pair with tmem_wait_ld)
+AG_DEVICE_INLINE void tmem_ld32_nowait(uint32_t taddr, uint32_t (&r)[32]) {
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
         "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
@@ -80,118 +84,197 @@ AG_DEVICE_INLINE void tmem_ld32(uint32_t taddr, float (&v)[32]) {
           "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
           "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
         : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+AG_DEVICE_INLINE void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// Persistent CTAs, one per SM, each taking tiles t = blockIdx.x, blockIdx.x + gridDim.x, ...
+// of 128 chains x 256 observations; partial[tile_n * n + chain] = Σ_obs (acc + ρ₀)².
+// Warp roles: warp 0 lane 0 drives TMA through the TC_STAGES shared-memory ring, warp 1
+// lane 0 issues tcgen05.mma into one of two TMEM accumulators (2 x 256 columns), warps
+// 2-5 read the other accumulator with tcgen05.ld and reduce the previous tile, so the
+// epilogue and the next tile's MMAs overlap.  Tiles are visited in groups of
+// TC_GROUP_M chain tiles so that CTAs running at the same time share both operands' k
+// slices in L2.  Every wait is bounded; a timeout stops all roles, drains the copies
+// and MMAs in flight and frees TMEM.
+constexpr int TC_THREADS = 192;
+constexpr int TC_GROUP_M = 8;
+constexpr uint32_t TC_SMEM = TC_STAGES * TC_STAGE_BYTES + 1024 /*align*/ + 256 /*bars*/;
+
+AG_DEVICE_INLINE void tile_coords(int t, int mtiles, int ntiles, int& mt, int& nt) {
+    const int span = TC_GROUP_M * ntiles;
+    const int g = t / span, r = t % span;
+    const int gm = (mtiles - g * TC_GROUP_M) < TC_GROUP_M ? (mtiles - g * TC_GROUP_M) : TC_GROUP_M;
+    mt = g * TC_GROUP_M + r % gm;
+    nt = r / gm;
 }
 
-// One CTA: 128 chains x 256 observations; partial[tile_n * n + chain] = Σ_obs (acc + ρ₀)²
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(TC_THREADS, 1)
 linear_misfit_tc_kernel(const __grid_constant__ CUtensorMap map_a,   // chains  x K' (BF16)
                         const __grid_constant__ CUtensorMap map_b,   // obs     x K' (BF16)
-                        int n, int m_obs, int kblocks, const float* __restrict__ rho0,
-                        double* __restrict__ partial, uint32_t* __restrict__ flags) {
+                        int n, int m_obs, int kblocks, int mtiles, int ntiles,
+                        const float* __restrict__ rho0, double* __restrict__ partial,
+                        uint32_t* __restrict__ flags) {
     extern __shared__ uint8_t smem_raw[];
     const uint32_t raw = smem_addr(smem_raw);
     const uint32_t base = (raw + 1023u) & ~1023u;
     uint8_t* gbase = smem_raw + (base - raw);
-    float* s_rho = reinterpret_cast<float*>(gbase + TC_STAGES * TC_STAGE_BYTES);
-    uint64_t* bars = reinterpret_cast<uint64_t*>(gbase + TC_STAGES * TC_STAGE_BYTES + 1024);
-    uint64_t* full = bars;                       // [TC_STAGES]
-    uint64_t* empty = bars + TC_STAGES;          // [TC_STAGES]
-    uint64_t* done = bars + 2 * TC_STAGES;       // [1]
+    uint64_t* bars = reinterpret_cast<uint64_t*>(gbase + TC_STAGES * TC_STAGE_BYTES);
+    uint64_t* full = bars;                       // [TC_STAGES]  TMA -> MMA
+    uint64_t* empty = bars + TC_STAGES;          // [TC_STAGES]  MMA -> TMA
+    uint64_t* tfull = bars + 2 * TC_STAGES;      // [2]          MMA -> epilogue
+    uint64_t* tempty = bars + 2 * TC_STAGES + 2; // [2]          epilogue -> MMA
+    uint64_t* drain = bars + 2 * TC_STAGES + 4;  // [1]          all MMAs done (teardown)
     __shared__ uint32_t s_tmem;
     __shared__ int s_abort;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int m0 = blockIdx.x * TC_BM;           // first chain
-    const int n0 = blockIdx.y * TC_BN;           // first observation
+    const int total = mtiles * ntiles;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < TC_STAGES; ++s) {
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
         }
-        mbar_init(done, 1);
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&tfull[b], 1);
+            mbar_init(&tempty[b], 4);
+        }
+        mbar_init(drain, 1);
         fence_mbar_init();
         s_abort = 0;
     }
-    for (int j = threadIdx.x; j < TC_BN; j += blockDim.x) s_rho[j] = (n0 + j < m_obs) ? rho0[n0 + j] : 0.f;
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
-                     ::"r"(smem_addr(&s_tmem)), "r"(TC_BN) : "memory");
+                     ::"r"(smem_addr(&s_tmem)), "r"(2 * TC_BN) : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = s_tmem;
+    auto aborted = [&]() { return *(volatile int*)&s_abort != 0; };
 
-    if (threadIdx.x == 32) {
-        // TMA producer
-        for (int kb = 0; kb < kblocks; ++kb) {
-            const int s = kb % TC_STAGES;
-            if (kb >= TC_STAGES && !mbar_wait_bounded(&empty[s], ((kb / TC_STAGES) - 1) & 1, TC_WAIT)) {
-                atomicExch(&s_abort, 1);
-                break;
+    int issued = 0;                              // TMA stages issued (producer thread)
+    if (warp == 0 && lane == 0) {
+        // TMA producer: the stage ring runs on across tiles
+        for (int t = blockIdx.x; t < total && !aborted(); t += gridDim.x) {
+            int mt, nt;
+            tile_coords(t, mtiles, ntiles, mt, nt);
+            for (int kb = 0; kb < kblocks; ++kb, ++issued) {
+                const int s = issued % TC_STAGES;
+                if (issued >= TC_STAGES &&
+                    !mbar_wait_bounded(&empty[s], (uint32_t)((issued / TC_STAGES) - 1) & 1u, TC_WAIT)) {
+                    atomicExch(&s_abort, 1);
+                    break;
+                }
+                if (aborted()) break;
+                const uint32_t sa = base + s * TC_STAGE_BYTES;
+                mbar_arrive_expect_tx(&full[s], TC_STAGE_BYTES);
+                tma_load_2d(sa, &map_a, kb * TC_BK, mt * TC_BM, smem_addr(&full[s]));
+                tma_load_2d(sa + TC_A_BYTES, &map_b, kb * TC_BK, nt * TC_BN, smem_addr(&full[s]));
             }
-            if (*(volatile int*)&s_abort) break;
-            const uint32_t sa = base + s * TC_STAGE_BYTES;
-            mbar_arrive_expect_tx(&full[s], TC_STAGE_BYTES);
-            tma_load_2d(sa, &map_a, kb * TC_BK, m0, smem_addr(&full[s]));
-            tma_load_2d(sa + TC_A_BYTES, &map_b, kb * TC_BK, n0, smem_addr(&full[s]));
         }
-    } else if (threadIdx.x == 64) {
-        // MMA issuer
+    } else if (warp == 1 && lane == 0) {
+        // MMA issuer: tile j of this CTA accumulates into TMEM columns (j & 1) * 256
         const uint32_t idesc = idesc_bf16(TC_BM, TC_BN);
-        int kb = 0;
-        for (; kb < kblocks; ++kb) {
-            const int s = kb % TC_STAGES;
-            if (!mbar_wait_bounded(&full[s], (kb / TC_STAGES) & 1, TC_WAIT)) {
+        int it = 0, local = 0;
+        for (int t = blockIdx.x; t < total && !aborted(); t += gridDim.x, ++local) {
+            const int b = local & 1;
+            if (local >= 2 && !mbar_wait_bounded(&tempty[b], (uint32_t)((local >> 1) - 1) & 1u, TC_WAIT)) {
                 atomicExch(&s_abort, 1);
                 break;
             }
             tc_fence_after();
-            const uint32_t sa = base + s * TC_STAGE_BYTES;
-            const uint64_t adesc = sw128_desc(sa), bdesc = sw128_desc(sa + TC_A_BYTES);
+            const uint32_t acc_addr = tmem + (uint32_t)(b * TC_BN);
+            bool ok = true;
+            for (int kb = 0; kb < kblocks; ++kb, ++it) {
+                const int s = it % TC_STAGES;
+                if (!mbar_wait_bounded(&full[s], (uint32_t)(it / TC_STAGES) & 1u, TC_WAIT)) {
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t sa = base + s * TC_STAGE_BYTES;
+                const uint64_t adesc = sw128_desc(sa), bdesc = sw128_desc(sa + TC_A_BYTES);
 #pragma unroll
-            for (int k = 0; k < TC_BK / 16; ++k)   // K = 16 per instruction: +32 bytes
-                mma_bf16(tmem, adesc + 2 * k, bdesc + 2 * k, idesc, (kb > 0 || k > 0) ? 1u : 0u);
-            mma_commit(smem_addr(&empty[s]));
-        }
-        mma_commit(smem_addr(done));           // fires when every issued MMA has completed
-    }
-    __syncwarp();
-    // epilogue: thread = chain row (TMEM lane), sums over the tile's observations
-    const bool waited = mbar_wait_bounded(done, 0, TC_WAIT);
-    // tcgen05.ld is warp-collective: decide for the whole CTA
-    const int ok = __syncthreads_and(waited && !*(volatile int*)&s_abort);
-    tc_fence_after();
-    const int chain = m0 + warp * 32 + lane;
-    double acc = 0.0;
-    if (ok) {
-        const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
-#pragma unroll 1
-        for (int c0 = 0; c0 < TC_BN; c0 += 32) {
-            float v[32];
-            tmem_ld32(tmem + lane_base + (uint32_t)c0, v);
-            float s = 0.f;
-#pragma unroll
-            for (int i = 0; i < 32; ++i) {
-                const float r = v[i] + s_rho[c0 + i];
-                s = (n0 + c0 + i < m_obs) ? fmaf(r, r, s) : s;
+                for (int k = 0; k < TC_BK / 16; ++k)   // K = 16 per instruction: +32 bytes
+                    mma_bf16(acc_addr, adesc + 2 * k, bdesc + 2 * k, idesc, (kb > 0 || k > 0) ? 1u : 0u);
+                mma_commit(smem_addr(&empty[s]));
             }
-            acc += (double)s;
+            if (!ok) {
+                atomicExch(&s_abort, 1);
+                break;
+            }
+            mma_commit(smem_addr(&tfull[b]));    // fires when this tile's MMAs have completed
         }
-        if (chain < n) partial[(size_t)blockIdx.y * n + chain] = acc;
-    } else if (threadIdx.x == 0) {
-        raise_flag(flags, DEV_ERR_TIMEOUT);
+        mma_commit(smem_addr(drain));            // fires when every issued MMA has completed
+    } else if (warp >= 2) {
+        // epilogue: thread = chain row (TMEM lane quarter of this warp), sums over observations
+        const int quarter = warp & 3;
+        const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
+        int local = 0;
+        for (int t = blockIdx.x; t < total; t += gridDim.x, ++local) {
+            const int b = local & 1;
+            const bool ok = __all_sync(0xffffffffu,
+                                       mbar_wait_bounded(&tfull[b], (uint32_t)(local >> 1) & 1u, TC_WAIT));
+            if (!ok || aborted()) {
+                if (lane == 0) atomicExch(&s_abort, 1);
+                break;
+            }
+            tc_fence_after();
+            int mt, nt;
+            tile_coords(t, mtiles, ntiles, mt, nt);
+            const int n0 = nt * TC_BN;
+            const int chain = mt * TC_BM + quarter * 32 + lane;
+            double acc = 0.0;
+#pragma unroll 1
+            for (int c0 = 0; c0 < TC_BN; c0 += 64) {
+                // two 32-column loads in flight per wait; lane l holds ρ₀ of observation
+                // n0 + c0 + l (and + 32), broadcast by shuffles
+                uint32_t r0[32], r1[32];
+                tmem_ld32_nowait(tmem + lane_base + (uint32_t)(b * TC_BN + c0), r0);
+                tmem_ld32_nowait(tmem + lane_base + (uint32_t)(b * TC_BN + c0 + 32), r1);
+                const int obs_l = n0 + c0 + lane;
+                const float rho_a = (obs_l < m_obs) ? __ldg(rho0 + obs_l) : 0.f;
+                const float rho_b = (obs_l + 32 < m_obs) ? __ldg(rho0 + obs_l + 32) : 0.f;
+                tmem_wait_ld();
+                float sq = 0.f;
+#pragma unroll
+                for (int i = 0; i < 32; ++i) {
+                    const float r = __uint_as_float(r0[i]) + __shfl_sync(0xffffffffu, rho_a, i);
+                    sq = (n0 + c0 + i < m_obs) ? fmaf(r, r, sq) : sq;
+                }
+                acc += (double)sq;
+                sq = 0.f;
+#pragma unroll
+                for (int i = 0; i < 32; ++i) {
+                    const float r = __uint_as_float(r1[i]) + __shfl_sync(0xffffffffu, rho_b, i);
+                    sq = (n0 + c0 + 32 + i < m_obs) ? fmaf(r, r, sq) : sq;
+                }
+                acc += (double)sq;
+            }
+            if (chain < n) partial[(size_t)nt * n + chain] = acc;
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&tempty[b]);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && aborted()) raise_flag(flags, DEV_ERR_TIMEOUT);
+    if (warp == 0 && lane == 0 && aborted()) {
+        // copies still in flight land before the CTA's shared memory goes away
+        for (int k = (issued > TC_STAGES ? issued - TC_STAGES : 0); k < issued; ++k)
+            mbar_wait_bounded(&full[k % TC_STAGES], (uint32_t)(k / TC_STAGES) & 1u, TC_WAIT);
+    }
+    if (warp == 1) {
+        // every MMA this CTA issued has completed before TMEM is released
+        mbar_wait_bounded(drain, 0, TC_WAIT);
     }
     tc_fence_before();
     __syncthreads();
     if (warp == 0) {
         tc_fence_after();
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_BN) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * TC_BN) : "memory");
     }
 }
 
@@ -207,18 +290,19 @@ __global__ void whiten_rho0_kernel(const double* __restrict__ W, const double* _
 }
 
 // θ₀ = column means of θ (one thread per parameter, fixed order)
-// Column means in two passes with a fixed summation order: block (c, ·) sums rows
-// [c·kMeanRows, (c+1)·kMeanRows) of its columns (threads over columns: coalesced rows),
-// then one thread per column adds the chunk sums in chunk order.
-constexpr int kMeanRows = 128;
+// Column means in two passes with a fixed summation order: block (c, ·) sums a chunk
+// of consecutive rows of its columns (threads over columns: coalesced rows), then one
+// thread per column adds the chunk sums in chunk order.  At most kMeanChunks chunks.
+constexpr int kMeanChunks = 256;
 static inline int cdiv(long a, long b) { return (int)((a + b - 1) / b); }
+static inline int mean_rows(int n) { return cdiv(n, kMeanChunks) > 32 ? cdiv(n, kMeanChunks) : 32; }
 
 template <class T>
-__global__ void colsum_partial_kernel(const T* __restrict__ x, int ld, int col0, int n, int cols,
+__global__ void colsum_partial_kernel(const T* __restrict__ x, int ld, int col0, int n, int cols, int rows,
                                       double* __restrict__ part) {
     const int j = blockIdx.y * blockDim.x + threadIdx.x;
     if (j >= cols) return;
-    const int r0 = blockIdx.x * kMeanRows, r1 = min(n, r0 + kMeanRows);
+    const int r0 = blockIdx.x * rows, r1 = min(n, r0 + rows);
     double s = 0.0;
     for (int i = r0; i < r1; ++i) s += (double)x[(size_t)i * ld + col0 + j];
     part[(size_t)blockIdx.x * cols + j] = s;
@@ -236,8 +320,9 @@ __global__ void colsum_final_kernel(const double* __restrict__ part, int nchunks
 template <class T>
 static void column_means(const T* x, int ld, int col0, int n, int cols, double* part, double* mean,
                          cudaStream_t s) {
-    const int nchunks = cdiv(n, kMeanRows);
-    colsum_partial_kernel<T><<<dim3(nchunks, cdiv(cols, 256)), 256, 0, s>>>(x, ld, col0, n, cols, part);
+    const int rows = mean_rows(n);
+    const int nchunks = cdiv(n, rows);
+    colsum_partial_kernel<T><<<dim3(nchunks, cdiv(cols, 256)), 256, 0, s>>>(x, ld, col0, n, cols, rows, part);
     colsum_final_kernel<<<cdiv(cols, 256), 256, 0, s>>>(part, nchunks, cols, n, mean);
 }
 
@@ -359,6 +444,15 @@ static int make_map(CUtensorMap* map, const void* ptr_, int rows, int cols, int 
     return AG_OK;
 }
 
+// multiprocessors of the current device (persistent grid size)
+static int sm_count(int* out) {
+    int dev = 0;
+    int rc = cuda_status(cudaGetDevice(&dev), "cudaGetDevice");
+    if (rc) return rc;
+    return cuda_status(cudaDeviceGetAttribute(out, cudaDevAttrMultiProcessorCount, dev),
+                       "cudaDeviceGetAttribute(multiProcessorCount)");
+}
+
 }  // namespace ag
 
 using namespace ag;
@@ -380,7 +474,7 @@ extern "C" size_t ag_linear_workspace_bytes(int32_t m, int32_t p, int32_t n) {
     const size_t kp = ag_linear_kpad(p);
     return al256(p * sizeof(double)) + al256((size_t)m * sizeof(float)) +
            al256((size_t)n * 3 * kp * 2) + al256((size_t)cdiv(m, TC_BN) * n * sizeof(double)) +
-           al256((size_t)cdiv(n, kMeanRows) * p * sizeof(double));
+           al256((size_t)kMeanChunks * p * sizeof(double));
 }
 
 extern "C" int ag_linear_llk(const ag_linear_model* lm, const double* theta, int32_t n, double norm,
@@ -420,8 +514,12 @@ extern "C" int ag_linear_llk(const ag_linear_model* lm, const double* theta, int
         if (rc) return rc;
         attr = true;
     }
-    dim3 grid(cdiv(n, TC_BM), tiles);
-    linear_misfit_tc_kernel<<<grid, 128, TC_SMEM, s>>>(ma, mb, n, m, 3 * kp / TC_BK, rho0, partial, flags);
+    const int mtiles = cdiv(n, TC_BM), total = mtiles * tiles;
+    int sms = 0;
+    rc = sm_count(&sms);
+    if (rc) return rc;
+    linear_misfit_tc_kernel<<<total < sms ? total : sms, TC_THREADS, TC_SMEM, s>>>(
+        ma, mb, n, m, 3 * kp / TC_BK, mtiles, tiles, rho0, partial, flags);
     rc = launch_status("linear_misfit_tc_kernel");
     if (rc) return rc;
     linear_reduce_kernel<<<cdiv(n, 256), 256, 0, s>>>(n, tiles, partial, norm, llk, 0);
@@ -433,7 +531,7 @@ extern "C" size_t ag_whiten_workspace_bytes(int32_t m, int32_t n) {
     const size_t kp = ag_linear_kpad(m);
     return al256(m * sizeof(double)) + al256(sizeof(double)) + al256((size_t)m * sizeof(float)) +
            al256((size_t)n * 3 * kp * 2) + al256((size_t)cdiv(m, TC_BN) * n * sizeof(double)) +
-           al256((size_t)cdiv(n, kMeanRows) * m * sizeof(double));
+           al256((size_t)kMeanChunks * m * sizeof(double));
 }
 
 extern "C" int ag_whiten_llk(const ag_whiten_block* blk, const float* resid, int32_t ldr, int32_t n,
@@ -475,8 +573,12 @@ extern "C" int ag_whiten_llk(const ag_whiten_block* blk, const float* resid, int
     whiten_rho0_kernel<<<cdiv((long)m * 32, 256), 256, 0, s>>>(blk->w64, mean, m, rho0);
     rc = launch_status("whiten_rho0_kernel");
     if (rc) return rc;
-    dim3 grid(cdiv(n, TC_BM), tiles);
-    linear_misfit_tc_kernel<<<grid, 128, TC_SMEM, s>>>(ma, mb, n, m, 3 * kp / TC_BK, rho0, partial, flags);
+    const int mtiles = cdiv(n, TC_BM), total = mtiles * tiles;
+    int sms = 0;
+    rc = sm_count(&sms);
+    if (rc) return rc;
+    linear_misfit_tc_kernel<<<total < sms ? total : sms, TC_THREADS, TC_SMEM, s>>>(
+        ma, mb, n, m, 3 * kp / TC_BK, mtiles, tiles, rho0, partial, flags);
     rc = launch_status("linear_misfit_tc_kernel (whitening)");
     if (rc) return rc;
     linear_reduce_kernel<<<cdiv(n, 256), 256, 0, s>>>(n, tiles, partial, 0.0, llk, 1);
