@@ -577,9 +577,9 @@ def run_ours(args):
                                     "(MEASURED_PEAKS.json has no FP32 figure)"},
         "e2e": {"value": world * N * S / t_e2e, "unit": "chain-steps/s", "h2d_bytes_per_step": io_bytes,
                 "d2h_bytes_per_step": io_bytes},
-        # per stage: 28 COV schedule + 2 Σ + 5 resampling + cholesky + adapt, and per Metropolis
+        # per stage: 28 COV schedule + 3 Σ + 5 resampling + cholesky + adapt, and per Metropolis
         # step propose, CDM set-up, CDM likelihood, accept
-        "gpu_launches": (37 + 4 * S) * args.steps,
+        "gpu_launches": (38 + 4 * S) * args.steps,
         "cpu_baseline": {"value": cpu_rate, "unit": "chain-steps/s", "cores": cores, "kind": "port",
                          "sample": f"{args.cpu_chains} chains x {X.size} stations, likelihood only, "
                                    f"{cpu_dt:.1f} s (FP64 C restatement of models/cdm/cdm/libcdm.py)"},

@@ -116,6 +116,30 @@ def test_cdm_launch_variants_identical(cuda):
         np.testing.assert_array_equal(llk, llk0, err_msg=f"variant {v}")
 
 
+def test_cdm_degenerate_axes(cuda):
+    """The reference's special cases (libcdm.py:226-242): one zero semi-axis leaves a single
+    rectangle, all three zero give no displacement; a rotation by 0 makes four sides
+    exactly vertical, which contribute nothing (libcdm.py:320-324)."""
+    g = np.linspace(-20e3, 20e3, 200)[::8]
+    X, Y = [a.ravel() for a in np.meshgrid(g, g)]
+    los = np.tile(LOS, (X.size, 1))
+    # x, y, depth, opening, ax, ay, az, ωx, ωy, ωz
+    theta = np.array([
+        [1e3, -2e3, 5e3, 10.0, 0.0, 1500.0, 800.0, 20.0, -35.0, 60.0],     # ax = 0
+        [1e3, -2e3, 5e3, 10.0, 1200.0, 0.0, 800.0, 20.0, -35.0, 60.0],     # ay = 0
+        [1e3, -2e3, 5e3, 10.0, 1200.0, 1500.0, 0.0, 20.0, -35.0, 60.0],    # az = 0
+        [1e3, -2e3, 5e3, 10.0, 0.0, 0.0, 0.0, 20.0, -35.0, 60.0],          # point: no displacement
+        [-3e3, 4e3, 6e3, -8.0, 900.0, 1100.0, 700.0, 0.0, 0.0, 30.0],      # vertical sides
+    ])
+    strat, _ = cdm_strategy(X, Y, los, np.zeros(X.size), np.full(X.size, 9e-6))
+    _, res = _residuals(strat, theta, X.size)
+    ref = cdm_los_oracle(theta, X, Y, los)
+    assert np.all(res[3] == 0.0) and np.all(ref[3] == 0.0)
+    for k in (0, 1, 2, 4):
+        err = np.max(np.abs(res[k] - ref[k])) / np.max(np.abs(ref[k]))
+        assert err <= TOL_CDM, (k, err)
+
+
 def test_cdm_llk_given_residuals(cuda):
     rng = np.random.default_rng(2)
     g = np.linspace(-20e3, 20e3, 40)
