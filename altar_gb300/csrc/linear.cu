@@ -506,14 +506,11 @@ extern "C" int ag_linear_llk(const ag_linear_model* lm, const double* theta, int
     if (rc) return rc;
     rc = make_map(&mb, lm->a_split, m, 3 * kp, TC_BN);
     if (rc) return rc;
-    static bool attr = false;
-    if (!attr) {
-        rc = cuda_status(cudaFuncSetAttribute(linear_misfit_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              (int)TC_SMEM),
-                         "cudaFuncSetAttribute(linear_misfit_tc_kernel)");
-        if (rc) return rc;
-        attr = true;
-    }
+    // per call: the attribute belongs to the current device's context
+    rc = cuda_status(cudaFuncSetAttribute(linear_misfit_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)TC_SMEM),
+                     "cudaFuncSetAttribute(linear_misfit_tc_kernel)");
+    if (rc) return rc;
     const int mtiles = cdiv(n, TC_BM), total = mtiles * tiles;
     int sms = 0;
     rc = sm_count(&sms);

@@ -199,7 +199,18 @@ def cdm_psets():
     return {nm: Contiguous(c, Uniform(b)) for nm, c, b in zip(names, counts, bounds)}
 
 
-def anneal(kind, X, Y, los, d, N, rank, args):
+def invariants(th):
+    """Posterior summaries that do not depend on which of the CDM's equivalent
+    parameterisations a run settles in (the same body is described by permuted semi-axes
+    with matching rotations): centroid x, y, depth, opening, and the semi-axes sorted per
+    sample.  Mean and standard deviation of each over the final sample."""
+    a = np.sort(th[:, 4:7], axis=1)
+    q = np.concatenate([th[:, 0:4], a], axis=1)
+    return {"names": ["x", "y", "depth", "opening", "a_min", "a_mid", "a_max"],
+            "mean": q.mean(0).tolist(), "sd": q.std(0).tolist()}
+
+
+def anneal(kind, X, Y, los, d, N, rank, args, seed=1234):
     """One CATMIP run to β = 1 with the plain or the delayed-acceptance sampler."""
     import torch
     from altar_gb300 import Application
@@ -214,7 +225,7 @@ def anneal(kind, X, Y, los, d, N, rank, args):
                                     start_beta=args.da_start_beta, inner=args.da_inner,
                                     outer=args.da_outer)
     model = CDM(cdm_psets(), observations=Observations(X, Y, los, d, SIGMA ** 2), autotune=not args.no_autotune)
-    app = Application(model, job=Job(chains=N, steps=5), rng=RNG(1234 + rank),
+    app = Application(model, job=Job(chains=N, steps=5), rng=RNG(seed + rank),
                       controller=Annealer(sampler=sampler))
     app.initialize()
     torch.cuda.synchronize()
@@ -231,6 +242,7 @@ def anneal(kind, X, Y, los, d, N, rank, args):
            "chain_steps": steps, "chain_steps_per_s": steps / dt,
            "likelihoods_evaluated": evaluated / max(1, steps),
            "mean": th.mean(0).tolist(), "sd": th.std(0).tolist(),
+           "invariants": invariants(th),
            "acceptance": [r["accepted"] / max(1, r["accepted"] + r["rejected"] + r["unlikely"]) for r in reps],
            "betas": [r["beta"] for r in reps]}
     if kind == "da":
@@ -423,27 +435,38 @@ def run_ours(args):
     bounds = [PRIORS[0], PRIORS[2], PRIORS[3], PRIORS[4], PRIORS[7]]
     psets = {nm: Contiguous(c, Uniform(b)) for nm, c, b in zip(names, counts, bounds)}
     if args.mode in ("anneal", "compare"):
-        runs = ["plain", "da"] if args.mode == "compare" else [args.sampler]
+        kinds = ["plain", "da"] if args.mode == "compare" else [args.sampler]
         out = {}
-        for kind in runs:
-            out[kind] = anneal(kind, X, Y, los, d, N, rank, args)
+        for seed in args.seeds:
+            for kind in kinds:
+                out[f"{kind}_s{seed}"] = anneal(kind, X, Y, los, d, N, rank, args, seed=seed)
         for extra in args.da_variants:
             inner, outer = (int(v) for v in extra.split("x"))
             args.da_inner, args.da_outer = inner, outer
-            out[f"da_{inner}x{outer}"] = anneal("da", X, Y, los, d, N, rank, args)
+            out[f"da_{inner}x{outer}_s{args.seeds[0]}"] = anneal("da", X, Y, los, d, N, rank, args,
+                                                                seed=args.seeds[0])
         line = {"metric": "CDM time-to-beta=1", "unit": "s", "n_gpus": world, "higher_is_better": False,
                 "config": {"workload": "cdm-40k-obs", "chains": N, "stations": X.size, "steps_per_stage": 5,
-                           "truth": truth.tolist()},
+                           "truth": truth.tolist(), "seeds": args.seeds,
+                           "da": {"inner": args.da_inner, "outer": args.da_outer,
+                                  "delta_limit": args.delta_limit, "rms_limit": args.rms_limit}},
                 "runs": out}
-        if "plain" in out and "da" in out:
-            a, b = out["plain"], out["da"]
-            line["value"] = b["time_s"]
-            line["speedup_da_vs_plain"] = a["time_s"] / b["time_s"]
-            sd = np.array(a["sd"])
-            line["posterior_mean_diff_in_sd"] = (np.abs(np.array(a["mean"]) - np.array(b["mean"])) /
-                                                 np.where(sd > 0, sd, 1)).tolist()
+        if args.mode == "compare":
+            tp = sum(out[f"plain_s{s_}"]["time_s"] for s_ in args.seeds)
+            td = sum(out[f"da_s{s_}"]["time_s"] for s_ in args.seeds)
+            line["value"] = td / len(args.seeds)
+            line["plain_time_s"] = tp / len(args.seeds)
+            line["speedup_da_vs_plain"] = tp / td
+            # per seed: difference of the mode-independent summaries in plain posterior sd
+            diffs = {}
+            for s_ in args.seeds:
+                a, b = out[f"plain_s{s_}"]["invariants"], out[f"da_s{s_}"]["invariants"]
+                sd = np.array(a["sd"])
+                diffs[str(s_)] = (np.abs(np.array(a["mean"]) - np.array(b["mean"])) /
+                                  np.where(sd > 0, sd, 1)).tolist()
+            line["invariant_mean_diff_in_sd"] = diffs
         else:
-            line["value"] = out[runs[0]]["time_s"]
+            line["value"] = out[f"{kinds[0]}_s{args.seeds[0]}"]["time_s"]
         if rank == 0:
             print(json.dumps(line))
         return 0
@@ -614,11 +637,13 @@ def main():
                     help="stations of the three datasets of --mode dense")
     ap.add_argument("--no-full-run", dest="full_run", action="store_false",
                     help="skip the whole plain run to beta = 1 after the timed stages")
-    ap.add_argument("--da-inner", type=int, default=1)
-    ap.add_argument("--da-outer", type=int, default=None)
+    ap.add_argument("--da-inner", type=int, default=10, help="surrogate moves per exact correction")
+    ap.add_argument("--da-outer", type=int, default=1, help="exact corrections per stage")
     ap.add_argument("--da-variants", nargs="*", default=[], help="extra DA runs as INNERxOUTER, e.g. 5x2")
+    ap.add_argument("--seeds", type=int, nargs="+", default=[1234],
+                    help="random seeds of the compare/anneal runs (one plain and one DA run per seed)")
     ap.add_argument("--rms-limit", type=float, default=0.5)
-    ap.add_argument("--delta-limit", type=float, default=1.0)
+    ap.add_argument("--delta-limit", type=float, default=2.0)
     ap.add_argument("--epochs", type=int, default=40)
     ap.add_argument("--chains", type=int, default=32768)
     ap.add_argument("--cpu-chains", type=int, default=128)

@@ -47,7 +47,9 @@ def oracle_llk(G, d, Cd, theta):
     return -0.5 * (d.size * math.log(2 * math.pi) + logdet) - 0.5 * np.einsum("ij,ji->i", r, sol)
 
 
-@pytest.mark.parametrize("m,p,n", [(512, 64, 384), (1024, 256, 1024), (777, 100, 300)])
+# the last case has 1,024 tiles of 128 chains x 256 observations: each persistent CTA takes
+# several tiles and reuses both TMEM accumulators
+@pytest.mark.parametrize("m,p,n", [(512, 64, 384), (1024, 256, 1024), (777, 100, 300), (2048, 64, 16384)])
 def test_linear_llk_tensor_cores(cuda, m, p, n):
     G, d, Cd, truth = problem(m, p)
     rng = np.random.default_rng(1)
