@@ -9,6 +9,7 @@ later stages; the host only reads β (and the stage report) once per stage.
 """
 import ctypes
 import logging
+import time
 
 import torch
 
@@ -101,7 +102,8 @@ class CUDAAnnealing:
     def bottom(self, annealer):
         scal, cnt, flags = (t.cpu() for t in self._last)
         acc, rej, unl = (int(v) for v in cnt)
-        rep = {"stage": self.iteration, "beta": float(scal[0]), "dbeta": float(scal[1]),
+        rep = {"stage": self.iteration, "time": time.perf_counter(), "beta": float(scal[0]),
+               "dbeta": float(scal[1]),
                "cov": float(scal[2]), "scaling": float(self.step.state.scaling.item()),
                "accepted": acc, "rejected": rej, "unlikely": unl, "flags": int(flags[0])}
         rep.update(annealer.sampler.report())

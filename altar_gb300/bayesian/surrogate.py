@@ -24,6 +24,7 @@ surrogate posterior and evaluates the exact model only on the survivors
 """
 import ctypes
 import math
+import time
 
 import numpy as np
 import torch
@@ -31,6 +32,19 @@ import torch
 from .. import _native
 from ..device import DEVICE, ptr, stream_handle, workspace
 from .metropolis import Metropolis
+
+
+def _orthonormal_columns(Y):
+    """Orthonormal basis of the columns of a tall FP64 matrix by Cholesky QR, twice
+    (Fukaya et al. 2014): the Gram matrices are (k+o) x (k+o) and are factored on the
+    host, so no dense solver library runs on the device."""
+    for _ in range(2):
+        G = (Y.T @ Y).cpu().numpy()
+        G += np.eye(G.shape[0]) * (1e-14 * np.trace(G) / G.shape[0] + 1e-300)
+        R = np.linalg.cholesky(G).T                                # G = Rᵀ R
+        Rinv = np.linalg.solve(R, np.eye(R.shape[0]))
+        Y = Y @ torch.from_numpy(Rinv).to(Y.device)
+    return Y
 
 
 class Surrogate:
@@ -83,12 +97,14 @@ class Surrogate:
         gen = torch.Generator(device=DEVICE)
         gen.manual_seed(self.seed + 7)
         omega = torch.randn(F.shape[1], k + oversample, device=DEVICE, generator=gen)
-        Q, _ = torch.linalg.qr(Fc @ omega)                         # (S, k+o) range of the fields
-        Bt = (Q.T @ Fc).double()                                   # (k+o, Mp)
-        evals, evecs = torch.linalg.eigh(Bt @ Bt.T)
-        idx = torch.argsort(evals, descending=True)[:k]
-        lam = evals[idx].clamp_min(1e-30)
-        B = (Bt.T @ evecs[:, idx]) / torch.sqrt(lam)              # orthonormal columns (Mp, k)
+        Q = _orthonormal_columns((Fc @ omega).double())            # (S, k+o) range of the fields
+        Bt = (Q.float().T @ Fc).double()                           # (k+o, Mp)
+        # the small (k+o) x (k+o) eigenproblem on the host
+        evals, evecs = np.linalg.eigh((Bt @ Bt.T).cpu().numpy())
+        order = np.argsort(evals)[::-1][:k]
+        lam = torch.from_numpy(np.maximum(evals[order], 1e-30).copy()).to(DEVICE)
+        V = torch.from_numpy(np.ascontiguousarray(evecs[:, order])).to(DEVICE)
+        B = (Bt.T @ V) / torch.sqrt(lam)                           # orthonormal columns (Mp, k)
         # one common scale (the leading component's spread): the training loss in
         # normalised coefficients is then proportional to the field-space error, so
         # noise-level components cannot dominate it
@@ -215,6 +231,7 @@ class DelayedAcceptance(Metropolis):
         super().__init__(**kwds)
         self.delta_limit = float(delta_limit)
         self.delta = None
+        self._prepare_s = 0.0
         self._backoff = 0
         self.inner = int(inner)
         self.outer = None if outer is None else int(outer)
@@ -235,25 +252,32 @@ class DelayedAcceptance(Metropolis):
 
     def initialize(self, application):
         super().initialize(application)
-        # load the dense linear-algebra libraries the refits use (QR, symmetric eigensolver)
-        # now, so that their one-time start-up does not land inside the first refit
-        a = torch.eye(8, dtype=torch.float64, device=DEVICE)
-        torch.linalg.qr(a.float())
-        torch.linalg.eigh(a)
-        torch.cuda.synchronize()
+        # start the device BLAS the refits use now, so that its one-time set-up does not
+        # land inside the first refit
+        for dt in (torch.float32, torch.float64):
+            a = torch.ones(64, 64, dtype=dt, device=DEVICE)
+            (a @ a).sum().item()
         return self
 
     def mode_key(self):
         return self.mode
 
     def report(self):
-        rep = {"mode": self.mode, "rms_sigma": self.rms, "delta_sd": self.delta, "refits": self.refits}
+        rep = {"mode": self.mode, "rms_sigma": self.rms, "delta_sd": self.delta, "refits": self.refits,
+               "prepare_s": self._prepare_s}
         if self.mode == "da" and self.screened is not None:
             rep["screened"] = int(self.screened.item())
         return rep
 
     # ---- per-stage host decisions (eager, before the walk graph)
     def prepare(self, annealer, step):
+        t0 = time.perf_counter()
+        try:
+            return self._prepare(annealer, step)
+        finally:
+            self._prepare_s = time.perf_counter() - t0
+
+    def _prepare(self, annealer, step):
         self._stage += 1
         if self.screened is not None:
             self.screened.zero_()
