@@ -215,7 +215,8 @@ class DelayedAcceptance(Metropolis):
     """Metropolis with a surrogate screen (stage 1) before the exact model (stage 2)."""
 
     def __init__(self, surrogate=None, rms_limit=0.5, delta_limit=2.0, fit_chains=4096, check_chains=256,
-                 epochs=40, start_beta=0.0, retry_every=3, spread=3.0, inner=10, outer=1, **kwds):
+                 epochs=40, start_beta=0.0, stop_beta=0.1, retry_every=3, spread=3.0, inner=10, outer=1,
+                 **kwds):
         """rms_limit: largest RMS field error (data standard deviations) of a usable surrogate;
         delta_limit: largest spread (standard deviation over trial proposals) of the error of
         the surrogate's tempered log-posterior ratio, β[(s(y) - s(x)) - (l(y) - l(x))].  Delayed
@@ -225,9 +226,12 @@ class DelayedAcceptance(Metropolis):
         inner: surrogate Metropolis moves per exact correction (1 = two-stage delayed
         acceptance; k > 1 = surrogate-transition proposals, Liu 2001, corrected by the same
         exact second stage); outer: exact corrections per stage in the surrogate mode
-        (None: the job's steps).  The defaults (10 surrogate moves, one exact correction
-        per stage, ratio spread up to 2) were the fastest setting measured on the CDM
-        workload at an unchanged posterior."""
+        (None: the job's steps).  start_beta, stop_beta: the surrogate is used only for
+        start_beta <= β < stop_beta; the stages after stop_beta walk exactly, which lets
+        the final population relax with the exact kernel alone.  The defaults (10 surrogate
+        moves and one exact correction per stage, ratio spread up to 2, exact stages from
+        β = 0.1) were the fastest setting measured on the CDM workload whose posterior
+        summaries matched plain Metropolis to within its own run-to-run spread."""
         super().__init__(**kwds)
         self.delta_limit = float(delta_limit)
         self.delta = None
@@ -238,7 +242,7 @@ class DelayedAcceptance(Metropolis):
         self.surrogate = surrogate if surrogate is not None else Surrogate(batch=1024)
         self.rms_limit = float(rms_limit)
         self.fit_chains, self.check_chains = int(fit_chains), int(check_chains)
-        self.epochs, self.start_beta = int(epochs), float(start_beta)
+        self.epochs, self.start_beta, self.stop_beta = int(epochs), float(start_beta), float(stop_beta)
         self.retry_every, self.spread = int(retry_every), float(spread)
         self.mode = "plain"
         self.rms = None
@@ -281,7 +285,8 @@ class DelayedAcceptance(Metropolis):
         self._stage += 1
         if self.screened is not None:
             self.screened.zero_()
-        if step.beta < self.start_beta:
+        beta = step.beta
+        if beta < self.start_beta or beta >= self.stop_beta:
             self.mode = "plain"
             return self
         model, strat = annealer.model, annealer.model.strategy

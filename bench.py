@@ -222,7 +222,8 @@ def anneal(kind, X, Y, los, d, N, rank, args, seed=1234, max_stages=None):
     if kind == "da":
         sampler = DelayedAcceptance(surrogate=Surrogate(seed=5, batch=1024), rms_limit=args.rms_limit,
                                     delta_limit=args.delta_limit, epochs=args.epochs,
-                                    start_beta=args.da_start_beta, inner=args.da_inner,
+                                    start_beta=args.da_start_beta, stop_beta=args.da_stop_beta,
+                                    inner=args.da_inner,
                                     outer=args.da_outer)
     model = CDM(cdm_psets(), observations=Observations(X, Y, los, d, SIGMA ** 2), autotune=not args.no_autotune)
     app = Application(model, job=Job(chains=N, steps=5), rng=RNG(seed + rank),
@@ -454,7 +455,8 @@ def run_ours(args):
                 "config": {"workload": "cdm-40k-obs", "chains": N, "stations": X.size, "steps_per_stage": 5,
                            "truth": truth.tolist(), "seeds": args.seeds,
                            "da": {"inner": args.da_inner, "outer": args.da_outer,
-                                  "delta_limit": args.delta_limit, "rms_limit": args.rms_limit}},
+                                  "delta_limit": args.delta_limit, "rms_limit": args.rms_limit,
+                                  "stop_beta": args.da_stop_beta}},
                 "runs": out, "untimed_warmup_s": warm}
         if args.mode == "compare":
             tp = sum(out[f"plain_s{s_}"]["time_s"] for s_ in args.seeds)
@@ -636,6 +638,7 @@ def main():
     ap.add_argument("--sampler", default="plain", choices=["plain", "da"])
     ap.add_argument("--max-stages", type=int, default=400)
     ap.add_argument("--da-start-beta", type=float, default=0.0)
+    ap.add_argument("--da-stop-beta", type=float, default=0.1)
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--variant", type=int, default=None, help="force one CDM launch variant (no autotuning)")
     ap.add_argument("--dense-sizes", type=int, nargs=3, default=[12000, 30000, 7500],
