@@ -204,7 +204,7 @@ def test_delayed_acceptance_posterior(cuda):
     plain = run(None, 7)
     sur = Surrogate((4, 128, 128, 32), seed=2, batch=512, lr=2e-3)
     da = DelayedAcceptance(surrogate=sur, rms_limit=50.0, delta_limit=float("inf"), fit_chains=1024,
-                           check_chains=128, epochs=20, inner=1, outer=None)
+                           check_chains=128, epochs=20, inner=1, outer=None, stop_beta=1.0)
     dw = run(da, 7)
     assert sur.trained and any(r.get("mode") == "da" for r in dw.reports)
     tp, td = plain.step.theta.cpu().numpy(), dw.step.theta.cpu().numpy()
@@ -235,7 +235,7 @@ def test_surrogate_transition_posterior(cuda):
     sur = Surrogate((4, 128, 128, 32), seed=2, batch=512, lr=2e-3)
     da = DelayedAcceptance(surrogate=sur, rms_limit=50.0, delta_limit=float("inf"), fit_chains=1024,
                            check_chains=128, epochs=20,
-                           inner=3, outer=2)
+                           inner=3, outer=2, stop_beta=1.0)
     dw = run(da)
     assert any(r.get("mode") == "da" for r in dw.reports)
     tp, td = plain.step.theta.cpu().numpy(), dw.step.theta.cpu().numpy()
