@@ -654,7 +654,8 @@ def main():
     ap.add_argument("--delta-limit", type=float, default=2.0)
     ap.add_argument("--epochs", type=int, default=40)
     ap.add_argument("--chains", type=int, default=32768)
-    ap.add_argument("--cpu-chains", type=int, default=128)
+    ap.add_argument("--cpu-chains", type=int, default=2048,
+                    help="chains in the bounded CPU sample (about 10 s on 16 host cores)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     if args.impl == "reference":
