@@ -5,8 +5,9 @@
 // covariance is folded once into A = L⁻¹ G and b = L⁻¹ d (Cd = L Lᵀ), so that
 // rᵀ Cd⁻¹ r = |A θ - b|², and each chain's misfit is
 //     ρ = A (θ - θ₀) + ρ₀,   ρ₀ = A θ₀ - b  (FP64, the residual-correction pass),
-// with θ₀ the population mean: the tensor-core product only carries the
-// centred part.  A and δ = θ - θ₀ are split into BF16 pairs (x ≈ hi + lo) and
+// with θ₀ a centre of the population (the mean of up to 256 evenly spaced
+// chains): the tensor-core product only carries the centred part.  A and
+// δ = θ - θ₀ are split into BF16 pairs (x ≈ hi + lo) and
 // the product A δ is one GEMM over the concatenated K axis
 //     [δ_hi | δ_lo | δ_hi] · [A_hi | A_hi | A_lo]ᵀ
 // (three BF16 products, FP32 accumulation; the dropped lo·lo term is
@@ -290,40 +291,35 @@ __global__ void whiten_rho0_kernel(const double* __restrict__ W, const double* _
 }
 
 // θ₀ = column means of θ (one thread per parameter, fixed order)
-// Column means in two passes with a fixed summation order: block (c, ·) sums a chunk
-// of consecutive rows of its columns (threads over columns: coalesced rows), then one
-// thread per column adds the chunk sums in chunk order.  At most kMeanChunks chunks.
-constexpr int kMeanChunks = 256;
+// Centring point θ₀ (or r̄): the mean of up to kCentreRows rows taken at an even stride.
+// Any centre gives the same result, because ρ₀ = A θ₀ - b carries it exactly in FP64;
+// the centre only has to lie inside the population so that the BF16 split of θ - θ₀ keeps
+// its relative precision.  One thread per column, rows in a fixed order.
+constexpr int kCentreRows = 256;
 static inline int cdiv(long a, long b) { return (int)((a + b - 1) / b); }
-static inline int mean_rows(int n) { return cdiv(n, kMeanChunks) > 32 ? cdiv(n, kMeanChunks) : 32; }
 
 template <class T>
-__global__ void colsum_partial_kernel(const T* __restrict__ x, int ld, int col0, int n, int cols, int rows,
-                                      double* __restrict__ part) {
-    const int j = blockIdx.y * blockDim.x + threadIdx.x;
-    if (j >= cols) return;
-    const int r0 = blockIdx.x * rows, r1 = min(n, r0 + rows);
+__global__ void __launch_bounds__(256) centre_kernel(const T* __restrict__ x, int ld, int col0, int n, int cols,
+                                                     double* __restrict__ centre) {
+    // 32 columns per CTA (lanes), the sampled rows split over the 8 warps, then the warp
+    // partial sums added in warp order
+    __shared__ double part[8][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int j = blockIdx.x * 32 + lane;
+    const int rows = n < kCentreRows ? n : kCentreRows;
+    const long stride = n / rows;                      // >= 1
     double s = 0.0;
-    for (int i = r0; i < r1; ++i) s += (double)x[(size_t)i * ld + col0 + j];
-    part[(size_t)blockIdx.x * cols + j] = s;
-}
-
-__global__ void colsum_final_kernel(const double* __restrict__ part, int nchunks, int cols, int n,
-                                    double* __restrict__ mean) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= cols) return;
-    double s = 0.0;
-    for (int c = 0; c < nchunks; ++c) s += part[(size_t)c * cols + j];
-    mean[j] = s / n;
-}
-
-template <class T>
-static void column_means(const T* x, int ld, int col0, int n, int cols, double* part, double* mean,
-                         cudaStream_t s) {
-    const int rows = mean_rows(n);
-    const int nchunks = cdiv(n, rows);
-    colsum_partial_kernel<T><<<dim3(nchunks, cdiv(cols, 256)), 256, 0, s>>>(x, ld, col0, n, cols, rows, part);
-    colsum_final_kernel<<<cdiv(cols, 256), 256, 0, s>>>(part, nchunks, cols, n, mean);
+    if (j < cols) {
+#pragma unroll 4
+        for (int k = warp; k < rows; k += 8) s += (double)__ldg(x + (size_t)(k * stride) * ld + col0 + j);
+    }
+    part[warp][lane] = s;
+    __syncthreads();
+    if (warp == 0 && j < cols) {
+        double t = 0.0;
+        for (int w = 0; w < 8; ++w) t += part[w][lane];
+        centre[j] = t / rows;
+    }
 }
 
 // ρ₀ = A θ₀ - b in FP64 (one warp per observation)
@@ -337,20 +333,30 @@ __global__ void rho0_kernel(const double* __restrict__ A, const double* __restri
     if (lane == 0) rho0[row] = (float)(s - b[row]);
 }
 
-// δ = θ - θ₀ split as [hi | lo | hi] (BF16, row length kp3 = 3 kp, kp = p padded to 64)
-__global__ void split_theta_kernel(const double* __restrict__ theta, const double* __restrict__ theta0,
-                                   int n, int p, int kp, __nv_bfloat16* __restrict__ out) {
+// δ = x - centre split as [hi | lo | hi] (BF16, row length 3 kp, kp = columns padded to
+// 64): one thread per 8 consecutive columns of a row, three 16-byte stores.  Rows of x have
+// stride ld and start at column col0 (θ: ld = p, col0 = 0; a residual block: the residual
+// rows and the block's first column).
+template <class T>
+__global__ void split_centred_kernel(const T* __restrict__ x, int ld, int col0, const double* __restrict__ centre,
+                                     int n, int cols, int kp, __nv_bfloat16* __restrict__ out) {
     const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= (long)n * kp) return;
-    const int i = (int)(e / kp), j = (int)(e % kp);
-    float d = 0.f;
-    if (j < p) d = (float)(theta[(size_t)i * p + j] - theta0[j]);
-    const __nv_bfloat16 hi = __float2bfloat16_rn(d);
-    const __nv_bfloat16 lo = __float2bfloat16_rn(d - __bfloat162float(hi));
+    const int groups = kp >> 3;
+    if (e >= (long)n * groups) return;
+    const int i = (int)(e / groups), j0 = (int)(e % groups) * 8;
+    __align__(16) __nv_bfloat16 hi[8], lo[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const int j = j0 + q;
+        const float d = (j < cols) ? (float)((double)x[(size_t)i * ld + col0 + j] - centre[j]) : 0.f;
+        hi[q] = __float2bfloat16_rn(d);
+        lo[q] = __float2bfloat16_rn(d - __bfloat162float(hi[q]));
+    }
     __nv_bfloat16* row = out + (size_t)i * 3 * kp;
-    row[j] = hi;
-    row[kp + j] = lo;
-    row[2 * kp + j] = hi;
+    const uint4 h = *reinterpret_cast<const uint4*>(hi), l = *reinterpret_cast<const uint4*>(lo);
+    *reinterpret_cast<uint4*>(row + j0) = h;
+    *reinterpret_cast<uint4*>(row + kp + j0) = l;
+    *reinterpret_cast<uint4*>(row + 2 * kp + j0) = h;
 }
 
 // A split as [hi | hi | lo]
@@ -377,21 +383,6 @@ __global__ void linear_reduce_kernel(int n, int tiles, const double* __restrict_
     llk[i] = (accumulate ? llk[i] : norm) - 0.5 * s;
 }
 
-// δ = r - r̄ split as [hi | lo | hi] (BF16), rows of length 3 kp
-__global__ void split_block_kernel(const float* __restrict__ r, int ld, int col0, const double* __restrict__ mean,
-                                   int n, int m, int kp, __nv_bfloat16* __restrict__ out) {
-    const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= (long)n * kp) return;
-    const int i = (int)(e / kp), j = (int)(e % kp);
-    float d = 0.f;
-    if (j < m) d = (float)((double)r[(size_t)i * ld + col0 + j] - mean[j]);
-    const __nv_bfloat16 hi = __float2bfloat16_rn(d);
-    const __nv_bfloat16 lo = __float2bfloat16_rn(d - __bfloat162float(hi));
-    __nv_bfloat16* row = out + (size_t)i * 3 * kp;
-    row[j] = hi;
-    row[kp + j] = lo;
-    row[2 * kp + j] = hi;
-}
 
 
 
@@ -473,8 +464,7 @@ extern "C" size_t ag_linear_workspace_bytes(int32_t m, int32_t p, int32_t n) {
     if (m <= 0 || p <= 0 || n <= 0) return 0;
     const size_t kp = ag_linear_kpad(p);
     return al256(p * sizeof(double)) + al256((size_t)m * sizeof(float)) +
-           al256((size_t)n * 3 * kp * 2) + al256((size_t)cdiv(m, TC_BN) * n * sizeof(double)) +
-           al256((size_t)kMeanChunks * p * sizeof(double));
+           al256((size_t)n * 3 * kp * 2) + al256((size_t)cdiv(m, TC_BN) * n * sizeof(double));
 }
 
 extern "C" int ag_linear_llk(const ag_linear_model* lm, const double* theta, int32_t n, double norm,
@@ -493,12 +483,12 @@ extern "C" int ag_linear_llk(const ag_linear_model* lm, const double* theta, int
     double* theta0 = reinterpret_cast<double*>(ws); ws += al256(p * sizeof(double));
     float* rho0 = reinterpret_cast<float*>(ws); ws += al256((size_t)m * sizeof(float));
     __nv_bfloat16* tsplit = reinterpret_cast<__nv_bfloat16*>(ws); ws += al256((size_t)n * 3 * kp * 2);
-    double* partial = reinterpret_cast<double*>(ws); ws += al256((size_t)cdiv(m, TC_BN) * n * sizeof(double));
-    double* colpart = reinterpret_cast<double*>(ws);
+    double* partial = reinterpret_cast<double*>(ws);
     const int tiles = cdiv(m, TC_BN);
-    column_means(theta, p, 0, n, p, colpart, theta0, s);
+    centre_kernel<double><<<cdiv(p, 32), 256, 0, s>>>(theta, p, 0, n, p, theta0);
     rho0_kernel<<<cdiv((long)m * 32, 256), 256, 0, s>>>(lm->a64, lm->b64, theta0, m, p, rho0);
-    split_theta_kernel<<<cdiv((long)n * kp, 256), 256, 0, s>>>(theta, theta0, n, p, kp, tsplit);
+    split_centred_kernel<double><<<cdiv((long)n * (kp / 8), 256), 256, 0, s>>>(theta, p, 0, theta0, n, p, kp,
+                                                                                tsplit);
     int rc = launch_status("linear prologue kernels");
     if (rc) return rc;
     CUtensorMap ma, mb;
@@ -527,8 +517,7 @@ extern "C" size_t ag_whiten_workspace_bytes(int32_t m, int32_t n) {
     if (m <= 0 || n <= 0) return 0;
     const size_t kp = ag_linear_kpad(m);
     return al256(m * sizeof(double)) + al256(sizeof(double)) + al256((size_t)m * sizeof(float)) +
-           al256((size_t)n * 3 * kp * 2) + al256((size_t)cdiv(m, TC_BN) * n * sizeof(double)) +
-           al256((size_t)kMeanChunks * m * sizeof(double));
+           al256((size_t)n * 3 * kp * 2) + al256((size_t)cdiv(m, TC_BN) * n * sizeof(double));
 }
 
 extern "C" int ag_whiten_llk(const ag_whiten_block* blk, const float* resid, int32_t ldr, int32_t n,
@@ -549,14 +538,14 @@ extern "C" int ag_whiten_llk(const ag_whiten_block* blk, const float* resid, int
     ws += al256(sizeof(double));
     float* rho0 = reinterpret_cast<float*>(ws); ws += al256((size_t)m * sizeof(float));
     __nv_bfloat16* rsplit = reinterpret_cast<__nv_bfloat16*>(ws); ws += al256((size_t)n * 3 * kp * 2);
-    double* partial = reinterpret_cast<double*>(ws); ws += al256((size_t)cdiv(m, TC_BN) * n * sizeof(double));
-    double* colpart = reinterpret_cast<double*>(ws);
+    double* partial = reinterpret_cast<double*>(ws);
     const int tiles = cdiv(m, TC_BN);
-    column_means(resid, ldr, col0, n, m, colpart, mean, s);
+    centre_kernel<float><<<cdiv(m, 32), 256, 0, s>>>(resid, ldr, col0, n, m, mean);
     int rc = launch_status("whitening prologue");
     if (rc) return rc;
-    split_block_kernel<<<cdiv((long)n * kp, 256), 256, 0, s>>>(resid, ldr, col0, mean, n, m, kp, rsplit);
-    rc = launch_status("split_block_kernel");
+    split_centred_kernel<float><<<cdiv((long)n * (kp / 8), 256), 256, 0, s>>>(resid, ldr, col0, mean, n, m, kp,
+                                                                              rsplit);
+    rc = launch_status("split_centred_kernel");
     if (rc) return rc;
     CUtensorMap ma, mb;
     rc = make_map(&ma, rsplit, n, 3 * kp, TC_BM);

@@ -314,8 +314,9 @@ int ag_linear_llk_fp64(const ag_linear_model* model, const double* theta, int32_
  * Dense-Cd whitening of one dataset's residual block (replaces the per-chain
  * L2.withCovariance dtrmv loop, altar/altar/norms/L2.py:39-52, for dense Cd):
  * llk[i] -= 1/2 |W (r_i - r̄) + W r̄|² over the block's columns, with W = L⁻¹
- * (Cd = L Lᵀ), r̄ the mean residual over the chains, W (r - r̄) on the tcgen05
- * tensor cores (split BF16, FP32 accumulation) and W r̄ in FP64.
+ * (Cd = L Lᵀ), r̄ the mean residual of up to 256 evenly spaced chains,
+ * W (r - r̄) on the tcgen05 tensor cores (split BF16, FP32 accumulation) and
+ * W r̄ in FP64.
  */
 typedef struct ag_whiten_block {
     const double* w64;        /* [m][m] FP64 W = L⁻¹ */
