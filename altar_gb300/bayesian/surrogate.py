@@ -215,8 +215,8 @@ class DelayedAcceptance(Metropolis):
     """Metropolis with a surrogate screen (stage 1) before the exact model (stage 2)."""
 
     def __init__(self, surrogate=None, rms_limit=0.5, delta_limit=2.0, fit_chains=4096, check_chains=256,
-                 epochs=40, start_beta=0.0, stop_beta=0.1, retry_every=3, spread=3.0, inner=10, outer=1,
-                 **kwds):
+                 epochs=40, refit_epochs=None, start_beta=0.0, stop_beta=0.1, retry_every=3, spread=3.0,
+                 inner=10, outer=1, **kwds):
         """rms_limit: largest RMS field error (data standard deviations) of a usable surrogate;
         delta_limit: largest spread (standard deviation over trial proposals) of the error of
         the surrogate's tempered log-posterior ratio, β[(s(y) - s(x)) - (l(y) - l(x))].  Delayed
@@ -243,6 +243,8 @@ class DelayedAcceptance(Metropolis):
         self.rms_limit = float(rms_limit)
         self.fit_chains, self.check_chains = int(fit_chains), int(check_chains)
         self.epochs, self.start_beta, self.stop_beta = int(epochs), float(start_beta), float(stop_beta)
+        # later fits start from the previous weights and need fewer passes
+        self.refit_epochs = self.epochs if refit_epochs is None else int(refit_epochs)
         self.retry_every, self.spread = int(retry_every), float(spread)
         self.mode = "plain"
         self.rms = None
@@ -377,7 +379,7 @@ class DelayedAcceptance(Metropolis):
             sur.init_params()
         sur.reserve(th.shape[0], p)
         sur.add(x, sur.coefficients(fields))
-        sur.train(epochs=self.epochs)
+        sur.train(epochs=self.epochs if self.refits == 0 else self.refit_epochs)
         self.refits += 1
 
     def _check(self, annealer, step, rows):

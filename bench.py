@@ -222,6 +222,7 @@ def anneal(kind, X, Y, los, d, N, rank, args, seed=1234, max_stages=None):
     if kind == "da":
         sampler = DelayedAcceptance(surrogate=Surrogate(seed=5, batch=1024), rms_limit=args.rms_limit,
                                     delta_limit=args.delta_limit, epochs=args.epochs,
+                                    refit_epochs=args.refit_epochs,
                                     start_beta=args.da_start_beta, stop_beta=args.da_stop_beta,
                                     inner=args.da_inner,
                                     outer=args.da_outer)
@@ -652,6 +653,7 @@ def main():
                     help="random seeds of the compare/anneal runs (one plain and one DA run per seed)")
     ap.add_argument("--rms-limit", type=float, default=0.5)
     ap.add_argument("--delta-limit", type=float, default=2.0)
+    ap.add_argument("--refit-epochs", type=int, default=None, help="training epochs of every fit after the first")
     ap.add_argument("--epochs", type=int, default=40)
     ap.add_argument("--chains", type=int, default=32768)
     ap.add_argument("--cpu-chains", type=int, default=2048,
