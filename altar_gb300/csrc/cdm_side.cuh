@@ -1,0 +1,452 @@
+// CDM per-side arithmetic: FP64 set-up of the 12 angular-dislocation pairs of
+// a chain (corners, frames, coefficients) and the FP32 evaluation of one pair
+// at a group of stations.  Used by the likelihood kernels in forward.cu; the
+// functions are plain inline code so that the same source can also be compiled
+// for the host to study its rounding.
+//
+// Reference: models/cdm/cdm/libcdm.py:174-242 (corners, active rectangles),
+// libcdm.py:310-372 (angular-dislocation pair of one side, artefact-free
+// configurations I and II), libcdm.py:375-430 (AngDisDisp terms).
+#pragma once
+#include <math.h>
+#include <stdint.h>
+
+#ifndef AG_DEVICE_INLINE
+#define AG_DEVICE_INLINE __device__ __forceinline__
+#endif
+#ifndef AG_CDM_FN
+#define AG_CDM_FN __device__ inline
+#endif
+
+namespace ag {
+
+constexpr int kSides = 12;
+
+// ---------------------------------------------------------------------------
+// per-side constants of one angular-dislocation pair (40 floats).  β is the
+// angle of the side from the downward vertical; "configuration II" values,
+// the per-station sign sg = -1 of configuration I (β - π) is applied in the
+// pair evaluation.  Coefficients of the two log differences carry ln 2 (the
+// logs are evaluated in base 2) and those of the Burgers-function difference
+// carry the factor 2 of Fi = 2 atan2(...).
+struct __align__(16) SideC {
+    float4 q[10];
+};
+// q0: c, s, k1, k2            frame (unit horizontal side direction) and vertex A
+// q1: dy1, aA, aB, da         y1(B) - y1(A); depths of A and B; aB - aA
+// q2: sb, cb, tb2, ctb2       sin β, cos β, tan(β/2), cot(β/2)
+// q3: daS, C1F, C2F, C3F      da·(aA+aB); 2 × coefficients of ΔFi
+// q4: C1P, C2P, kc1, kc2      ln 2 × coefficients of Δlog(r+a); k·cot·b1, k·cot·b2
+// q5: nb1, nb2, hb1, hb2      2ν b1, 2ν b2, k b1/2, k b2/2
+// q6: b1, b2, C1m10, C3m10
+// q7: C1Q, C2Q, C3Q, C1m11    ln 2 × configuration-signed coefficients of Δlog(r-z3)
+// q8: C3m11, C1m12, aAsb, naAcb   aA·sin β, -aA·cos β
+// q9: dz1, dz3, kc2L, 0       Δz1, Δz3 (configuration II); ln 2 · kc2
+
+// Per-side constant by its position in SideC (q[i >> 2], component i & 3)
+enum : int {
+    K_C = 0, K_S, K_K1, K_K2, K_DY1, K_AA, K_AB, K_DA, K_SB, K_CB, K_TB2, K_CTB2, K_DAS, K_C1F, K_C2F, K_C3F,
+    K_C1P, K_C2P, K_KC1, K_KC2, K_NB1, K_NB2, K_HB1, K_HB2, K_B1, K_B2, K_C1M10, K_C3M10, K_C1Q, K_C2Q, K_C3Q,
+    K_C1M11, K_C3M11, K_C1M12, K_AASB, K_NAACB, K_DZ1, K_DZ3, K_KC2L
+};
+
+// ---------------------------------------------------------------------------
+// FP64 per-chain set-up: rotation, corners, geometry check, per-side constants
+struct Vec3 { double x, y, z; };
+AG_CDM_FN Vec3 v_sub(Vec3 a, Vec3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+AG_CDM_FN Vec3 v_add(Vec3 a, Vec3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+AG_CDM_FN Vec3 v_scale(Vec3 a, double s) { return {a.x * s, a.y * s, a.z * s}; }
+AG_CDM_FN Vec3 v_cross(Vec3 a, Vec3 b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+AG_CDM_FN double v_dot(Vec3 a, Vec3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+
+AG_CDM_FN void split_hilo(double v, float& hi, float& lo) {
+    hi = (float)v;
+    lo = (float)(v - (double)hi);
+}
+
+AG_CDM_FN void fill_side(SideC& S, Vec3 pa, Vec3 pb, Vec3 bvec, double nu, double x0, double y0,
+                         bool& active) {
+    const double PI = 3.14159265358979323846;
+    const double LN2 = 0.69314718055994530942;
+    Vec3 side = v_sub(pb, pa);
+    double L = sqrt(v_dot(side, side));
+    double beta = acos(-side.z / L);
+    // vertical sides contribute nothing (libcdm.py:320-324)
+    const double eps = 2.220446049250313e-16;
+    if (!(L > 0.0) || fabs(beta) < eps || fabs(PI - beta) < eps) {
+        active = false;
+        return;
+    }
+    active = true;
+    double hl = sqrt(side.x * side.x + side.y * side.y);
+    double c = side.x / hl, s = side.y / hl;         // e1 = (c, s, 0), e2 = (s, -c, 0)
+    double sb = hl / L, cb = -side.z / L;            // β in (0, π): sin β >= 0
+    double tb2 = (cb >= 0.0) ? sb / (1.0 + cb) : (1.0 - cb) / sb;
+    double ctb2 = 1.0 / tb2;
+    double cot = cb / sb;
+    double k = 1.0 - 2.0 * nu;
+    double rx = pa.x - x0, ry = pa.y - y0;
+    double k1 = c * rx + s * ry;
+    double k2 = s * rx - c * ry;
+    double aA = -pa.z, aB = -pb.z, da = aB - aA;
+    double dy1 = -hl;                                // y1(B) - y1(A) = -e1·side
+    // slip in the angular-dislocation frame, with the 1/(2π) of the formula folded in
+    const double inv2pi = 0.5 / PI;
+    double b1 = (c * bvec.x + s * bvec.y) * inv2pi;
+    double b2 = (s * bvec.x - c * bvec.y) * inv2pi;
+    double b3 = -bvec.z * inv2pi;
+    double kc1 = k * cot * b1, kc2 = k * cot * b2;
+    double C1F = b1 * (1.0 - k * cot * cot);
+    double C2F = b2 * (1.0 + k * cot * cot);
+    double C3F = kc1 + b3;
+    double C1P = -b2 * k * (0.5 - cot * cot);
+    double C2P = b1 * k * (0.5 + cot * cot);
+    double C1m10 = -b1 * sb * cb + b3 * sb * sb;
+    double C3m10 = -b1 * cb * cb + b3 * sb * cb;
+    double C1Q = -kc2 * cot * cb;
+    double C2Q = -kc1 / sb;
+    double C3Q = kc2 * cb;
+    double C1m11 = b2 * sb;
+    double C3m11 = b2 * cb;
+    double C1m12 = b1 * cb - b3 * sb;
+    S.q[0] = make_float4((float)c, (float)s, (float)k1, (float)k2);
+    S.q[1] = make_float4((float)dy1, (float)aA, (float)aB, (float)da);
+    S.q[2] = make_float4((float)sb, (float)cb, (float)tb2, (float)ctb2);
+    S.q[3] = make_float4((float)(da * (aA + aB)), (float)(2.0 * C1F), (float)(2.0 * C2F), (float)(2.0 * C3F));
+    S.q[4] = make_float4((float)(LN2 * C1P), (float)(LN2 * C2P), (float)kc1, (float)kc2);
+    S.q[5] = make_float4((float)(2.0 * nu * b1), (float)(2.0 * nu * b2), (float)(0.5 * k * b1),
+                         (float)(0.5 * k * b2));
+    S.q[6] = make_float4((float)b1, (float)b2, (float)C1m10, (float)C3m10);
+    S.q[7] = make_float4((float)(LN2 * C1Q), (float)(LN2 * C2Q), (float)(LN2 * C3Q), (float)C1m11);
+    S.q[8] = make_float4((float)C3m11, (float)C1m12, (float)(aA * sb), (float)(-aA * cb));
+    S.q[9] = make_float4((float)(dy1 * cb + da * sb), (float)(dy1 * sb - da * cb), (float)(LN2 * kc2), 0.f);
+}
+
+// corners of the three rectangles (libcdm.py:174-217); returns true if any is above the surface
+template <class Layout>
+AG_CDM_FN bool cdm_corners(const double* th, const Layout& L, Vec3 V[3][4]) {
+    const double x0 = th[L.x_idx], y0 = th[L.x_idx + 1], depth = th[L.depth_idx];
+    const double lx = 2.0 * th[L.axes_idx], ly = 2.0 * th[L.axes_idx + 1],
+                 lz = 2.0 * th[L.axes_idx + 2];
+    double sx, cx, sy, cy, sz, cz;
+    sincospi(th[L.omega_idx] / 180.0, &sx, &cx);
+    sincospi(th[L.omega_idx + 1] / 180.0, &sy, &cy);
+    sincospi(th[L.omega_idx + 2] / 180.0, &sz, &cz);
+    // R = Rz·Ry·Rx with Rx = [[1,0,0],[0,cx,sx],[0,-sx,cx]], Ry = [[cy,0,-sy],[0,1,0],[sy,0,cy]],
+    // Rz = [[cz,sz,0],[-sz,cz,0],[0,0,1]]; columns ex, ey, ez are the body axes in EFCS
+    const double ryx[3][3] = {{cy, sy * sx, -sy * cx},   // Ry·Rx
+                              {0.0, cx, sx},
+                              {sy, cy * -sx, cy * cx}};
+    double R[3][3];
+    const double rz[3][3] = {{cz, sz, 0.0}, {-sz, cz, 0.0}, {0.0, 0.0, 1.0}};
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            R[i][j] = rz[i][0] * ryx[0][j] + rz[i][1] * ryx[1][j] + rz[i][2] * ryx[2][j];
+    Vec3 ex{R[0][0], R[1][0], R[2][0]}, ey{R[0][1], R[1][1], R[2][1]}, ez{R[0][2], R[1][2], R[2][2]};
+    Vec3 c0{x0, y0, -depth};
+    Vec3 p1 = v_add(c0, v_add(v_scale(ey, 0.5 * ly), v_scale(ez, 0.5 * lz)));
+    Vec3 p2 = v_sub(p1, v_scale(ey, ly));
+    Vec3 p3 = v_sub(p2, v_scale(ez, lz));
+    Vec3 p4 = v_sub(p1, v_scale(ez, lz));
+    Vec3 q1 = v_add(v_sub(c0, v_scale(ex, 0.5 * lx)), v_scale(ez, 0.5 * lz));
+    Vec3 q2 = v_add(q1, v_scale(ex, lx));
+    Vec3 q3 = v_sub(q2, v_scale(ez, lz));
+    Vec3 q4 = v_sub(q1, v_scale(ez, lz));
+    Vec3 r1 = v_add(c0, v_add(v_scale(ex, 0.5 * lx), v_scale(ey, 0.5 * ly)));
+    Vec3 r2 = v_sub(r1, v_scale(ex, lx));
+    Vec3 r3 = v_sub(r2, v_scale(ey, ly));
+    Vec3 r4 = v_sub(r1, v_scale(ey, ly));
+    V[0][0] = p1; V[0][1] = p2; V[0][2] = p3; V[0][3] = p4;
+    V[1][0] = q1; V[1][1] = q2; V[1][2] = q3; V[1][3] = q4;
+    V[2][0] = r1; V[2][1] = r2; V[2][2] = r3; V[2][3] = r4;
+    bool above = false;
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 4; ++b) above |= (V[a][b].z > 0.0);
+    return above;
+}
+
+// Constants of the active sides of a chain whose corners V lie below the surface;
+// returns the mask of active sides (bit 4r + e: side e of rectangle r)
+template <class Layout>
+AG_CDM_FN uint32_t cdm_sides(const double* th, const Layout& L, const Vec3 V[3][4], double x0, double y0,
+                             SideC* side) {
+    // which rectangles take part (libcdm.py:226-242)
+    const double ax = th[L.axes_idx], ay = th[L.axes_idx + 1], az = th[L.axes_idx + 2];
+    bool use[3];
+    if (ax == 0.0 && ay == 0.0 && az == 0.0) {
+        use[0] = use[1] = use[2] = false;
+    } else if (ax == 0.0 && ay != 0.0 && az != 0.0) {
+        use[0] = true; use[1] = use[2] = false;
+    } else if (ax != 0.0 && ay == 0.0 && az != 0.0) {
+        use[1] = true; use[0] = use[2] = false;
+    } else if (ax != 0.0 && ay != 0.0 && az == 0.0) {
+        use[2] = true; use[0] = use[1] = false;
+    } else {
+        use[0] = use[1] = use[2] = true;
+    }
+    const double opening = th[L.strength_idx];
+    uint32_t mask = 0u;
+    for (int r = 0; r < 3; ++r) {
+        if (!use[r]) continue;
+        Vec3 nrm = v_cross(v_sub(V[r][1], V[r][0]), v_sub(V[r][3], V[r][0]));
+        nrm = v_scale(nrm, 1.0 / sqrt(v_dot(nrm, nrm)));
+        Vec3 b = v_scale(nrm, opening);
+        for (int e = 0; e < 4; ++e) {
+            bool act;
+            fill_side(side[r * 4 + e], V[r][e], V[r][(e + 1) & 3], b, L.nu, x0, y0, act);
+            if (act) mask |= 1u << (r * 4 + e);
+        }
+    }
+    return mask;
+}
+
+// ---------------------------------------------------------------------------
+// FP32 elementary functions (own implementations)
+
+AG_DEVICE_INLINE float fast_rcp(float x) { return __fdividef(1.0f, x); }
+
+// log2(ρ) of a ratio ρ > 0 given s = (ρ - 1)/(ρ + 1), which the caller forms
+// from a difference without cancellation.  For ρ in [√½, √2] (|s| <= 3 - 2√2)
+// log2 ρ = 2 atanh(s)/ln 2 = (2/ln 2)(s + s³/3 + s⁵/5 + s⁷/7 + s⁹/9) + O(s¹¹),
+// truncation < 2e-9 relative, so ratios near 1 keep full relative accuracy;
+// outside that range |log2 ρ| >= 0.5 and the hardware base-2 logarithm of ρ
+// (absolute error <= 2^-22.6 on [0.5, 2], 2 ulp elsewhere) is used.
+AG_DEVICE_INLINE float log2_ratio(float s, float rho) {
+    const float t = __fmul_rn(s, s);
+    float p = fmaf(t, 3.205988980e-01f, 4.121985831e-01f);
+    p = fmaf(p, t, 5.770780164e-01f);
+    p = fmaf(p, t, 9.617966939e-01f);
+    p = fmaf(p, t, 2.885390082e+00f);
+    const float near = __fmul_rn(s, p);
+    return fabsf(s) <= 0.17157288f ? near : __log2f(rho);
+}
+
+// atan2(y, x): octant reduction to t = min/max in [0, 1], atan(t) = t·P(t²) with
+// P of degree 8, coefficients fitted here by iteratively reweighted least squares
+// on the relative error over [0, 1] (<= 1.9 ulp in FP32 Horner form), then
+// π/2 - r, π - r and the sign of y restore the quadrant.  atan2(0, 0) = 0.
+AG_DEVICE_INLINE float atan2_poly(float y, float x) {
+    const float ax = fabsf(x), ay = fabsf(y);
+    const float mx = fmaxf(ax, ay), mn = fminf(ax, ay);
+    const float t = (mx > 0.0f) ? mn * fast_rcp(mx) : 0.0f;
+    const float u = t * t;
+    float p = 2.903841436e-03f;
+    p = fmaf(p, u, -1.628421992e-02f);
+    p = fmaf(p, u, 4.304145649e-02f);
+    p = fmaf(p, u, -7.533866167e-02f);
+    p = fmaf(p, u, 1.065477580e-01f);
+    p = fmaf(p, u, -1.420716196e-01f);
+    p = fmaf(p, u, 1.999305785e-01f);
+    p = fmaf(p, u, -3.333309293e-01f);
+    p = fmaf(p, u, 1.0f);
+    float r = p * t;
+    r = (ay > ax) ? 1.57079632679f - r : r;
+    r = (x < 0.0f) ? 3.14159265359f - r : r;
+    return copysignf(r, y);
+}
+
+// ---------------------------------------------------------------------------
+// Arithmetic of side_pair.  Every product that feeds a sum is written as an
+// explicit FMA and the remaining adds and multiplies use the non-contracting
+// round-to-nearest forms, so the rounding of each operation is fixed by the
+// source rather than by the compiler's contraction choices.  (A two-station
+// form with packed FP32x2 instructions was measured 2-4% slower on this kernel:
+// the FMA pipe throttles the packed instructions, and it was removed.)
+AG_DEVICE_INLINE float vfma(float a, float b, float c) { return fmaf(a, b, c); }
+AG_DEVICE_INLINE float vadd(float a, float b) { return __fadd_rn(a, b); }
+AG_DEVICE_INLINE float vsub(float a, float b) { return __fsub_rn(a, b); }
+AG_DEVICE_INLINE float vmul(float a, float b) { return __fmul_rn(a, b); }
+AG_DEVICE_INLINE float vneg(float a) { return -a; }
+AG_DEVICE_INLINE bool vge0(float a) { return a >= 0.0f; }
+AG_DEVICE_INLINE bool vgt0(float a) { return a > 0.0f; }
+AG_DEVICE_INLINE bool vand(bool a, bool b) { return a && b; }
+AG_DEVICE_INLINE float vsel(bool c, float a, float b) { return c ? a : b; }
+AG_DEVICE_INLINE float frcp(float x) { return fast_rcp(x); }
+AG_DEVICE_INLINE float vrsqrt(float x) { return rsqrtf(x); }
+AG_DEVICE_INLINE float vlog2r(float s, float rho) { return log2_ratio(s, rho); }
+AG_DEVICE_INLINE float vatan2(float y, float x) { return atan2_poly(y, x); }
+
+// Several stations per lane as a group of scalars: every operation is the scalar one
+// on each element, so results are identical to the one-station form, while the
+// independent chains of dependent instructions interleave (instruction-level
+// parallelism for the MUFU and FMA latencies) and each side constant is loaded from
+// shared memory once for the whole group.
+template <int N>
+struct SV {
+    float v[N];
+    AG_DEVICE_INLINE SV() {}
+    AG_DEVICE_INLINE SV(float x) {
+#pragma unroll
+        for (int i = 0; i < N; ++i) v[i] = x;
+    }
+};
+template <int N>
+struct CV { bool v[N]; };
+#define AG_SV_MAP(expr)                  \
+    SV<N> r;                             \
+    _Pragma("unroll") for (int i = 0; i < N; ++i) r.v[i] = (expr); \
+    return r
+#define AG_CV_MAP(expr)                  \
+    CV<N> r;                             \
+    _Pragma("unroll") for (int i = 0; i < N; ++i) r.v[i] = (expr); \
+    return r
+template <int N> AG_DEVICE_INLINE SV<N> vfma(SV<N> x, SV<N> y, SV<N> z) { AG_SV_MAP(fmaf(x.v[i], y.v[i], z.v[i])); }
+template <int N> AG_DEVICE_INLINE SV<N> vadd(SV<N> x, SV<N> y) { AG_SV_MAP(__fadd_rn(x.v[i], y.v[i])); }
+template <int N> AG_DEVICE_INLINE SV<N> vsub(SV<N> x, SV<N> y) { AG_SV_MAP(__fsub_rn(x.v[i], y.v[i])); }
+template <int N> AG_DEVICE_INLINE SV<N> vmul(SV<N> x, SV<N> y) { AG_SV_MAP(__fmul_rn(x.v[i], y.v[i])); }
+template <int N> AG_DEVICE_INLINE SV<N> vneg(SV<N> x) { AG_SV_MAP(-x.v[i]); }
+template <int N> AG_DEVICE_INLINE CV<N> vge0(SV<N> x) { AG_CV_MAP(x.v[i] >= 0.0f); }
+template <int N> AG_DEVICE_INLINE CV<N> vgt0(SV<N> x) { AG_CV_MAP(x.v[i] > 0.0f); }
+template <int N> AG_DEVICE_INLINE CV<N> vand(CV<N> x, CV<N> y) { AG_CV_MAP(x.v[i] && y.v[i]); }
+template <int N> AG_DEVICE_INLINE SV<N> vsel(CV<N> c, SV<N> x, SV<N> y) { AG_SV_MAP(c.v[i] ? x.v[i] : y.v[i]); }
+template <int N> AG_DEVICE_INLINE SV<N> frcp(SV<N> x) { AG_SV_MAP(fast_rcp(x.v[i])); }
+template <int N> AG_DEVICE_INLINE SV<N> vrsqrt(SV<N> x) { AG_SV_MAP(rsqrtf(x.v[i])); }
+template <int N> AG_DEVICE_INLINE SV<N> vlog2r(SV<N> s, SV<N> rho) { AG_SV_MAP(log2_ratio(s.v[i], rho.v[i])); }
+template <int N> AG_DEVICE_INLINE SV<N> vatan2(SV<N> y, SV<N> x) { AG_SV_MAP(atan2_poly(y.v[i], x.v[i])); }
+#undef AG_SV_MAP
+#undef AG_CV_MAP
+
+struct ScalarSide {
+    float4 q[10];
+    AG_DEVICE_INLINE explicit ScalarSide(const SideC& S) {
+#pragma unroll
+        for (int i = 0; i < 10; ++i) q[i] = S.q[i];
+    }
+    template <int I>
+    AG_DEVICE_INLINE float at() const {
+        const float4 t = q[I >> 2];
+        return (I & 3) == 0 ? t.x : (I & 3) == 1 ? t.y : (I & 3) == 2 ? t.z : t.w;
+    }
+    template <int I>
+    AG_DEVICE_INLINE float neg() const { return -at<I>(); }
+};
+
+#define KC(i) V(k.template at<i>())
+#define KN(i) V(k.template neg<i>())
+
+// ---------------------------------------------------------------------------
+// One angular-dislocation pair in difference arithmetic: every quantity is
+// carried as (value at A, difference B - A), the difference propagated by exact
+// identities (Δ(uv) = Δu·v_B + u_A·Δv, Δ(1/u) = -Δu/(u_A u_B),
+// Δr = Δ(r²)/(r_A + r_B), Δlog u from s = Δu/(u_A + u_B), the Burgers-function
+// difference as one atan2 of the rotation from A to B), so the v(B) - v(A)
+// cancellation of the reference formula never happens in floating point.
+template <class V, class K>
+AG_DEVICE_INLINE void side_pair(const K& k, V Xr, V Yr, V& ue, V& un, V& uv) {
+    const V c = KC(K_C), s = KC(K_S);
+    const V dy1 = KC(K_DY1), aA = KC(K_AA), aB = KC(K_AB), da = KC(K_DA);
+    // station in the angular-dislocation frame of vertex A; y2 is the same at B
+    const V y1A = vfma(c, Xr, vfma(s, Yr, KN(K_K1)));
+    const V y2 = vfma(s, Xr, vfma(KN(K_C), Yr, KN(K_K2)));
+    const V y1B = vadd(y1A, dy1);
+    // artefact-free configuration (libcdm.py:342-362): I if y1A >= 0 (β - π), else II (β);
+    // sin, cos and cot(β/2) of β - π are those of β times -1
+    const auto conf1 = vge0(y1A);
+    const V sg = vsel(conf1, V(-1.0f), V(1.0f));
+    const V ct2 = vsel(conf1, KN(K_TB2), KC(K_CTB2));
+    const V y22 = vmul(y2, y2);
+    // r (rA = r2A·irA enters every sum through an FMA)
+    const V r2A = vfma(y1A, y1A, vfma(aA, aA, y22));
+    const V r2B = vfma(y1B, y1B, vfma(aB, aB, y22));
+    const V irA = vrsqrt(r2A), irB = vrsqrt(r2B);
+    const V rB = vmul(r2B, irB);
+    const V dr = vmul(vfma(dy1, vadd(y1A, y1B), KC(K_DAS)), frcp(vfma(r2A, irA, rB)));
+    const V ndir = vmul(vmul(dr, irA), irB);           // -Δ(1/r)
+    // r + a
+    const V pA = vfma(r2A, irA, aA), pB = vfma(r2B, irB, aB), dp = vadd(dr, da);
+    const V ipA = frcp(pA), ipB = frcp(pB);
+    const V ndip = vmul(vmul(dp, ipA), ipB);           // -Δ(1/(r+a))
+    // z1 = sg (y1 cos β + a sin β), z3 = sg (y1 sin β - a cos β); Δz1, Δz3 are side constants
+    const V z1A = vmul(sg, vfma(y1A, KC(K_CB), KC(K_AASB)));
+    const V dz1 = vmul(sg, KC(K_DZ1));
+    const V z1B = vadd(z1A, dz1);
+    const V z3A = vmul(sg, vfma(y1A, KC(K_SB), KC(K_NAACB)));
+    const V dz3 = vmul(sg, KC(K_DZ3));
+    const V z3B = vadd(z3A, dz3);
+    // r - z3, cancellation-free: (z1² + y2²)/(r + z3) when z3 > 0, else (r + z3) - 2 z3
+    const auto posA = vgt0(z3A), posB = vgt0(z3B);
+    const V NA = vfma(z1A, z1A, y22), NB = vfma(z1B, z1B, y22);
+    const V DA = vfma(r2A, irA, z3A), DB = vfma(r2B, irB, z3B);
+    const V uA = vsel(posA, NA, vfma(V(-2.0f), z3A, DA)), vA = vsel(posA, DA, V(1.0f));
+    const V uB = vsel(posB, NB, vfma(V(-2.0f), z3B, DB)), vB = vsel(posB, DB, V(1.0f));
+    const V iuA = frcp(uA), iuB = frcp(uB);
+    const V iqA = vmul(vA, iuA), iqB = vmul(vB, iuB);
+    const V dN = vmul(dz1, vadd(z1A, z1B));
+    // both in the quotient form: Δq = (ΔN·D_A - N_A·ΔD)/(D_A D_B), ΔD = Δr + Δz3
+    const V dq = vsel(vand(posA, posB), vmul(vfma(dN, DA, vneg(vmul(NA, vadd(dr, dz3)))), frcp(vmul(DA, DB))),
+                      vsub(dr, dz3));
+    const V ndiq = vmul(vmul(dq, iqA), iqB);           // -Δ(1/q)
+    // log differences, base 2: s = Δu/(u_A + u_B) and the ratio u_B/u_A
+    const V dLp = vlog2r(vmul(dp, frcp(vadd(pA, pB))), vmul(pB, ipA));
+    const V xq = vmul(dq, iqA);                        // Δq/q_A
+    const V dLq = vlog2r(vmul(xq, frcp(vadd(V(2.0f), xq))), vadd(V(1.0f), xq));
+    // Burgers function difference: rotation of (x, y2) from A to B; y2 keeps its sign so
+    // the rotation never crosses atan2's cut (the factor 2 is in the coefficients)
+    const V xA = vfma(pA, ct2, vneg(y1A));
+    const V dx = vfma(dp, ct2, KN(K_DY1));
+    const V xB = vadd(xA, dx);
+    const V dF = vatan2(vmul(vneg(y2), dx), vfma(xA, xB, y22));
+    // monomials: value at A, value at B, difference
+    const V m1B = vmul(y2, ipB), ndm1 = vmul(y2, ndip);
+    const V m2A = vmul(y1A, ipA), m2B = vmul(y1B, ipB);
+    const V dm2 = vfma(dy1, ipB, vneg(vmul(y1A, ndip)));
+    const V dm3 = vfma(da, ipB, vmul(KN(K_AA), ndip));
+    const V dm4 = vfma(dm2, m1B, vneg(vmul(m2A, ndm1)));
+    const V dm35 = vfma(dm2, vfma(y1A, ipA, m2B), dm3);          // dm3 + dm2 (m2A + m2B)
+    const V dm36 = vfma(ndm1, vneg(vfma(y2, ipA, m1B)), dm3);    // dm3 + dm1 (m1A + m1B)
+    const V y1irA = vmul(y1A, irA), dy1ir = vfma(dy1, irB, vneg(vmul(y1A, ndir)));
+    const V y2irA = vmul(y2, irA), ndy2ir = vmul(y2, ndir);
+    const V nairA = vmul(KN(K_AA), irA), ndair = vfma(KN(K_DA), irB, vmul(aA, ndir));
+    const V m10B = vmul(y2, iqB), ndm10 = vmul(y2, ndiq);
+    const V m11B = vmul(z1B, iqB), dm11 = vfma(dz1, iqB, vneg(vmul(z1A, ndiq)));
+    const V c12 = vmul(sg, KC(K_C1M12));              // signed coefficient of the (m10 · r⁻¹) products
+    // The r⁻¹-weighted monomials share two brackets (distributivity of Δ(u v) = Δu v_B + u_A Δv):
+    //   v1: -b1 Δ(y1 r⁻¹ m1) + b2 Δ(y1 r⁻¹ m2) - b2 Δ(y1 r⁻¹ m11) + c12 Δ(y1 r⁻¹ m10)
+    //       = Δ(y1 r⁻¹)·X1 + (y1 r⁻¹)_A·ΔX1
+    //   v3: the same brackets with a r⁻¹ in place of y1 r⁻¹, negated
+    //   v2: b2 Δ(y1 r⁻¹ m1) + Δ(y2 r⁻¹)·X2 + (y2 r⁻¹)_A·ΔX2
+    // (ndm1, ndm10, ndy2ir: negated differences, folded into the coefficient signs)
+    const V X2 = vfma(KN(K_B1), m1B, vfma(KN(K_B2), m11B, vmul(c12, m10B)));
+    const V dX2 = vfma(KC(K_B1), ndm1, vfma(KN(K_B2), dm11, vneg(vmul(c12, ndm10))));
+    const V X1 = vfma(KC(K_B2), m2B, X2);
+    const V dX1 = vfma(KC(K_B2), dm2, dX2);
+    V v1 = vmul(KC(K_C1F), dF);
+    v1 = vfma(KC(K_C1P), dLp, v1);
+    v1 = vfma(KN(K_KC1), ndm1, v1);
+    v1 = vfma(KN(K_KC2), dm2, v1);
+    v1 = vfma(KN(K_HB2), dm35, v1);
+    v1 = vfma(KC(K_HB1), dm4, v1);
+    v1 = vfma(KN(K_C1M10), ndm10, v1);
+    v1 = vfma(dy1ir, X1, v1);
+    v1 = vfma(y1irA, dX1, v1);
+    v1 = vfma(sg, vfma(KC(K_C1Q), dLq, vmul(KC(K_C1M11), dm11)), v1);
+    V v2 = vmul(KC(K_C2F), dF);
+    v2 = vfma(KC(K_C2P), dLp, v2);
+    v2 = vfma(KC(K_KC2), ndm1, v2);
+    v2 = vfma(KN(K_KC1), dm2, v2);
+    v2 = vfma(KC(K_HB1), dm36, v2);
+    v2 = vfma(KN(K_HB2), dm4, v2);
+    v2 = vfma(KC(K_B2), vfma(dy1ir, m1B, vneg(vmul(y1irA, ndm1))), v2);
+    v2 = vfma(vneg(ndy2ir), X2, v2);
+    v2 = vfma(y2irA, dX2, v2);
+    v2 = vfma(vmul(sg, KC(K_C2Q)), dLq, v2);
+    V v3 = vmul(KC(K_C3F), dF);
+    v3 = vfma(KN(K_KC2L), dLp, v3);
+    v3 = vfma(KN(K_NB1), ndm1, v3);
+    v3 = vfma(KN(K_NB2), dm2, v3);
+    v3 = vfma(KN(K_C3M10), ndm10, v3);
+    v3 = vfma(ndair, X1, v3);
+    v3 = vfma(nairA, dX1, v3);
+    v3 = vfma(sg, vfma(KC(K_C3Q), dLq, vmul(KC(K_C3M11), dm11)), v3);
+    // back to EFCS: columns e1 = (c, s, 0), e2 = (s, -c, 0), e3 = (0, 0, -1)
+    ue = vfma(c, v1, vfma(s, v2, ue));
+    un = vfma(s, v1, vfma(KN(K_C), v2, un));
+    uv = vsub(uv, v3);
+}
+
+#undef KC
+#undef KN
+
+}  // namespace ag

@@ -108,57 +108,6 @@ AG_DEVICE_INLINE void normal_pair(u32x4 r, double& z0, double& z1) {
 }
 
 // ---------------------------------------------------------------------------
-// FP32 elementary functions for the forward models (own implementations)
-//
-// log1p(x), x > -1: u = 1 + x = m·2^e with m in [√½, √2) read from the bits of u,
-// log(m) = 2 atanh(s), s = (m - 1)/(m + 1), |s| <= 0.1716, summed as the series
-// 2 (s + s³/3 + s⁵/5 + s⁷/7 + s⁹/9) (truncation < 3e-9 relative).  When e = 0 the
-// exact s = x / (2 + x) is used, so small arguments keep full relative accuracy.
-// Measured against FP64: <= 2.8 ulp over x in (-0.99, 1e6).
-AG_DEVICE_INLINE float fast_rcp(float x) { return __fdividef(1.0f, x); }
-
-AG_DEVICE_INLINE float log1p_series(float x) {
-    const float u = 1.0f + x;
-    const int bits = __float_as_int(u);
-    const int e = (bits - 0x3f3504f3) >> 23;               // 0x3f3504f3 = √½
-    const float m = __int_as_float(bits - (e << 23));
-    const bool direct = (e == 0);
-    const float num = direct ? x : m - 1.0f;
-    const float den = direct ? 2.0f + x : m + 1.0f;
-    const float s = num * fast_rcp(den);
-    const float s2 = s * s;
-    float p = fmaf(s2, 2.0f / 9.0f, 2.0f / 7.0f);
-    p = fmaf(p, s2, 2.0f / 5.0f);
-    p = fmaf(p, s2, 2.0f / 3.0f);
-    const float lm = fmaf(s * s2, p, 2.0f * s);
-    return fmaf((float)e, 0.69314718056f, lm);
-}
-
-// atan2(y, x): octant reduction to t = min/max in [0, 1], atan(t) = t·P(t²) with
-// P of degree 8, coefficients fitted here by iteratively reweighted least squares
-// on the relative error over [0, 1] (<= 1.9 ulp in FP32 Horner form), then
-// π/2 - r, π - r and the sign of y restore the quadrant.  atan2(0, 0) = 0.
-AG_DEVICE_INLINE float atan2_poly(float y, float x) {
-    const float ax = fabsf(x), ay = fabsf(y);
-    const float mx = fmaxf(ax, ay), mn = fminf(ax, ay);
-    const float t = (mx > 0.0f) ? mn * fast_rcp(mx) : 0.0f;
-    const float u = t * t;
-    float p = 2.903841436e-03f;
-    p = fmaf(p, u, -1.628421992e-02f);
-    p = fmaf(p, u, 4.304145649e-02f);
-    p = fmaf(p, u, -7.533866167e-02f);
-    p = fmaf(p, u, 1.065477580e-01f);
-    p = fmaf(p, u, -1.420716196e-01f);
-    p = fmaf(p, u, 1.999305785e-01f);
-    p = fmaf(p, u, -3.333309293e-01f);
-    p = fmaf(p, u, 1.0f);
-    float r = p * t;
-    r = (ay > ax) ? 1.57079632679f - r : r;
-    r = (x < 0.0f) ? 3.14159265359f - r : r;
-    return copysignf(r, y);
-}
-
-// ---------------------------------------------------------------------------
 // float-float accumulation
 struct ff { float hi, lo; };
 

@@ -30,29 +30,16 @@
 
 #include "common.cuh"
 #include "internal.h"
+#include "cdm_side.cuh"
 
 namespace ag {
 
 constexpr int kMaxOffsets = 16;      // datasets with their own offset parameter
-constexpr int kSides = 12;
 constexpr int kTile = AG_STATION_TILE;
 constexpr uint32_t kWaitLimit = 1u << 24;
 
 // ---------------------------------------------------------------------------
-// per-side constants of one angular-dislocation pair (36 floats)
-struct __align__(16) SideC {
-    float4 q[9];
-};
-// q0: c, s, k1, k2          frame (unit horizontal side direction) and vertex A
-// q1: dy1, aA, aB, da       y1(B) - y1(A); depths of A and B; aB - aA
-// q2: sb, cb, tb2, ctb2     sin β, cos β, tan(β/2), cot(β/2) (configuration II)
-// q3: daS, C1F, C2F, C3F    da·(aA+aB); coefficients of ΔFi
-// q4: C1P, C2P, kc1, kc2    coefficients of Δlog(r+a); k·cot·b1, k·cot·b2
-// q5: nb1, nb2, hb1, hb2    2ν b1, 2ν b2, k b1/2, k b2/2
-// q6: b1, b2, C1m10, C3m10
-// q7: C1Q, C2Q, C3Q, C1m11  configuration-signed coefficients
-// q8: C3m11, C1m12, 0, 0
-
+// per-chain constants: stations are taken relative to the source centre (x0, y0)
 struct __align__(16) ChainC {
     float4 hdr;                 // x0_hi, x0_lo, y0_hi, y0_lo
     uint32_t side_mask;         // active sides; 0 = chain inactive
@@ -63,120 +50,6 @@ struct __align__(16) ChainC {
     SideC side[kSides];
 };
 static_assert(sizeof(ChainC) % 16 == 0, "ChainC must be a whole number of float4");
-
-// ---------------------------------------------------------------------------
-// FP64 per-chain set-up: rotation, corners, geometry check, per-side constants
-struct Vec3 { double x, y, z; };
-__device__ inline Vec3 v_sub(Vec3 a, Vec3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
-__device__ inline Vec3 v_add(Vec3 a, Vec3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
-__device__ inline Vec3 v_scale(Vec3 a, double s) { return {a.x * s, a.y * s, a.z * s}; }
-__device__ inline Vec3 v_cross(Vec3 a, Vec3 b) {
-    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
-}
-__device__ inline double v_dot(Vec3 a, Vec3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-
-__device__ inline void split_hilo(double v, float& hi, float& lo) {
-    hi = (float)v;
-    lo = (float)(v - (double)hi);
-}
-
-__device__ void fill_side(SideC& S, Vec3 pa, Vec3 pb, Vec3 bvec, double nu, double x0, double y0,
-                          bool& active) {
-    const double PI = 3.14159265358979323846;
-    Vec3 side = v_sub(pb, pa);
-    double L = sqrt(v_dot(side, side));
-    double beta = acos(-side.z / L);
-    // vertical sides contribute nothing (libcdm.py:320-324)
-    const double eps = 2.220446049250313e-16;
-    if (!(L > 0.0) || fabs(beta) < eps || fabs(PI - beta) < eps) {
-        active = false;
-        return;
-    }
-    active = true;
-    double hl = sqrt(side.x * side.x + side.y * side.y);
-    double c = side.x / hl, s = side.y / hl;         // e1 = (c, s, 0), e2 = (s, -c, 0)
-    double sb = hl / L, cb = -side.z / L;            // β in (0, π): sin β >= 0
-    double tb2 = (cb >= 0.0) ? sb / (1.0 + cb) : (1.0 - cb) / sb;
-    double ctb2 = 1.0 / tb2;
-    double cot = cb / sb;
-    double k = 1.0 - 2.0 * nu;
-    double rx = pa.x - x0, ry = pa.y - y0;
-    double k1 = c * rx + s * ry;
-    double k2 = s * rx - c * ry;
-    double aA = -pa.z, aB = -pb.z, da = aB - aA;
-    double dy1 = -hl;                                // y1(B) - y1(A) = -e1·side
-    // slip in the angular-dislocation frame, with the 1/(2π) of the formula folded in
-    const double inv2pi = 0.5 / PI;
-    double b1 = (c * bvec.x + s * bvec.y) * inv2pi;
-    double b2 = (s * bvec.x - c * bvec.y) * inv2pi;
-    double b3 = -bvec.z * inv2pi;
-    double kc1 = k * cot * b1, kc2 = k * cot * b2;
-    double C1F = b1 * (1.0 - k * cot * cot);
-    double C2F = b2 * (1.0 + k * cot * cot);
-    double C3F = kc1 + b3;
-    double C1P = -b2 * k * (0.5 - cot * cot);
-    double C2P = b1 * k * (0.5 + cot * cot);
-    double C1m10 = -b1 * sb * cb + b3 * sb * sb;
-    double C3m10 = -b1 * cb * cb + b3 * sb * cb;
-    double C1Q = -kc2 * cot * cb;
-    double C2Q = -kc1 / sb;
-    double C3Q = kc2 * cb;
-    double C1m11 = b2 * sb;
-    double C3m11 = b2 * cb;
-    double C1m12 = b1 * cb - b3 * sb;
-    S.q[0] = make_float4((float)c, (float)s, (float)k1, (float)k2);
-    S.q[1] = make_float4((float)dy1, (float)aA, (float)aB, (float)da);
-    S.q[2] = make_float4((float)sb, (float)cb, (float)tb2, (float)ctb2);
-    S.q[3] = make_float4((float)(da * (aA + aB)), (float)C1F, (float)C2F, (float)C3F);
-    S.q[4] = make_float4((float)C1P, (float)C2P, (float)kc1, (float)kc2);
-    S.q[5] = make_float4((float)(2.0 * nu * b1), (float)(2.0 * nu * b2), (float)(0.5 * k * b1),
-                         (float)(0.5 * k * b2));
-    S.q[6] = make_float4((float)b1, (float)b2, (float)C1m10, (float)C3m10);
-    S.q[7] = make_float4((float)C1Q, (float)C2Q, (float)C3Q, (float)C1m11);
-    S.q[8] = make_float4((float)C3m11, (float)C1m12, 0.f, 0.f);
-}
-
-// corners of the three rectangles (libcdm.py:174-217); returns true if any is above the surface
-__device__ bool cdm_corners(const double* th, const ag_layout& L, Vec3 V[3][4]) {
-    const double x0 = th[L.x_idx], y0 = th[L.x_idx + 1], depth = th[L.depth_idx];
-    const double lx = 2.0 * th[L.axes_idx], ly = 2.0 * th[L.axes_idx + 1],
-                 lz = 2.0 * th[L.axes_idx + 2];
-    double sx, cx, sy, cy, sz, cz;
-    sincospi(th[L.omega_idx] / 180.0, &sx, &cx);
-    sincospi(th[L.omega_idx + 1] / 180.0, &sy, &cy);
-    sincospi(th[L.omega_idx + 2] / 180.0, &sz, &cz);
-    // R = Rz·Ry·Rx with Rx = [[1,0,0],[0,cx,sx],[0,-sx,cx]], Ry = [[cy,0,-sy],[0,1,0],[sy,0,cy]],
-    // Rz = [[cz,sz,0],[-sz,cz,0],[0,0,1]]; columns ex, ey, ez are the body axes in EFCS
-    const double ryx[3][3] = {{cy, sy * sx, -sy * cx},   // Ry·Rx
-                              {0.0, cx, sx},
-                              {sy, cy * -sx, cy * cx}};
-    double R[3][3];
-    const double rz[3][3] = {{cz, sz, 0.0}, {-sz, cz, 0.0}, {0.0, 0.0, 1.0}};
-    for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j)
-            R[i][j] = rz[i][0] * ryx[0][j] + rz[i][1] * ryx[1][j] + rz[i][2] * ryx[2][j];
-    Vec3 ex{R[0][0], R[1][0], R[2][0]}, ey{R[0][1], R[1][1], R[2][1]}, ez{R[0][2], R[1][2], R[2][2]};
-    Vec3 c0{x0, y0, -depth};
-    Vec3 p1 = v_add(c0, v_add(v_scale(ey, 0.5 * ly), v_scale(ez, 0.5 * lz)));
-    Vec3 p2 = v_sub(p1, v_scale(ey, ly));
-    Vec3 p3 = v_sub(p2, v_scale(ez, lz));
-    Vec3 p4 = v_sub(p1, v_scale(ez, lz));
-    Vec3 q1 = v_add(v_sub(c0, v_scale(ex, 0.5 * lx)), v_scale(ez, 0.5 * lz));
-    Vec3 q2 = v_add(q1, v_scale(ex, lx));
-    Vec3 q3 = v_sub(q2, v_scale(ez, lz));
-    Vec3 q4 = v_sub(q1, v_scale(ez, lz));
-    Vec3 r1 = v_add(c0, v_add(v_scale(ex, 0.5 * lx), v_scale(ey, 0.5 * ly)));
-    Vec3 r2 = v_sub(r1, v_scale(ex, lx));
-    Vec3 r3 = v_sub(r2, v_scale(ey, ly));
-    Vec3 r4 = v_sub(r1, v_scale(ey, ly));
-    V[0][0] = p1; V[0][1] = p2; V[0][2] = p3; V[0][3] = p4;
-    V[1][0] = q1; V[1][1] = q2; V[1][2] = q3; V[1][3] = q4;
-    V[2][0] = r1; V[2][1] = r2; V[2][2] = r3; V[2][3] = r4;
-    bool above = false;
-    for (int a = 0; a < 3; ++a)
-        for (int b = 0; b < 4; ++b) above |= (V[a][b].z > 0.0);
-    return above;
-}
 
 // One thread per requested chain (all n, or the first *count_in of index_in).  Chains that
 // are masked or lie above the free surface get their status and nothing else; every other
@@ -213,33 +86,7 @@ __global__ void cdm_setup_kernel(ag_layout L, const double* __restrict__ theta, 
     split_hilo(y0, C.hdr.z, C.hdr.w);
     for (int k = 0; k < kMaxOffsets; ++k)
         C.off[k] = (k < noffsets) ? (float)th[L.offset_idx + k] : 0.f;
-    // which rectangles take part (libcdm.py:226-242)
-    const double ax = th[L.axes_idx], ay = th[L.axes_idx + 1], az = th[L.axes_idx + 2];
-    bool use[3];
-    if (ax == 0.0 && ay == 0.0 && az == 0.0) {
-        use[0] = use[1] = use[2] = false;
-    } else if (ax == 0.0 && ay != 0.0 && az != 0.0) {
-        use[0] = true; use[1] = use[2] = false;
-    } else if (ax != 0.0 && ay == 0.0 && az != 0.0) {
-        use[1] = true; use[0] = use[2] = false;
-    } else if (ax != 0.0 && ay != 0.0 && az == 0.0) {
-        use[2] = true; use[0] = use[1] = false;
-    } else {
-        use[0] = use[1] = use[2] = true;
-    }
-    const double opening = th[L.strength_idx];
-    uint32_t mask = 0u;
-    for (int r = 0; r < 3; ++r) {
-        if (!use[r]) continue;
-        Vec3 nrm = v_cross(v_sub(V[r][1], V[r][0]), v_sub(V[r][3], V[r][0]));
-        nrm = v_scale(nrm, 1.0 / sqrt(v_dot(nrm, nrm)));
-        Vec3 b = v_scale(nrm, opening);
-        for (int e = 0; e < 4; ++e) {
-            bool act;
-            fill_side(C.side[r * 4 + e], V[r][e], V[r][(e + 1) & 3], b, L.nu, x0, y0, act);
-            if (act) mask |= 1u << (r * 4 + e);
-        }
-    }
+    const uint32_t mask = cdm_sides(th, L, V, x0, y0, C.side);
     // a chain with no active side still needs a llk: keep bit 31 as "evaluate"
     C.side_mask = mask | 0x80000000u;
 }
@@ -251,208 +98,6 @@ __global__ void cdm_check_kernel(ag_layout L, const double* __restrict__ theta, 
     Vec3 V[3][4];
     if (cdm_corners(theta + (size_t)i * L.nparams, L, V)) chain_status[i] |= CHAIN_ABOVE_SURFACE;
 }
-
-// ---------------------------------------------------------------------------
-// Arithmetic of side_pair.  Every product that feeds a sum is written as an
-// explicit FMA and the remaining adds and multiplies use the non-contracting
-// round-to-nearest forms, so the rounding of each operation is fixed by the
-// source rather than by the compiler's contraction choices.  (A two-station
-// form with packed FP32x2 instructions was measured 2-4% slower on this kernel:
-// the FMA pipe throttles the packed instructions, and it was removed.)
-AG_DEVICE_INLINE float vfma(float a, float b, float c) { return fmaf(a, b, c); }
-AG_DEVICE_INLINE float vadd(float a, float b) { return __fadd_rn(a, b); }
-AG_DEVICE_INLINE float vsub(float a, float b) { return __fsub_rn(a, b); }
-AG_DEVICE_INLINE float vmul(float a, float b) { return __fmul_rn(a, b); }
-AG_DEVICE_INLINE float vneg(float a) { return -a; }
-AG_DEVICE_INLINE bool vge0(float a) { return a >= 0.0f; }
-AG_DEVICE_INLINE bool vgt0(float a) { return a > 0.0f; }
-AG_DEVICE_INLINE bool vand(bool a, bool b) { return a && b; }
-AG_DEVICE_INLINE float vsel(bool c, float a, float b) { return c ? a : b; }
-AG_DEVICE_INLINE float frcp(float x) { return fast_rcp(x); }
-AG_DEVICE_INLINE float vrsqrt(float x) { return rsqrtf(x); }
-AG_DEVICE_INLINE float vlog1p(float x) { return log1p_series(x); }
-AG_DEVICE_INLINE float vatan2(float y, float x) { return atan2_poly(y, x); }
-
-// Several stations per lane as a group of scalars: every operation is the scalar one
-// on each element, so results are identical to the one-station form, while the
-// independent chains of dependent instructions interleave (instruction-level
-// parallelism for the MUFU and FMA latencies) and each side constant is loaded from
-// shared memory once for the whole group.
-template <int N>
-struct SV {
-    float v[N];
-    AG_DEVICE_INLINE SV() {}
-    AG_DEVICE_INLINE SV(float x) {
-#pragma unroll
-        for (int i = 0; i < N; ++i) v[i] = x;
-    }
-};
-template <int N>
-struct CV { bool v[N]; };
-#define AG_SV_MAP(expr)                  \
-    SV<N> r;                             \
-    _Pragma("unroll") for (int i = 0; i < N; ++i) r.v[i] = (expr); \
-    return r
-#define AG_CV_MAP(expr)                  \
-    CV<N> r;                             \
-    _Pragma("unroll") for (int i = 0; i < N; ++i) r.v[i] = (expr); \
-    return r
-template <int N> AG_DEVICE_INLINE SV<N> vfma(SV<N> x, SV<N> y, SV<N> z) { AG_SV_MAP(fmaf(x.v[i], y.v[i], z.v[i])); }
-template <int N> AG_DEVICE_INLINE SV<N> vadd(SV<N> x, SV<N> y) { AG_SV_MAP(__fadd_rn(x.v[i], y.v[i])); }
-template <int N> AG_DEVICE_INLINE SV<N> vsub(SV<N> x, SV<N> y) { AG_SV_MAP(__fsub_rn(x.v[i], y.v[i])); }
-template <int N> AG_DEVICE_INLINE SV<N> vmul(SV<N> x, SV<N> y) { AG_SV_MAP(__fmul_rn(x.v[i], y.v[i])); }
-template <int N> AG_DEVICE_INLINE SV<N> vneg(SV<N> x) { AG_SV_MAP(-x.v[i]); }
-template <int N> AG_DEVICE_INLINE CV<N> vge0(SV<N> x) { AG_CV_MAP(x.v[i] >= 0.0f); }
-template <int N> AG_DEVICE_INLINE CV<N> vgt0(SV<N> x) { AG_CV_MAP(x.v[i] > 0.0f); }
-template <int N> AG_DEVICE_INLINE CV<N> vand(CV<N> x, CV<N> y) { AG_CV_MAP(x.v[i] && y.v[i]); }
-template <int N> AG_DEVICE_INLINE SV<N> vsel(CV<N> c, SV<N> x, SV<N> y) { AG_SV_MAP(c.v[i] ? x.v[i] : y.v[i]); }
-template <int N> AG_DEVICE_INLINE SV<N> frcp(SV<N> x) { AG_SV_MAP(fast_rcp(x.v[i])); }
-template <int N> AG_DEVICE_INLINE SV<N> vrsqrt(SV<N> x) { AG_SV_MAP(rsqrtf(x.v[i])); }
-template <int N> AG_DEVICE_INLINE SV<N> vlog1p(SV<N> x) { AG_SV_MAP(log1p_series(x.v[i])); }
-template <int N> AG_DEVICE_INLINE SV<N> vatan2(SV<N> y, SV<N> x) { AG_SV_MAP(atan2_poly(y.v[i], x.v[i])); }
-#undef AG_SV_MAP
-#undef AG_CV_MAP
-
-// Per-side constant by its position in SideC (q[i >> 2], component i & 3)
-enum : int {
-    K_C = 0, K_S, K_K1, K_K2, K_DY1, K_AA, K_AB, K_DA, K_SB, K_CB, K_TB2, K_CTB2, K_DAS, K_C1F, K_C2F, K_C3F,
-    K_C1P, K_C2P, K_KC1, K_KC2, K_NB1, K_NB2, K_HB1, K_HB2, K_B1, K_B2, K_C1M10, K_C3M10, K_C1Q, K_C2Q, K_C3Q,
-    K_C1M11, K_C3M11, K_C1M12
-};
-
-struct ScalarSide {
-    float4 q[9];
-    AG_DEVICE_INLINE explicit ScalarSide(const SideC& S) {
-#pragma unroll
-        for (int i = 0; i < 9; ++i) q[i] = S.q[i];
-    }
-    template <int I>
-    AG_DEVICE_INLINE float at() const {
-        const float4 t = q[I >> 2];
-        return (I & 3) == 0 ? t.x : (I & 3) == 1 ? t.y : (I & 3) == 2 ? t.z : t.w;
-    }
-    template <int I>
-    AG_DEVICE_INLINE float neg() const { return -at<I>(); }
-};
-
-#define KC(i) V(k.template at<i>())
-#define KN(i) V(k.template neg<i>())
-
-// ---------------------------------------------------------------------------
-// one angular-dislocation pair in difference arithmetic
-template <class V, class K>
-AG_DEVICE_INLINE void side_pair(const K& k, V Xr, V Yr, V& ue, V& un, V& uv) {
-    const V c = KC(K_C), s = KC(K_S);
-    const V dy1 = KC(K_DY1), aA = KC(K_AA), aB = KC(K_AB), da = KC(K_DA);
-    // station in the angular-dislocation frame of vertex A; y2 is the same at B
-    const V y1A = vfma(c, Xr, vfma(s, Yr, KN(K_K1)));
-    const V y2 = vfma(s, Xr, vfma(KN(K_C), Yr, KN(K_K2)));
-    const V y1B = vadd(y1A, dy1);
-    // artefact-free configuration (libcdm.py:342-362): I if y1A >= 0 (β - π), else II (β)
-    const auto conf1 = vge0(y1A);
-    const V sg = vsel(conf1, V(-1.0f), V(1.0f));
-    const V sB = vmul(sg, KC(K_SB)), cB = vmul(sg, KC(K_CB)), ncB = vmul(sg, KN(K_CB));
-    const V ct2 = vsel(conf1, KN(K_TB2), KC(K_CTB2));
-    const V y22 = vmul(y2, y2);
-    // r (rA = r2A·irA enters every sum through an FMA)
-    const V r2A = vfma(y1A, y1A, vfma(aA, aA, y22));
-    const V r2B = vfma(y1B, y1B, vfma(aB, aB, y22));
-    const V irA = vrsqrt(r2A), irB = vrsqrt(r2B);
-    const V rB = vmul(r2B, irB);
-    const V dr = vmul(vfma(dy1, vadd(y1A, y1B), KC(K_DAS)), frcp(vfma(r2A, irA, rB)));
-    const V ndir = vmul(vmul(dr, irA), irB);           // -Δ(1/r)
-    // r + a
-    const V pA = vfma(r2A, irA, aA), pB = vfma(r2B, irB, aB), dp = vadd(dr, da);
-    const V ipA = frcp(pA), ipB = frcp(pB);
-    const V ndip = vmul(vmul(dp, ipA), ipB);           // -Δ(1/(r+a))
-    // z1, z3
-    const V z1A = vfma(y1A, cB, vmul(aA, sB));
-    const V dz1 = vfma(dy1, cB, vmul(da, sB));
-    const V z1B = vadd(z1A, dz1);
-    const V z3A = vfma(y1A, sB, vmul(aA, ncB));
-    const V dz3 = vfma(dy1, sB, vmul(da, ncB));
-    const V z3B = vadd(z3A, dz3);
-    // r - z3, cancellation-free: (z1² + y2²)/(r + z3) when z3 > 0, else (r + z3) - 2 z3
-    const auto posA = vgt0(z3A), posB = vgt0(z3B);
-    const V NA = vfma(z1A, z1A, y22), NB = vfma(z1B, z1B, y22);
-    const V DA = vfma(r2A, irA, z3A), DB = vfma(r2B, irB, z3B);
-    const V uA = vsel(posA, NA, vfma(V(-2.0f), z3A, DA)), vA = vsel(posA, DA, V(1.0f));
-    const V uB = vsel(posB, NB, vfma(V(-2.0f), z3B, DB)), vB = vsel(posB, DB, V(1.0f));
-    const V iuA = frcp(uA), ivA = frcp(vA), iuB = frcp(uB), ivB = frcp(vB);
-    const V iqA = vmul(vA, iuA), iqB = vmul(vB, iuB);
-    const V dN = vmul(dz1, vadd(z1A, z1B));
-    const V dq = vsel(vand(posA, posB), vmul(vmul(vfma(dN, DA, vneg(vmul(NA, vadd(dr, dz3)))), ivA), ivB),
-                      vsub(dr, dz3));
-    const V ndiq = vmul(vmul(dq, iqA), iqB);           // -Δ(1/q)
-    // log differences
-    const V dLp = vlog1p(vmul(dp, ipA));
-    const V dLq = vlog1p(vmul(dq, iqA));
-    // Burgers function difference: rotation of (x, y2) from A to B; y2 keeps its sign so
-    // the rotation never crosses atan2's cut
-    const V xA = vfma(pA, ct2, vneg(y1A));
-    const V dx = vfma(dp, ct2, KN(K_DY1));
-    const V xB = vadd(xA, dx);
-    const V dF = vmul(V(2.0f), vatan2(vmul(vneg(y2), dx), vfma(xA, xB, y22)));
-    // monomials: value at A, value at B, difference
-    const V m1B = vmul(y2, ipB), ndm1 = vmul(y2, ndip);
-    const V m2A = vmul(y1A, ipA), m2B = vmul(y1B, ipB);
-    const V dm2 = vfma(dy1, ipB, vneg(vmul(y1A, ndip)));
-    const V dm3 = vfma(da, ipB, vmul(KN(K_AA), ndip));
-    const V dm4 = vfma(dm2, m1B, vneg(vmul(m2A, ndm1)));
-    const V dm35 = vfma(dm2, vfma(y1A, ipA, m2B), dm3);          // dm3 + dm2 (m2A + m2B)
-    const V dm36 = vfma(ndm1, vneg(vfma(y2, ipA, m1B)), dm3);    // dm3 + dm1 (m1A + m1B)
-    const V y1irA = vmul(y1A, irA), dy1ir = vfma(dy1, irB, vneg(vmul(y1A, ndir)));
-    const V y2irA = vmul(y2, irA), ndy2ir = vmul(y2, ndir);
-    const V nairA = vmul(KN(K_AA), irA), ndair = vfma(KN(K_DA), irB, vmul(aA, ndir));
-    const V m10B = vmul(y2, iqB), ndm10 = vmul(y2, ndiq);
-    const V m11B = vmul(z1B, iqB), dm11 = vfma(dz1, iqB, vneg(vmul(z1A, ndiq)));
-    const V c12 = vmul(sg, KC(K_C1M12));              // signed coefficient of the (m10 · r⁻¹) products
-    // The r⁻¹-weighted monomials share two brackets (distributivity of Δ(u v) = Δu v_B + u_A Δv):
-    //   v1: -b1 Δ(y1 r⁻¹ m1) + b2 Δ(y1 r⁻¹ m2) - b2 Δ(y1 r⁻¹ m11) + c12 Δ(y1 r⁻¹ m10)
-    //       = Δ(y1 r⁻¹)·X1 + (y1 r⁻¹)_A·ΔX1
-    //   v3: the same brackets with a r⁻¹ in place of y1 r⁻¹, negated
-    //   v2: b2 Δ(y1 r⁻¹ m1) + Δ(y2 r⁻¹)·X2 + (y2 r⁻¹)_A·ΔX2
-    // (ndm1, ndm10, ndy2ir: negated differences, folded into the coefficient signs)
-    const V X2 = vfma(KN(K_B1), m1B, vfma(KN(K_B2), m11B, vmul(c12, m10B)));
-    const V dX2 = vfma(KC(K_B1), ndm1, vfma(KN(K_B2), dm11, vneg(vmul(c12, ndm10))));
-    const V X1 = vfma(KC(K_B2), m2B, X2);
-    const V dX1 = vfma(KC(K_B2), dm2, dX2);
-    V v1 = vmul(KC(K_C1F), dF);
-    v1 = vfma(KC(K_C1P), dLp, v1);
-    v1 = vfma(KN(K_KC1), ndm1, v1);
-    v1 = vfma(KN(K_KC2), dm2, v1);
-    v1 = vfma(KN(K_HB2), dm35, v1);
-    v1 = vfma(KC(K_HB1), dm4, v1);
-    v1 = vfma(KN(K_C1M10), ndm10, v1);
-    v1 = vfma(dy1ir, X1, v1);
-    v1 = vfma(y1irA, dX1, v1);
-    v1 = vfma(sg, vfma(KC(K_C1Q), dLq, vmul(KC(K_C1M11), dm11)), v1);
-    V v2 = vmul(KC(K_C2F), dF);
-    v2 = vfma(KC(K_C2P), dLp, v2);
-    v2 = vfma(KC(K_KC2), ndm1, v2);
-    v2 = vfma(KN(K_KC1), dm2, v2);
-    v2 = vfma(KC(K_HB1), dm36, v2);
-    v2 = vfma(KN(K_HB2), dm4, v2);
-    v2 = vfma(KC(K_B2), vfma(dy1ir, m1B, vneg(vmul(y1irA, ndm1))), v2);
-    v2 = vfma(vneg(ndy2ir), X2, v2);
-    v2 = vfma(y2irA, dX2, v2);
-    v2 = vfma(vmul(sg, KC(K_C2Q)), dLq, v2);
-    V v3 = vmul(KC(K_C3F), dF);
-    v3 = vfma(KN(K_KC2), dLp, v3);
-    v3 = vfma(KN(K_NB1), ndm1, v3);
-    v3 = vfma(KN(K_NB2), dm2, v3);
-    v3 = vfma(KN(K_C3M10), ndm10, v3);
-    v3 = vfma(ndair, X1, v3);
-    v3 = vfma(nairA, dX1, v3);
-    v3 = vfma(sg, vfma(KC(K_C3Q), dLq, vmul(KC(K_C3M11), dm11)), v3);
-    // back to EFCS: columns e1 = (c, s, 0), e2 = (s, -c, 0), e3 = (0, 0, -1)
-    ue = vfma(c, v1, vfma(s, v2, ue));
-    un = vfma(s, v1, vfma(KN(K_C), v2, un));
-    uv = vsub(uv, v3);
-}
-
-#undef KC
-#undef KN
 
 // ---------------------------------------------------------------------------
 // CDM likelihood.  One warp per compacted chain slot, lanes over stations.

@@ -18,10 +18,13 @@
 // which leaves the exact posterior invariant.
 #include <math.h>
 #include <stdint.h>
+#include <cooperative_groups.h>
 #include <cuda_bf16.h>
 
 #include "common.cuh"
 #include "internal.h"
+
+namespace cg = cooperative_groups;
 
 namespace ag {
 
@@ -38,66 +41,106 @@ enum Epilogue : int { EPI_NONE = 0, EPI_BIAS = 1, EPI_BIAS_GELU = 2 };
 
 // C(m, n) = Σ_k A(m, k) B(k, n) with A(m,k) = A[m*sam + k*sak], B(k,n) = B[k*sbk + n*sbn]
 // (B in BF16 or FP32), then the epilogue: + bias[n], GELU (pre-activation to Z).
+//
+// 64 x 64 output tile per CTA, 256 threads with 4 x 4 outputs each, k-tiles of 16 staged in
+// shared memory; each operand is read along whichever of its two strides is 1 (coalesced
+// rows of 16 k or of 64 m / n) and the next k-tile is prefetched into registers while the
+// current one is multiplied.  Split K: the gridDim.z CTAs of one tile form a thread-block
+// cluster, each multiplies one K range, and the partial tiles are summed through
+// distributed shared memory in rank order (deterministic), each CTA reducing and writing
+// BM / gridDim.z rows.
+template <bool B_BF16>
+AG_DEVICE_INLINE float load_b(const void* Bv, long idx) {
+    return B_BF16 ? __bfloat162float(reinterpret_cast<const __nv_bfloat16*>(Bv)[idx])
+                  : reinterpret_cast<const float*>(Bv)[idx];
+}
+
 template <bool B_BF16>
 __global__ void __launch_bounds__(256) gemm_kernel(int M, int N, int K, const float* __restrict__ A,
                                                    long sam, long sak, const void* __restrict__ Bv,
                                                    long sbk, long sbn, float* __restrict__ C, long ldc,
                                                    const float* __restrict__ bias, int epi,
                                                    float* __restrict__ Z) {
-    __shared__ float As[BK][BM + 4];
-    __shared__ float Bs[BK][BN + 4];
-    const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+    __shared__ __align__(16) float As[BK][BM + 4];
+    __shared__ __align__(16) float Bs[BK][BN + 4];
+    __shared__ __align__(16) float Ps[BM][BN];          // partial tile (split K)
+    const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
     const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+    const int split = gridDim.z, part = blockIdx.z;
+    const int kchunk = ((K + split - 1) / split + BK - 1) / BK * BK;
+    const int kb = min(K, part * kchunk), ke = min(K, kb + kchunk);
+    // element e of a 16 x 64 operand tile: (k, m) with k fastest when that stride is 1
+    const bool a_k1 = (sak == 1), b_k1 = (sbk == 1);
+    float ra[4], rb[4];
+    auto fetch = [&](int k0) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int e = tid + 256 * q;
+            int kk = a_k1 ? e % BK : e / BM, mm = a_k1 ? e / BK : e % BM;
+            int m = m0 + mm, k = k0 + kk;
+            ra[q] = (m < M && k < ke) ? A[(long)m * sam + (long)k * sak] : 0.f;
+            kk = b_k1 ? e % BK : e / BN;
+            const int nn = b_k1 ? e / BK : e % BN;
+            const int n = n0 + nn;
+            k = k0 + kk;
+            rb[q] = (n < N && k < ke) ? load_b<B_BF16>(Bv, (long)k * sbk + (long)n * sbn) : 0.f;
+        }
+    };
+    auto stash = [&]() {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int e = tid + 256 * q;
+            As[a_k1 ? e % BK : e / BM][a_k1 ? e / BK : e % BM] = ra[q];
+            Bs[b_k1 ? e % BK : e / BN][b_k1 ? e / BK : e % BN] = rb[q];
+        }
+    };
     float acc[4][4] = {};
-    for (int k0 = 0; k0 < K; k0 += BK) {
-        for (int e = threadIdx.x; e < BK * BM; e += 256) {
-            const int kk = e / BM, mm = e % BM;
-            const int m = m0 + mm, k = k0 + kk;
-            As[kk][mm] = (m < M && k < K) ? A[(long)m * sam + (long)k * sak] : 0.f;
-        }
-        for (int e = threadIdx.x; e < BK * BN; e += 256) {
-            const int kk = e / BN, nn = e % BN;
-            const int n = n0 + nn, k = k0 + kk;
-            float v = 0.f;
-            if (n < N && k < K) {
-                const long idx = (long)k * sbk + (long)n * sbn;
-                v = B_BF16 ? __bfloat162float(reinterpret_cast<const __nv_bfloat16*>(Bv)[idx])
-                           : reinterpret_cast<const float*>(Bv)[idx];
-            }
-            Bs[kk][nn] = v;
-        }
+    if (kb < ke) fetch(kb);
+    for (int k0 = kb; k0 < ke; k0 += BK) {
+        stash();
         __syncthreads();
+        if (k0 + BK < ke) fetch(k0 + BK);
 #pragma unroll
         for (int kk = 0; kk < BK; ++kk) {
-            float a[4], b[4];
-#pragma unroll
-            for (int i = 0; i < 4; ++i) a[i] = As[kk][ty * 4 + i];
-#pragma unroll
-            for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx * 4 + j];
+            const float4 a = *reinterpret_cast<const float4*>(&As[kk][ty * 4]);
+            const float4 b = *reinterpret_cast<const float4*>(&Bs[kk][tx * 4]);
+            const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w};
 #pragma unroll
             for (int i = 0; i < 4; ++i)
 #pragma unroll
-                for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+                for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
         }
         __syncthreads();
     }
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        const int m = m0 + ty * 4 + i;
-        if (m >= M) continue;
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const int n = n0 + tx * 4 + j;
-            if (n >= N) continue;
-            float v = acc[i][j];
-            if (epi != EPI_NONE) v += bias[n];
-            if (epi == EPI_BIAS_GELU) {
-                Z[(long)m * ldc + n] = v;
-                v = gelu(v);
-            }
-            C[(long)m * ldc + n] = v;
+    auto store = [&](int m, int n, float v) {
+        if (m >= M || n >= N) return;
+        if (epi != EPI_NONE) v += bias[n];
+        if (epi == EPI_BIAS_GELU) {
+            Z[(long)m * ldc + n] = v;
+            v = gelu(v);
         }
+        C[(long)m * ldc + n] = v;
+    };
+    if (split == 1) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) store(m0 + ty * 4 + i, n0 + tx * 4 + j, acc[i][j]);
+        return;
     }
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+        *reinterpret_cast<float4*>(&Ps[ty * 4 + i][tx * 4]) = make_float4(acc[i][0], acc[i][1], acc[i][2], acc[i][3]);
+    cg::cluster_group cluster = cg::this_cluster();
+    cluster.sync();
+    const int rows = BM / split, r0 = part * rows;
+    for (int e = tid; e < rows * BN; e += 256) {
+        const int mm = r0 + e / BN, nn = e % BN;
+        float v = 0.f;
+        for (int r = 0; r < split; ++r) v += cluster.map_shared_rank(&Ps[0][0], r)[mm * BN + nn];
+        store(m0 + mm, n0 + nn, v);
+    }
+    cluster.sync();                                     // partial tiles stay alive until all have read them
 }
 
 // θ (FP64, N x p) -> x = 2 (θ - lo)/(hi - lo) - 1 (FP32); optional index list
@@ -166,23 +209,41 @@ __global__ void to_bf16_kernel(long count, const float* __restrict__ p, __nv_bfl
     if (e < count) q[e] = __float2bfloat16_rn(p[e]);
 }
 
-// llk_s = norm - ½ (q0 - 2 hᵀ c̃ + c̃ᵀ G c̃), c̃ = scale ⊙ c ; one warp per chain
-__global__ void surrogate_llk_kernel(int n, int k, const float* __restrict__ coeff,
-                                     const float* __restrict__ scale, const float* __restrict__ G,
-                                     const float* __restrict__ h, double q0, double norm,
-                                     double* __restrict__ llk) {
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (warp >= n) return;
-    const float* c = coeff + (long)warp * k;
-    double acc = 0.0;
-    for (int a = lane; a < k; a += 32) {
-        const float ca = c[a] * scale[a];
-        float row = 0.f;
-        for (int b = 0; b < k; ++b) row = fmaf(G[a * k + b], c[b] * scale[b], row);
-        acc += (double)ca * (double)row - 2.0 * (double)h[a] * (double)ca;
+// llk_s = norm - ½ (q0 - 2 hᵀ c̃ + c̃ᵀ G c̃), c̃ = scale ⊙ c ; one warp per chain.  Each CTA
+// stages Gᵀ in shared memory once (lane a then reads column a of a row of Gᵀ: consecutive
+// words, no bank conflict) and walks chains with a grid stride; the warp's c̃ goes through
+// shared memory and is read as a broadcast.
+constexpr int kSurMaxK = 96;
+constexpr int kSurWarps = 8;
+__global__ void __launch_bounds__(kSurWarps * 32)
+surrogate_llk_kernel(int n, int k, const float* __restrict__ coeff, const float* __restrict__ scale,
+                     const float* __restrict__ G, const float* __restrict__ h, double q0, double norm,
+                     double* __restrict__ llk) {
+    extern __shared__ float s_mem[];
+    float* sGT = s_mem;                                  // k x k, sGT[b k + a] = G[a k + b]
+    float* sc = s_mem + k * k + (threadIdx.x >> 5) * k;  // this warp's c̃
+    for (int e = threadIdx.x; e < k * k; e += blockDim.x) {
+        const int a = e / k, b = e - a * k;
+        sGT[b * k + a] = G[e];
     }
-    acc = warp_sum(acc);
-    if (lane == 0) llk[warp] = norm - 0.5 * (q0 + acc);
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int stride = gridDim.x * kSurWarps;
+    for (int i = blockIdx.x * kSurWarps + (threadIdx.x >> 5); i < n; i += stride) {
+        const float* c = coeff + (long)i * k;
+        for (int b = lane; b < k; b += 32) sc[b] = c[b] * scale[b];
+        __syncwarp();
+        double acc = 0.0;
+        for (int a = lane; a < k; a += 32) {
+            const float ca = sc[a];
+            float row = 0.f;
+            for (int b = 0; b < k; ++b) row = fmaf(sGT[b * k + a], sc[b], row);
+            acc += (double)ca * (double)row - 2.0 * (double)h[a] * (double)ca;
+        }
+        acc = warp_sum(acc);
+        if (lane == 0) llk[i] = norm - 0.5 * (q0 + acc);
+        __syncwarp();
+    }
 }
 
 // Stage 1 of delayed acceptance: surrogate Metropolis test and compaction of survivors
@@ -310,13 +371,31 @@ extern "C" int64_t ag_mlp_activation_floats(const ag_mlp* net, int32_t n) {
     return c;
 }
 
+// Split K over a cluster of up to 8 CTAs when the output tiles alone would leave most of the
+// GPU idle (the weight gradients: a few tiles, K = batch rows).
 static int gemm(cudaStream_t s, int M, int N, int K, const float* A, long sam, long sak, const void* B,
                 bool bbf16, long sbk, long sbn, float* C, long ldc, const float* bias, int epi, float* Z) {
-    dim3 grid(nblk(N, BN), nblk(M, BM));
-    if (bbf16)
-        gemm_kernel<true><<<grid, 256, 0, s>>>(M, N, K, A, sam, sak, B, sbk, sbn, C, ldc, bias, epi, Z);
-    else
-        gemm_kernel<false><<<grid, 256, 0, s>>>(M, N, K, A, sam, sak, B, sbk, sbn, C, ldc, bias, epi, Z);
+    const int tiles = nblk(N, BN) * nblk(M, BM);
+    int split = 1;
+    while (split < 8 && tiles * split < 128 && K >= 2 * BK * (split * 2)) split *= 2;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(nblk(N, BN), nblk(M, BM), split);
+    cfg.blockDim = dim3(256, 1, 1);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 1;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = split;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaError_t e = bbf16 ? cudaLaunchKernelEx(&cfg, gemm_kernel<true>, M, N, K, A, sam, sak, B, sbk, sbn, C, ldc,
+                                               bias, epi, Z)
+                          : cudaLaunchKernelEx(&cfg, gemm_kernel<false>, M, N, K, A, sam, sak, B, sbk, sbn, C, ldc,
+                                               bias, epi, Z);
+    int rc = cuda_status(e, "cudaLaunchKernelEx(gemm_kernel)");
+    if (rc) return rc;
     return launch_status("gemm_kernel");
 }
 
@@ -425,8 +504,16 @@ extern "C" int ag_surrogate_llk(int32_t n, int32_t k, const float* coeff, const 
                                 const float* gram, const float* h, double q0, double norm, double* llk,
                                 void* stream) {
     AG_REQUIRE(n > 0 && k > 0 && coeff && scale && gram && h && llk, "invalid arguments");
-    surrogate_llk_kernel<<<nblk((long)n * 32, 256), 256, 0, as_stream(stream)>>>(n, k, coeff, scale, gram, h,
-                                                                               q0, norm, llk);
+    AG_REQUIRE(k <= kSurMaxK, "at most %d surrogate coefficients are supported (got %d)", kSurMaxK, k);
+    const size_t smem = (size_t)(k * k + kSurWarps * k) * sizeof(float);
+    int dev = 0, sms = 0;
+    int rc = cuda_status(cudaGetDevice(&dev), "cudaGetDevice");
+    if (rc) return rc;
+    rc = cuda_status(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "multiProcessorCount");
+    if (rc) return rc;
+    const int grid = min(nblk(n, kSurWarps), 4 * sms);
+    surrogate_llk_kernel<<<grid, kSurWarps * 32, smem, as_stream(stream)>>>(n, k, coeff, scale, gram, h, q0,
+                                                                           norm, llk);
     return launch_status("surrogate_llk_kernel");
 }
 

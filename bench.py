@@ -37,12 +37,14 @@ LOS = (0.38, -0.08, 0.92)
 PRIORS = [(-1e4, 1e4), (-1e4, 1e4), (1e3, 1e4), (-50.0, 50.0), (100.0, 3000.0), (100.0, 3000.0),
           (100.0, 3000.0), (-90.0, 90.0), (-90.0, 90.0), (-90.0, 90.0)]
 # parameter order: x0, y0, depth, opening, ax, ay, az, ωx, ωy, ωz
-# FP32 operations per (chain, station) pair of the fused CDM kernel, counted from
-# altar_gb300/csrc/forward.cu and common.cuh (FMA = 2): per rectangle side 225 for the
-# difference-arithmetic pair + 2 x 18 (log1p_series) + 21 (atan2_poly) = 282, times 12
-# sides, + 31 per station (coordinates, LOS projection, float-float misfit);
-# special-function unit: 12 per side (2 rsqrt, 10 rcp)
-CDM_FLOP_PER_PAIR = 3415
+# FP32 operations per (chain, station) pair of the fused CDM kernel (FMA = 2): per
+# rectangle side 249 (the difference-arithmetic pair of altar_gb300/csrc/cdm_side.cuh
+# including 2 x 10 for log2_ratio and 21 for atan2_poly, counted by evaluating the pair
+# with a counting number type: tests/cdm_host/cdm_host.cpp), times 12 sides, + 31 per
+# station (coordinates, LOS projection, float-float misfit); special-function unit: 13
+# per side (2 rsqrt, 9 rcp, 2 lg2)
+CDM_FLOP_PER_PAIR = 3019
+CDM_SFU_PER_SIDE = 13
 L2_FLUSH_BYTES = 256 << 20
 
 

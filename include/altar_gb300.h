@@ -365,7 +365,7 @@ int ag_adam_step(int64_t count, float* params, const float* grads, float* m, flo
                  float lr, float b1, float b2, float eps, uint16_t* params_bf16, void* stream);
 /* BF16 copy of an FP32 buffer */
 int ag_to_bf16(int64_t count, const float* src, uint16_t* dst, void* stream);
-/* llk = norm - 1/2 (q0 - 2 hᵀ c̃ + c̃ᵀ G c̃) with c̃ = scale ⊙ coeff (n x k) */
+/* llk = norm - 1/2 (q0 - 2 hᵀ c̃ + c̃ᵀ G c̃) with c̃ = scale ⊙ coeff (n x k, k <= 96) */
 int ag_surrogate_llk(int32_t n, int32_t k, const float* coeff, const float* scale, const float* gram,
                      const float* h, double q0, double norm, double* llk, void* stream);
 /* delayed-acceptance stage 1 (Christen & Fox 2005): surrogate Metropolis test; survivors are

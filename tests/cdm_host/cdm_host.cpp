@@ -1,0 +1,94 @@
+// Host build of the CDM per-side arithmetic of the likelihood kernel (test harness).
+//
+// The device header altar_gb300/csrc/cdm_side.cuh is compiled here with g++ so that
+// its formulas can be checked on a machine without a GPU:
+//   * cdm_host_los: displacements of one source at a set of stations, with the device
+//     intrinsics replaced by correctly rounded host operations (the kernel's approximate
+//     reciprocal, reciprocal square root and base-2 logarithm differ from these by a
+//     few ulp), to compare against the FP64 oracle;
+//   * cdm_host_side_counts: the static operation count of one side (FP32 FLOP with an
+//     FMA counted as 2, and special-function operations), by evaluating the pair with a
+//     counting number type.
+#include <cmath>
+#include <cstdint>
+
+#define __host__
+#define __device__
+#define __forceinline__ inline
+#define __align__(n) alignas(n)
+struct float4 { float x, y, z, w; };
+static inline float4 make_float4(float a, float b, float c, float d) { return {a, b, c, d}; }
+static inline float __fadd_rn(float a, float b) { return a + b; }
+static inline float __fsub_rn(float a, float b) { return a - b; }
+static inline float __fmul_rn(float a, float b) { return a * b; }
+static inline float __fdividef(float a, float b) { return a / b; }
+static inline float rsqrtf(float x) { return 1.0f / std::sqrt(x); }
+#define __log2f(x) std::log2(x)
+static inline void sincospi(double x, double* s, double* c) {
+    *s = std::sin(M_PI * x);
+    *c = std::cos(M_PI * x);
+}
+#define AG_DEVICE_INLINE inline
+#define AG_CDM_FN inline
+#include "../../altar_gb300/csrc/cdm_side.cuh"
+
+using namespace ag;
+
+// parameter positions of the CDM workload layout: x, y, depth, opening, ax, ay, az, ωx, ωy, ωz
+struct HostLayout { int x_idx, depth_idx, strength_idx, axes_idx, omega_idx; double nu; };
+
+extern "C" int cdm_host_los(const double* th, int n, const double* X, const double* Y, const double* los,
+                            double nu, double* out) {
+    HostLayout L{0, 2, 3, 4, 7, nu};
+    Vec3 V[3][4];
+    if (cdm_corners(th, L, V)) return -1;
+    SideC side[kSides];
+    const double x0 = th[0], y0 = th[1];
+    const uint32_t mask = cdm_sides(th, L, V, x0, y0, side);
+    float x0h, x0l, y0h, y0l;
+    split_hilo(x0, x0h, x0l);
+    split_hilo(y0, y0h, y0l);
+    for (int j = 0; j < n; ++j) {
+        float ah, al, bh, bl;
+        split_hilo(X[j], ah, al);
+        split_hilo(Y[j], bh, bl);
+        const float Xr = (ah - x0h) + (al - x0l), Yr = (bh - y0h) + (bl - y0l);
+        float ue = 0.f, un = 0.f, uv = 0.f;
+        for (int k = 0; k < kSides; ++k)
+            if (mask >> k & 1u) side_pair<float>(ScalarSide(side[k]), Xr, Yr, ue, un, uv);
+        out[j] = (double)ue * los[3 * j] + (double)un * los[3 * j + 1] + (double)uv * los[3 * j + 2];
+    }
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// operation counting
+static long g_flop = 0, g_sfu = 0;
+struct CountF { float v; CountF() {} CountF(float x) : v(x) {} };
+struct CountB { bool v; };
+inline CountF vfma(CountF a, CountF b, CountF c) { g_flop += 2; return std::fma(a.v, b.v, c.v); }
+inline CountF vadd(CountF a, CountF b) { g_flop += 1; return a.v + b.v; }
+inline CountF vsub(CountF a, CountF b) { g_flop += 1; return a.v - b.v; }
+inline CountF vmul(CountF a, CountF b) { g_flop += 1; return a.v * b.v; }
+inline CountF vneg(CountF a) { return -a.v; }
+inline CountB vge0(CountF a) { return {a.v >= 0.f}; }
+inline CountB vgt0(CountF a) { return {a.v > 0.f}; }
+inline CountB vand(CountB a, CountB b) { return {a.v && b.v}; }
+inline CountF vsel(CountB c, CountF a, CountF b) { return c.v ? a : b; }
+inline CountF frcp(CountF x) { g_sfu += 1; return 1.0f / x.v; }
+inline CountF vrsqrt(CountF x) { g_sfu += 1; return 1.0f / std::sqrt(x.v); }
+// log2_ratio: s², 4 FMA, s·p (10 FLOP) + one base-2 logarithm
+inline CountF vlog2r(CountF s, CountF r) { g_flop += 10; g_sfu += 1; return log2_ratio(s.v, r.v); }
+// atan2_poly: mn/mx (mul), t², 8 FMA, t·p, two quadrant subtractions (21 FLOP) + one reciprocal
+inline CountF vatan2(CountF y, CountF x) { g_flop += 21; g_sfu += 1; return atan2_poly(y.v, x.v); }
+
+extern "C" void cdm_host_side_counts(long* flop, long* sfu) {
+    SideC S;
+    bool act;
+    fill_side(S, Vec3{100, 200, -3000}, Vec3{900, -300, -2500}, Vec3{1, 2, 3}, 0.25, 0, 0, act);
+    CountF ue(0.f), un(0.f), uv(0.f);
+    g_flop = g_sfu = 0;
+    side_pair<CountF>(ScalarSide(S), CountF(1000.f), CountF(-2000.f), ue, un, uv);
+    *flop = g_flop;
+    *sfu = g_sfu;
+}

@@ -1,0 +1,72 @@
+"""The CDM likelihood kernel's per-side arithmetic, compiled for the host (no GPU).
+
+tests/cdm_host/cdm_host.cpp builds altar_gb300/csrc/cdm_side.cuh with g++, the device
+intrinsics replaced by correctly rounded host operations.  Checked here:
+  * the formulas against the FP64 oracle (models/cdm/cdm/libcdm.py restated in
+    oracle/cdm.py) on prior sources, with the same normwise tolerances the GPU tests use
+    for sources whose sides lie at least 10° from the vertical;
+  * the static FP32 operation count of one pair, which bench.py's roofline uses.
+"""
+import ctypes
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from oracle import cdm
+
+from gpu_helpers import CDM_LAYOUT, LOS, cdm_prior_rows, min_vertical_angle
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+P = ctypes.POINTER
+
+
+@pytest.fixture(scope="module")
+def host(tmp_path_factory):
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("g++ not available")
+    so = str(tmp_path_factory.mktemp("cdm_host") / "cdm_host.so")
+    subprocess.run([cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared",
+                    os.path.join(HERE, "cdm_host", "cdm_host.cpp"), "-o", so], check=True)
+    lib = ctypes.CDLL(so)
+    lib.cdm_host_los.argtypes = [P(ctypes.c_double), ctypes.c_int, P(ctypes.c_double), P(ctypes.c_double),
+                                 P(ctypes.c_double), ctypes.c_double, P(ctypes.c_double)]
+    lib.cdm_host_los.restype = ctypes.c_int
+    lib.cdm_host_side_counts.argtypes = [P(ctypes.c_long), P(ctypes.c_long)]
+    return lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(P(ctypes.c_double))
+
+
+def test_flop_count_matches_bench_constant(host):
+    import bench
+    flop, sfu = ctypes.c_long(), ctypes.c_long()
+    host.cdm_host_side_counts(ctypes.byref(flop), ctypes.byref(sfu))
+    # 12 sides + per station: relative coordinates (6), LOS projection (5), residual (1),
+    # float-float w·r² accumulation (19)
+    assert 12 * flop.value + 31 == bench.CDM_FLOP_PER_PAIR
+    assert sfu.value == bench.CDM_SFU_PER_SIDE
+
+
+def test_side_arithmetic_against_oracle(host):
+    g = np.linspace(-20e3, 20e3, 30)
+    X, Y = [np.ascontiguousarray(a.ravel()) for a in np.meshgrid(g, g)]
+    los = np.ascontiguousarray(np.tile(LOS, (X.size, 1)))
+    theta = cdm_prior_rows(24, seed=3)
+    errs, flat = [], []
+    for th in theta:
+        ref = cdm.los_displacements(th, CDM_LAYOUT, X, Y, los, 0.25)
+        out = np.empty(X.size)
+        t = np.ascontiguousarray(th, dtype=np.float64)
+        assert host.cdm_host_los(_dp(t), X.size, _dp(X), _dp(Y), _dp(los), 0.25, _dp(out)) == 0
+        errs.append(np.max(np.abs(out - ref)) / np.max(np.abs(ref)))
+        flat.append(min_vertical_angle(th) >= 10.0)
+    errs, flat = np.array(errs), np.array(flat)
+    assert flat.sum() >= 16
+    assert np.all(errs[flat] <= 1e-4), errs[flat].max()
+    assert np.median(errs) <= 5e-6, np.median(errs)

@@ -1,11 +1,14 @@
 """Forward models + misfit on the GPU against the oracle and the reference fixtures.
 
 Tolerances (FP32 device arithmetic against FP64 references):
-  * CDM LOS displacement, per source, normwise: |u_gpu - u_ref|_inf <= TOL_CDM * |u_ref|_inf
-    for sources whose sides all lie at least 10° from the vertical; near-vertical sides
-    lose accuracy in the angular-dislocation formula itself (terms ~cot²β cancel) and are
-    checked with the looser TOL_CDM_STEEP.  The median error over sources must stay
-    below TOL_CDM_MEDIAN.
+  * CDM LOS displacement, per source, normwise: |u_gpu - u_ref|_inf <= tol * |u_ref|_inf
+    with tol = TOL_CDM for sources whose sides all lie at least 10° from the vertical.
+    Near-vertical sides lose accuracy in the angular-dislocation formula itself: its
+    coefficients grow like cot²β and the terms they multiply cancel, so FP32 rounding
+    (of the coefficients and of the arithmetic) is amplified by ~cot²β.  Sources with a
+    side 2-10° from the vertical are checked against TOL_CDM_STEEP, those with a side
+    within 2° against TOL_CDM_VERTICAL (a side 0.2° from the vertical: cot²β ≈ 8e4).
+    The median error over sources must stay below TOL_CDM_MEDIAN.
   * Mogi LOS displacement: normwise 1e-5.
   * log-likelihood given the device's own FP32 residuals: 1e-9 relative (FP64 oracle sum).
 """
@@ -25,7 +28,14 @@ pytestmark = pytest.mark.gpu
 
 TOL_CDM = 1e-4
 TOL_CDM_MEDIAN = 5e-6
-TOL_CDM_STEEP = 5e-2
+TOL_CDM_STEEP = 1e-3
+TOL_CDM_VERTICAL = 1e-1
+
+
+def tol_cdm(th):
+    """Normwise tolerance of a source by the smallest angle between its sides and the vertical."""
+    a = min_vertical_angle(th)
+    return TOL_CDM if a >= 10.0 else TOL_CDM_STEEP if a >= 2.0 else TOL_CDM_VERTICAL
 G = np.load(os.path.join(os.path.dirname(__file__), "golden", "cdm_golden.npz"))
 
 
@@ -55,8 +65,7 @@ def test_cdm_matches_reference_fixtures(cuda):
     for k, u in enumerate(G["ref_u"]):
         ref = u[0] * LOS[0] + u[1] * LOS[1] + u[2] * LOS[2]
         err = np.max(np.abs(res[k] - ref)) / np.max(np.abs(ref))
-        steep = min_vertical_angle(theta[k]) < 10.0
-        assert err <= (TOL_CDM_STEEP if steep else TOL_CDM), (k, err)
+        assert err <= tol_cdm(theta[k]), (k, err)
         errs.append(err)
     assert np.median(errs) <= TOL_CDM_MEDIAN
 
@@ -72,8 +81,7 @@ def test_cdm_matlab_goldens(cuda):
         _, res = _residuals(strat, th, 12)
         ref = G[comp] * 1e3                                 # displacement scales with length
         # the Matlab source's body z axis is ~9° from the vertical: near-vertical class
-        tol = TOL_CDM_STEEP if min_vertical_angle(th[0]) < 10.0 else TOL_CDM
-        assert np.max(np.abs(res[0] - ref)) <= tol * np.max(np.abs(ref)), comp
+        assert np.max(np.abs(res[0] - ref)) <= tol_cdm(th[0]) * np.max(np.abs(ref)), comp
         assert np.max(np.abs(res[0] - ref)) <= 1e-4 * np.max(np.abs(ref)), comp
 
 
@@ -87,9 +95,9 @@ def test_cdm_prior_sources_workload_grid(cuda):
     strat, _ = cdm_strategy(X, Y, los, np.zeros(X.size), np.full(X.size, 9e-6))
     _, res = _residuals(strat, theta, X.size)
     errs = np.max(np.abs(res - ref), 1) / np.max(np.abs(ref), 1)
-    steep = np.array([min_vertical_angle(t) < 10.0 for t in theta])
-    assert np.all(errs[~steep] <= TOL_CDM), errs[~steep].max()
-    assert np.all(errs[steep] <= TOL_CDM_STEEP)
+    tol = np.array([tol_cdm(t) for t in theta])
+    steep = tol > TOL_CDM
+    assert np.all(errs <= tol), [(e, t) for e, t in zip(errs, tol) if e > t]
     assert np.median(errs) <= TOL_CDM_MEDIAN
     print(f"CDM normwise error: median {np.median(errs):.2e}, max (>=10deg) {errs[~steep].max():.2e}")
 
