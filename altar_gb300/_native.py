@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "_lib")
 LIBPATH = os.path.join(LIBDIR, "libaltar_gb300.so")
-SOURCES = ("forward.cu", "stage.cu", "surrogate.cu", "linear.cu", "api.cu")
+SOURCES = ("forward.cu", "stage.cu", "surrogate.cu", "linear.cu", "reverso.cu", "api.cu")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 
@@ -106,6 +106,14 @@ class WhitenBlock(ctypes.Structure):
     _fields_ = [("w64", c_void_p), ("w_split", c_void_p), ("col0", c_int32), ("m", c_int32)]
 
 
+class ReversoModel(ctypes.Structure):
+    _fields_ = [("txy", c_void_p), ("d", c_void_p), ("w", c_void_p), ("n_obs", c_int32), ("nparams", c_int32),
+                ("qin_idx", c_int32), ("hs_idx", c_int32), ("hd_idx", c_int32), ("as_idx", c_int32),
+                ("ad_idx", c_int32), ("ac_idx", c_int32), ("east_cos", c_int32), ("reserved", c_int32),
+                ("G", ctypes.c_double), ("v", ctypes.c_double), ("mu", ctypes.c_double),
+                ("drho", ctypes.c_double), ("g", ctypes.c_double)]
+
+
 class MLP(ctypes.Structure):
     _fields_ = [("nlayers", c_int32), ("sizes", c_int32 * 9)]
 
@@ -132,6 +140,7 @@ _SIGNATURES = {
     "ag_linear_llk_fp64": (c_int, [P, P, c_int32, c_double, P, P]),
     "ag_whiten_workspace_bytes": (c_size_t, [c_int32, c_int32]),
     "ag_whiten_llk": (c_int, [P, P, c_int32, c_int32, P, P, c_size_t, P, P]),
+    "ag_reverso_llk": (c_int, [P, P, c_int32, ctypes.c_double, P, P, P, P]),
     "ag_mlp_param_count": (ctypes.c_int64, [P]),
     "ag_mlp_activation_floats": (ctypes.c_int64, [P, c_int32]),
     "ag_normalize_inputs": (c_int, [P, c_int32, c_int32, P, P, P, P]),

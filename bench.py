@@ -48,20 +48,42 @@ CDM_SFU_PER_SIDE = 13
 L2_FLUSH_BYTES = 256 << 20
 
 
-def problem(seed=2024):
-    from oracle import cdm, cref
+def problem(seed=2024, on_device=True):
+    """Synthetic CDM data: a truth drawn from the priors (redrawn while the source
+    crosses the free surface), its LOS displacements, plus N(0, σ²) noise.  The GPU arm
+    computes the displacements with the library's own FP32 kernel (the residuals of an
+    all-zero data set); the CPU reference arm (on_device=False) with the FP64 C
+    restatement it times.  Both draw the same truth and the same noise."""
     g = np.linspace(-SPAN, SPAN, M_SIDE)
     X, Y = [a.ravel() for a in np.meshgrid(g, g)]
     los = np.tile(LOS, (X.size, 1))
     rng = np.random.default_rng(seed)
+    if not on_device:
+        from oracle import cdm, cref
+        while True:
+            th = np.array([rng.uniform(*b) for b in PRIORS])
+            if not cdm.above_surface(th[0], th[1], th[2], *th[4:7], *th[7:10]):
+                break
+        u, bad = cref.cdm_los(th, cref.RefLayout(10, 0, 2, 3, 4, 7, 0, 0.25), X, Y, los)
+        return X, Y, los, u + rng.normal(0.0, SIGMA, X.size), th
+    import torch
+    from altar_gb300 import _native
+    from altar_gb300.models import CDM
+    from altar_gb300.models.forward import CUDA
+    from altar_gb300.models.observations import Observations
+    model = CDM(cdm_psets(), observations=Observations(X, Y, los, np.zeros(X.size), np.ones(X.size)))
+    model.initializeParameterSets()
+    strat = CUDA(_native.AG_MODEL_CDM).initialize(None, model)
+    out = torch.empty(1, dtype=torch.float64, device="cuda")
+    res = torch.zeros(1, strat.stations.m_padded, dtype=torch.float32, device="cuda")
     while True:
         th = np.array([rng.uniform(*b) for b in PRIORS])
-        if not cdm.above_surface(th[0], th[1], th[2], *th[4:7], *th[7:10]):
+        status = torch.zeros(1, dtype=torch.int32, device="cuda")
+        strat.forward(torch.from_numpy(th[None]).cuda(), out, status=status, residuals=res)
+        if int(status.item()) == 0:
             break
-    lay = cref.RefLayout(10, 0, 2, 3, 4, 7, 0, 0.25)
-    u, bad = cref.cdm_los(th, lay, X, Y, los)
-    d = u + rng.normal(0.0, SIGMA, X.size)
-    return X, Y, los, d, th
+    u = res[0, :X.size].double().cpu().numpy()
+    return X, Y, los, u + rng.normal(0.0, SIGMA, X.size), th
 
 
 def peaks():
@@ -167,7 +189,7 @@ def run_reference(args):
     # under torchrun only rank 0 measures; the CPU arm needs no process group
     if int(os.environ.get("RANK", "0")) != 0:
         return 0
-    X, Y, los, d, truth = problem()
+    X, Y, los, d, truth = problem(on_device=False)
     chains = args.cpu_chains
     rates, threads = [], os.cpu_count() or 1
     for i in range(args.warmup + args.steps):
@@ -333,6 +355,95 @@ def run_linear(args):
                          "note": "achieved counts 2·M·P·N; the split-BF16 GEMM executes 3x that"},
             "fp64_cuda_cores_ms": t64 * 1e3,
             "clocks": clk.summary()}))
+    return 0
+
+
+def reverso_cpu_baseline(theta, txy, d, var):
+    """The FP64 oracle's Reverso likelihoods of the same samples on one host core
+    (seconds, values): the CPU baseline, and the check of the device's values."""
+    from oracle import reverso as oracle_reverso
+    t0 = time.perf_counter()
+    ref = oracle_reverso.data_llk(theta, txy, d, var, east_cos=True)
+    return time.perf_counter() - t0, ref
+
+
+def run_reverso(args):
+    """The reference's Reverso example (models/reverso/examples/reverso.pfg): 4,096 chains,
+    20 Metropolis steps per stage, the 35-point synthetic case of
+    examples/synthetic/reverso.py, the default ("fast") strategy, annealed from the prior
+    to β = 1.  Reports the time to β = 1 of a run after an untimed one (graph capture,
+    first launches), the FP64 likelihood kernel alone, and the FP64 oracle evaluating the
+    same likelihoods on one host core."""
+    import torch
+    from altar_gb300 import Application
+    from altar_gb300.bayesian import Annealer
+    from altar_gb300.distributions import Uniform
+    from altar_gb300.models import Contiguous, Reverso
+    from altar_gb300.simulations import RNG, Job
+    from altar_gb300.models.reverso import PSETS
+    rank, world, local, dist = dist_setup()
+    torch.cuda.set_device(local)
+    N = args.chains if args.chains != 32768 else 4096
+    priors = [(0.4, 0.8), (2500.0, 3500.0), (3500.0, 4500.0), (1500.0, 2500.0), (1500.0, 2500.0), (1.0, 2.0)]
+    # the synthetic case of examples/synthetic/reverso.py: times 10^-6 .. 1 yr, 1-5 km east,
+    # the generator's convention (u_E = u_r sin φ), σ² = max(0.05 u, 0.01)²; displacements by
+    # the library's own kernel at the generator's default parameters
+    year = 365.25 * 24 * 3600
+    txy = np.array([(10.0 ** e * year, float(r), 0.0) for e in range(-6, 1) for r in range(1000, 6000, 1000)])
+    psets = lambda: {name: Contiguous(1, Uniform(b)) for name, b in zip(PSETS, priors)}
+    gen = Reverso(psets(), txy=txy, d=np.zeros_like(txy), var=np.ones_like(txy), mode="analytic")
+    gen.initialize(Application(gen, job=Job(chains=1, steps=1), rng=RNG(0)))
+    truth = torch.tensor([[0.6, 3.0e3, 4.0e3, 2.0e3, 2.2e3, 1.5]], dtype=torch.float64, device="cuda")
+    d = gen.displacements(truth)[0].cpu().numpy()
+    var = np.maximum(0.05 * d, 0.01) ** 2
+
+    def run(seed):
+        model = Reverso(psets(), txy=txy, d=d, var=var, mode="fast")
+        app = Application(model, job=Job(chains=N, steps=20), rng=RNG(seed + rank), controller=Annealer())
+        app.initialize()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        app.controller.posterior(model, max_stages=args.max_stages)
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0, app
+
+    run(11)
+    times, stages, steps = [], [], 0
+    for k in range(max(1, args.steps)):
+        dt, app = run(100 + k)
+        reps = app.controller.worker.reports
+        times.append(dt)
+        stages.append(len(reps))
+        steps += sum(r["accepted"] + r["rejected"] + r["unlikely"] for r in reps)
+        final_beta = reps[-1]["beta"]
+    model = app.model
+    theta = app.controller.worker.step.theta
+    out = torch.empty(N, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream()
+    for _ in range(3):
+        model.forward(theta, out)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(10)]
+    for a, b in evs:
+        a.record(stream)
+        model.forward(theta, out)
+        b.record(stream)
+    torch.cuda.synchronize()
+    t_eval = sum(a.elapsed_time(b) for a, b in evs) / len(evs) / 1e3
+    t_cpu, ref = reverso_cpu_baseline(theta.cpu().numpy(), txy, d, var)
+    assert np.allclose(out.cpu().numpy(), ref, rtol=1e-12, atol=0.0), "device and oracle disagree"
+    t_run = max_over_ranks(float(np.mean(times)), dist, device="cuda")
+    if rank == 0:
+        print(json.dumps({
+            "metric": "Reverso time-to-beta=1", "value": t_run, "unit": "s", "n_gpus": world,
+            "steps": len(times), "warmup": 1, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (the reference's generator: 35 points, 1e-6..1 yr, 1-5 km)",
+            "config": {"workload": "reverso-example", "chains": N, "steps_per_stage": 20, "observations": 35,
+                       "strategy": "fast", "stages": stages, "final_beta": final_beta},
+            "chain_steps_per_s": steps / float(np.sum(times)),
+            "llk_kernel_ms": t_eval * 1e3,
+            "cpu_baseline": {"value": N / t_cpu, "unit": "chain-llk/s", "cores": 1, "kind": "port",
+                             "sample": f"{N} chains x 35 points, one vectorised numpy evaluation (oracle/reverso.py)"},
+            "gpu_llk_per_s": N / t_eval}))
     return 0
 
 
@@ -637,7 +748,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--mode", default="walk", choices=["walk", "anneal", "compare", "linear", "dense"])
+    ap.add_argument("--mode", default="walk", choices=["walk", "anneal", "compare", "linear", "dense", "reverso"])
     ap.add_argument("--sampler", default="plain", choices=["plain", "da"])
     ap.add_argument("--max-stages", type=int, default=400)
     ap.add_argument("--da-start-beta", type=float, default=0.0)
@@ -668,6 +779,8 @@ def main():
         return run_linear(args)
     if args.mode == "dense":
         return run_dense(args)
+    if args.mode == "reverso":
+        return run_reverso(args)
     return run_ours(args)
 
 

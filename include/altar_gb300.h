@@ -331,6 +331,33 @@ int ag_whiten_llk(const ag_whiten_block* block, const float* resid, int32_t ldr,
                   void* workspace, size_t workspace_bytes, uint32_t* flags, void* stream);
 
 /* ---------------------------------------------------------------------------
+ * Reverso two-reservoir magma model (FP64).  Replaces the libreverso capsule
+ * module (models/reverso/ext/reverso/source.cc: newSource(G, v, mu, drho, g),
+ * locations, data, layout(Qin, H_s, H_d, a_s, a_d, a_c indices), displacements,
+ * residuals) and the per-sample norm loop of models/reverso/reverso/Fast.py:52-90.
+ */
+typedef struct ag_reverso_model {
+    const double* txy;       /* [n_obs][3]: time (s), east, north (m) of each observation point */
+    const double* d;         /* [n_obs][3]: observed displacement east, north, up (m) */
+    const double* w;         /* [n_obs][3]: 1/σ² of each component (diagonal Cd); 0 drops it */
+    int32_t n_obs;
+    int32_t nparams;         /* row stride of θ */
+    int32_t qin_idx, hs_idx, hd_idx, as_idx, ad_idx, ac_idx;   /* parameter positions */
+    int32_t east_cos;        /* 1: u_E = u_r cos φ, u_N = u_r sin φ (reverso.cc:92-96, the default
+                                strategy); 0: u_E = u_r sin φ, u_N = u_r cos φ (Native.py:96-100) */
+    int32_t reserved;
+    double G, v, mu, drho, g;  /* shear modulus, Poisson ratio, viscosity, density contrast, gravity */
+} ag_reverso_model;
+
+/*
+ * llk[i] = norm - 1/2 Σ w (u - d)² over the 3 n_obs components of sample i; rows with
+ * mask[i] != 0 are skipped (mask may be NULL).  predicted (NULL = none): n rows of the
+ * 3 n_obs displacements (east, north, up per point), the reference's displacements().
+ */
+int ag_reverso_llk(const ag_reverso_model* model, const double* theta, int32_t n, double norm,
+                   const uint32_t* mask, double* llk, double* predicted, void* stream);
+
+/* ---------------------------------------------------------------------------
  * Learned surrogate and delayed acceptance.  No counterpart in the reference:
  * an MLP maps normalised source parameters to PCA coefficients of the LOS
  * field; it screens proposals (stage 1) before the exact model (stage 2).
