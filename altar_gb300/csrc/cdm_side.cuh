@@ -23,14 +23,22 @@ namespace ag {
 constexpr int kSides = 12;
 
 // ---------------------------------------------------------------------------
-// per-side constants of one angular-dislocation pair (40 floats).  β is the
+// per-side constants of one angular-dislocation pair (48 floats).  β is the
 // angle of the side from the downward vertical; "configuration II" values,
 // the per-station sign sg = -1 of configuration I (β - π) is applied in the
 // pair evaluation.  Coefficients of the two log differences carry ln 2 (the
 // logs are evaluated in base 2) and those of the Burgers-function difference
 // carry the factor 2 of Fi = 2 atan2(...).
+//
+// Near-vertical ("steep") sides, |cot β| >= kSteepCot: the coefficients of the
+// log differences grow like cot²β while the combination they multiply,
+// Q = Δlog(r+a) - sg cos β Δlog(r-z3), is O(β); evaluated as two O(1) logs
+// it cancels and FP32 rounding is amplified by cot²β.  For these sides the
+// set-up splits the log terms into Q (coefficients KQ1..KQ3) plus benign
+// remainders (C1P, C2P, C2Q replaced, C1Q, C3Q, kc2L zero), and the pair
+// evaluates Q from exact identities without the cancellation (side_pair).
 struct __align__(16) SideC {
-    float4 q[10];
+    float4 q[12];
 };
 // q0: c, s, k1, k2            frame (unit horizontal side direction) and vertex A
 // q1: dy1, aA, aB, da         y1(B) - y1(A); depths of A and B; aB - aA
@@ -41,13 +49,17 @@ struct __align__(16) SideC {
 // q6: b1, b2, C1m10, C3m10
 // q7: C1Q, C2Q, C3Q, C1m11    ln 2 × configuration-signed coefficients of Δlog(r-z3)
 // q8: C3m11, C1m12, aAsb, naAcb   aA·sin β, -aA·cos β
-// q9: dz1, dz3, kc2L, 0       Δz1, Δz3 (configuration II); ln 2 · kc2
+// q9: dz1, dz3, kc2L, omc     Δz1, Δz3 (configuration II); ln 2 · kc2; 1 - |cos β|
+// q10: a1c, dc, ssb, KQ1      steep sides: aA·omc, Δc, sign(cos β)·sin β, ln 2 k cot²β b2
+// q11: KQ2, KQ3, 0, 0         steep sides: ln 2 k cot²β b1, -ln 2 k cot β b2
+constexpr double kSteepCot = 3.0;
 
 // Per-side constant by its position in SideC (q[i >> 2], component i & 3)
 enum : int {
     K_C = 0, K_S, K_K1, K_K2, K_DY1, K_AA, K_AB, K_DA, K_SB, K_CB, K_TB2, K_CTB2, K_DAS, K_C1F, K_C2F, K_C3F,
     K_C1P, K_C2P, K_KC1, K_KC2, K_NB1, K_NB2, K_HB1, K_HB2, K_B1, K_B2, K_C1M10, K_C3M10, K_C1Q, K_C2Q, K_C3Q,
-    K_C1M11, K_C3M11, K_C1M12, K_AASB, K_NAACB, K_DZ1, K_DZ3, K_KC2L
+    K_C1M11, K_C3M11, K_C1M12, K_AASB, K_NAACB, K_DZ1, K_DZ3, K_KC2L, K_OMC, K_A1C, K_DC, K_SSB, K_KQ1,
+    K_KQ2, K_KQ3
 };
 
 // ---------------------------------------------------------------------------
@@ -67,7 +79,7 @@ AG_CDM_FN void split_hilo(double v, float& hi, float& lo) {
 }
 
 AG_CDM_FN void fill_side(SideC& S, Vec3 pa, Vec3 pb, Vec3 bvec, double nu, double x0, double y0,
-                         bool& active) {
+                         bool& active, bool& steep) {
     const double PI = 3.14159265358979323846;
     const double LN2 = 0.69314718055994530942;
     Vec3 side = v_sub(pb, pa);
@@ -75,6 +87,7 @@ AG_CDM_FN void fill_side(SideC& S, Vec3 pa, Vec3 pb, Vec3 bvec, double nu, doubl
     double beta = acos(-side.z / L);
     // vertical sides contribute nothing (libcdm.py:320-324)
     const double eps = 2.220446049250313e-16;
+    steep = false;
     if (!(L > 0.0) || fabs(beta) < eps || fabs(PI - beta) < eps) {
         active = false;
         return;
@@ -121,7 +134,22 @@ AG_CDM_FN void fill_side(SideC& S, Vec3 pa, Vec3 pb, Vec3 bvec, double nu, doubl
     S.q[6] = make_float4((float)b1, (float)b2, (float)C1m10, (float)C3m10);
     S.q[7] = make_float4((float)(LN2 * C1Q), (float)(LN2 * C2Q), (float)(LN2 * C3Q), (float)C1m11);
     S.q[8] = make_float4((float)C3m11, (float)C1m12, (float)(aA * sb), (float)(-aA * cb));
-    S.q[9] = make_float4((float)(dy1 * cb + da * sb), (float)(dy1 * sb - da * cb), (float)(LN2 * kc2), 0.f);
+    const double omc = sb * sb / (1.0 + fabs(cb));   // 1 - |cos β| without cancellation
+    const double sgn = (cb >= 0.0) ? 1.0 : -1.0;
+    S.q[9] = make_float4((float)(dy1 * cb + da * sb), (float)(dy1 * sb - da * cb), (float)(LN2 * kc2), (float)omc);
+    S.q[10] = make_float4((float)(aA * omc), (float)(da * omc + sgn * dy1 * sb), (float)(sgn * sb),
+                          (float)(LN2 * k * cot * cot * b2));
+    S.q[11] = make_float4((float)(LN2 * k * cot * cot * b1), (float)(-LN2 * k * cot * b2), 0.f, 0.f);
+    steep = fabs(cot) >= kSteepCot;
+    if (steep) {
+        // log terms as KQ·Q plus remainders (derivation at side_pair)
+        S.q[4].x = (float)(-LN2 * 0.5 * k * b2);       // v1: -k b2/2 · Δlog(r+a)
+        S.q[4].y = (float)(LN2 * 0.5 * k * b1);        // v2: k b1/2 · Δlog(r+a)
+        S.q[7].x = 0.f;                                  // v1: no Δlog(r-z3) term
+        S.q[7].y = (float)(-LN2 * k * b1 * cb);        // v2: -sg k b1 cos β · Δlog(r-z3)
+        S.q[7].z = 0.f;                                  // v3: no Δlog(r-z3) term
+        S.q[9].z = 0.f;                                  // v3: no Δlog(r+a) term
+    }
 }
 
 // corners of the three rectangles (libcdm.py:174-217); returns true if any is above the surface
@@ -168,7 +196,8 @@ AG_CDM_FN bool cdm_corners(const double* th, const Layout& L, Vec3 V[3][4]) {
 }
 
 // Constants of the active sides of a chain whose corners V lie below the surface;
-// returns the mask of active sides (bit 4r + e: side e of rectangle r)
+// returns the mask of active sides (bit 4r + e: side e of rectangle r) and of the
+// steep ones among them (bit 12 + 4r + e)
 template <class Layout>
 AG_CDM_FN uint32_t cdm_sides(const double* th, const Layout& L, const Vec3 V[3][4], double x0, double y0,
                              SideC* side) {
@@ -194,9 +223,10 @@ AG_CDM_FN uint32_t cdm_sides(const double* th, const Layout& L, const Vec3 V[3][
         nrm = v_scale(nrm, 1.0 / sqrt(v_dot(nrm, nrm)));
         Vec3 b = v_scale(nrm, opening);
         for (int e = 0; e < 4; ++e) {
-            bool act;
-            fill_side(side[r * 4 + e], V[r][e], V[r][(e + 1) & 3], b, L.nu, x0, y0, act);
+            bool act, steep;
+            fill_side(side[r * 4 + e], V[r][e], V[r][(e + 1) & 3], b, L.nu, x0, y0, act, steep);
             if (act) mask |= 1u << (r * 4 + e);
+            if (act && steep) mask |= 1u << (kSides + r * 4 + e);
         }
     }
     return mask;
@@ -309,10 +339,10 @@ template <int N> AG_DEVICE_INLINE SV<N> vatan2(SV<N> y, SV<N> x) { AG_SV_MAP(ata
 #undef AG_CV_MAP
 
 struct ScalarSide {
-    float4 q[10];
+    float4 q[12];
     AG_DEVICE_INLINE explicit ScalarSide(const SideC& S) {
 #pragma unroll
-        for (int i = 0; i < 10; ++i) q[i] = S.q[i];
+        for (int i = 0; i < 12; ++i) q[i] = S.q[i];
     }
     template <int I>
     AG_DEVICE_INLINE float at() const {
@@ -334,7 +364,7 @@ struct ScalarSide {
 // difference as one atan2 of the rotation from A to B), so the v(B) - v(A)
 // cancellation of the reference formula never happens in floating point.
 template <class V, class K>
-AG_DEVICE_INLINE void side_pair(const K& k, V Xr, V Yr, V& ue, V& un, V& uv) {
+AG_DEVICE_INLINE void side_pair(const K& k, V Xr, V Yr, V& ue, V& un, V& uv, bool steep) {
     const V c = KC(K_C), s = KC(K_S);
     const V dy1 = KC(K_DY1), aA = KC(K_AA), aB = KC(K_AB), da = KC(K_DA);
     // station in the angular-dislocation frame of vertex A; y2 is the same at B
@@ -440,6 +470,33 @@ AG_DEVICE_INLINE void side_pair(const K& k, V Xr, V Yr, V& ue, V& un, V& uv) {
     v3 = vfma(ndair, X1, v3);
     v3 = vfma(nairA, dX1, v3);
     v3 = vfma(sg, vfma(KC(K_C3Q), dLq, vmul(KC(K_C3M11), dm11)), v3);
+    if (steep) {
+        // Near-vertical side: the log terms are K·Q plus benign remainders (set-up), with
+        //   Q = Δlog(r+a) - sg cos β Δlog(r-z3) = O(β)
+        // from exact identities in p = r + a, q = r - z3, c = a (1 - |cos β|) + sign(cos β) y1 sin β:
+        //   ratio form (sg = sign cos β):   p/q = 1 + c/q,        Q = Δlog(p/q) + (1 - |cos β|) Δlog q
+        //   product form (sg = -sign cos β): p q = y1² + y2² + p c, Q = Δlog(pq) - (1 - |cos β|) Δlog q
+        // where c/q and the terms of p q carry no cancellation, and their differences come from
+        // the product rule on (value at A, difference) pairs.
+        const V cA = vfma(KC(K_SSB), y1A, KC(K_A1C));
+        const V dc = KC(K_DC), omc = KC(K_OMC);
+        const auto ratio = vgt0(vmul(sg, KC(K_CB)));
+        // ratio form: E = c/q, Δlog(1 + E) from s = ΔE/(2 + E_A + E_B), ratio 1 + ΔE/(1 + E_A)
+        const V EA = vmul(cA, iqA);
+        const V dE = vfma(dc, iqB, vneg(vmul(cA, ndiq)));
+        // product form: G = y1² + y2² + p c, Δlog G from s = ΔG/(G_A + G_B), ratio 1 + ΔG/G_A
+        const V GA = vfma(pA, cA, vfma(y1A, y1A, y22));
+        const V dG = vfma(dy1, vadd(y1A, y1B), vfma(dp, vadd(cA, dc), vmul(pA, dc)));
+        // one logarithm per station, of the form its configuration needs
+        const V num = vsel(ratio, dE, dG);
+        const V den1 = vsel(ratio, vadd(vadd(V(2.0f), EA), vadd(EA, dE)), vfma(V(2.0f), GA, dG));
+        const V den2 = vsel(ratio, vadd(V(1.0f), EA), GA);
+        const V L = vlog2r(vmul(num, frcp(den1)), vfma(num, frcp(den2), V(1.0f)));
+        const V Q = vfma(vsel(ratio, omc, vneg(omc)), dLq, L);
+        v1 = vfma(KC(K_KQ1), Q, v1);
+        v2 = vfma(KC(K_KQ2), Q, v2);
+        v3 = vfma(KC(K_KQ3), Q, v3);
+    }
     // back to EFCS: columns e1 = (c, s, 0), e2 = (s, -c, 0), e3 = (0, 0, -1)
     ue = vfma(c, v1, vfma(s, v2, ue));
     un = vfma(s, v1, vfma(KN(K_C), v2, un));

@@ -204,7 +204,7 @@ cdm_llk_kernel(const ChainC* __restrict__ chains, const int32_t* __restrict__ sl
                     while (msk) {
                         const int sidx = __ffs(msk) - 1;
                         msk &= msk - 1;
-                        side_pair<SV<SPL>>(ScalarSide(C.side[sidx]), Xr, Yr, ue, un, uv);
+                        side_pair<SV<SPL>>(ScalarSide(C.side[sidx]), Xr, Yr, ue, un, uv, (smask >> (kSides + sidx)) & 1u);
                     }
 #pragma unroll
                     for (int q = 0; q < SPL; ++q) finish(ue.v[q], un.v[q], uv.v[q], j0 + 32 * q);
@@ -220,7 +220,7 @@ cdm_llk_kernel(const ChainC* __restrict__ chains, const int32_t* __restrict__ sl
                     while (msk) {
                         const int sidx = __ffs(msk) - 1;
                         msk &= msk - 1;
-                        side_pair<float>(ScalarSide(C.side[sidx]), Xr, Yr, ue, un, uv);
+                        side_pair<float>(ScalarSide(C.side[sidx]), Xr, Yr, ue, un, uv, (smask >> (kSides + sidx)) & 1u);
                     }
                     finish(ue, un, uv, j);
                 }

@@ -55,7 +55,7 @@ extern "C" int cdm_host_los(const double* th, int n, const double* X, const doub
         const float Xr = (ah - x0h) + (al - x0l), Yr = (bh - y0h) + (bl - y0l);
         float ue = 0.f, un = 0.f, uv = 0.f;
         for (int k = 0; k < kSides; ++k)
-            if (mask >> k & 1u) side_pair<float>(ScalarSide(side[k]), Xr, Yr, ue, un, uv);
+            if (mask >> k & 1u) side_pair<float>(ScalarSide(side[k]), Xr, Yr, ue, un, uv, (mask >> (kSides + k)) & 1u);
         out[j] = (double)ue * los[3 * j] + (double)un * los[3 * j + 1] + (double)uv * los[3 * j + 2];
     }
     return 0;
@@ -82,13 +82,15 @@ inline CountF vlog2r(CountF s, CountF r) { g_flop += 10; g_sfu += 1; return log2
 // atan2_poly: mn/mx (mul), t², 8 FMA, t·p, two quadrant subtractions (21 FLOP) + one reciprocal
 inline CountF vatan2(CountF y, CountF x) { g_flop += 21; g_sfu += 1; return atan2_poly(y.v, x.v); }
 
-extern "C" void cdm_host_side_counts(long* flop, long* sfu) {
+extern "C" void cdm_host_side_counts(long* flop, long* sfu, long* flop_steep, long* sfu_steep) {
     SideC S;
-    bool act;
-    fill_side(S, Vec3{100, 200, -3000}, Vec3{900, -300, -2500}, Vec3{1, 2, 3}, 0.25, 0, 0, act);
-    CountF ue(0.f), un(0.f), uv(0.f);
-    g_flop = g_sfu = 0;
-    side_pair<CountF>(ScalarSide(S), CountF(1000.f), CountF(-2000.f), ue, un, uv);
-    *flop = g_flop;
-    *sfu = g_sfu;
+    bool act, steep;
+    fill_side(S, Vec3{100, 200, -3000}, Vec3{900, -300, -2500}, Vec3{1, 2, 3}, 0.25, 0, 0, act, steep);
+    for (int s = 0; s < 2; ++s) {
+        CountF ue(0.f), un(0.f), uv(0.f);
+        g_flop = g_sfu = 0;
+        side_pair<CountF>(ScalarSide(S), CountF(1000.f), CountF(-2000.f), ue, un, uv, s == 1);
+        *(s ? flop_steep : flop) = g_flop;
+        *(s ? sfu_steep : sfu) = g_sfu;
+    }
 }

@@ -35,7 +35,7 @@ def host(tmp_path_factory):
     lib.cdm_host_los.argtypes = [P(ctypes.c_double), ctypes.c_int, P(ctypes.c_double), P(ctypes.c_double),
                                  P(ctypes.c_double), ctypes.c_double, P(ctypes.c_double)]
     lib.cdm_host_los.restype = ctypes.c_int
-    lib.cdm_host_side_counts.argtypes = [P(ctypes.c_long), P(ctypes.c_long)]
+    lib.cdm_host_side_counts.argtypes = [P(ctypes.c_long)] * 4
     return lib
 
 
@@ -45,12 +45,14 @@ def _dp(a):
 
 def test_flop_count_matches_bench_constant(host):
     import bench
-    flop, sfu = ctypes.c_long(), ctypes.c_long()
-    host.cdm_host_side_counts(ctypes.byref(flop), ctypes.byref(sfu))
+    flop, sfu, flop_s, sfu_s = (ctypes.c_long() for _ in range(4))
+    host.cdm_host_side_counts(ctypes.byref(flop), ctypes.byref(sfu), ctypes.byref(flop_s), ctypes.byref(sfu_s))
     # 12 sides + per station: relative coordinates (6), LOS projection (5), residual (1),
-    # float-float w·r² accumulation (19)
+    # float-float w·r² accumulation (19); near-vertical sides add the cancellation-free
+    # log combination
     assert 12 * flop.value + 31 == bench.CDM_FLOP_PER_PAIR
     assert sfu.value == bench.CDM_SFU_PER_SIDE
+    assert (flop_s.value - flop.value, sfu_s.value - sfu.value) == bench.CDM_STEEP_EXTRA
 
 
 def test_side_arithmetic_against_oracle(host):
@@ -70,3 +72,25 @@ def test_side_arithmetic_against_oracle(host):
     assert flat.sum() >= 16
     assert np.all(errs[flat] <= 1e-4), errs[flat].max()
     assert np.median(errs) <= 5e-6, np.median(errs)
+    # near-vertical sides: the error grows like cot β, not cot²β (cancellation-free logs)
+    cot = np.array([1.0 / np.tan(np.radians(min_vertical_angle(th))) for th in theta])
+    assert np.all(errs <= np.maximum(1e-4, 2e-5 * cot)), [(e, c) for e, c in zip(errs, cot) if e > max(1e-4, 2e-5 * c)]
+
+
+def test_steep_sides_without_cot2_amplification(host):
+    """Sources with a side within 2° of the vertical (drawn from the priors): the error
+    stays within 2e-5 · cot β of the oracle, where the two-log form of the reference
+    formula loses up to cot²β · 2⁻²⁴ (0.2 at 0.03°)."""
+    g = np.linspace(-20e3, 20e3, 30)
+    X, Y = [np.ascontiguousarray(a.ravel()) for a in np.meshgrid(g, g)]
+    los = np.ascontiguousarray(np.tile(LOS, (X.size, 1)))
+    theta = [th for th in cdm_prior_rows(300, seed=5) if min_vertical_angle(th) < 2.0]
+    assert len(theta) >= 8
+    for th in theta:
+        ref = cdm.los_displacements(th, CDM_LAYOUT, X, Y, los, 0.25)
+        out = np.empty(X.size)
+        t = np.ascontiguousarray(th, dtype=np.float64)
+        assert host.cdm_host_los(_dp(t), X.size, _dp(X), _dp(Y), _dp(los), 0.25, _dp(out)) == 0
+        err = np.max(np.abs(out - ref)) / np.max(np.abs(ref))
+        cot = 1.0 / np.tan(np.radians(min_vertical_angle(th)))
+        assert err <= 2e-5 * cot, (min_vertical_angle(th), err)
