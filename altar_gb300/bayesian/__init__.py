@@ -7,7 +7,7 @@ from .brent import Brent
 from .cov import COV
 from .annealing import CUDAAnnealing
 from .annealer import Annealer
-from .surrogate import DelayedAcceptance, Surrogate
+from .surrogate import DelayedAcceptance, SubsetSurrogate, Surrogate
 
 __all__ = ["CoolingStep", "StageState", "Notifier", "Profiler", "Metropolis", "Grid", "Brent", "COV",
-           "CUDAAnnealing", "Annealer", "DelayedAcceptance", "Surrogate"]
+           "CUDAAnnealing", "Annealer", "DelayedAcceptance", "Surrogate", "SubsetSurrogate"]

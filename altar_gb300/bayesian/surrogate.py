@@ -186,8 +186,10 @@ class Surrogate:
         return self.losses
 
     # ---- inference
-    def predict(self, theta, lo, hi, out_llk, bufs):
-        """Surrogate data log-likelihood of device θ rows into out_llk."""
+    needs_fit = True
+
+    def predict(self, theta, lo, hi, out_llk, bufs, mask=None):
+        """Surrogate data log-likelihood of device θ rows into out_llk (mask: unused)."""
         n, p = theta.shape
         x, coeff, acts = bufs
         s = stream_handle()
@@ -209,6 +211,64 @@ class Surrogate:
     def reconstruct(self, coeff_norm):
         b = self.basis
         return b["mu"] + (coeff_norm * b["scale"]) @ b["B"].T
+
+
+class _SubsetModel:
+    """The parameter layout of a model over a subset of its observations."""
+
+    def __init__(self, model, obs):
+        self.obs = obs
+        self._model = model
+
+    def layout(self):
+        return self._model.layout()
+
+
+class SubsetSurrogate:
+    """Coarse likelihood: the exact forward model on every ``stride``-th observation, with
+    the misfit weights multiplied by ``stride``, so that its data log-likelihood estimates
+    the full one as a quadrature of the residual field (Christen & Fox 2005 use such a
+    coarse model as the first stage of delayed acceptance).  For a smooth displacement
+    field the error of a log-likelihood ratio between nearby samples is far below that of
+    a fitted network, and nothing is trained; each evaluation costs ~1/stride of the exact
+    one.  ``strides`` (coarsest first) are the levels the sampler may pick from, per stage:
+    the coarsest whose tempered-ratio check passes.  Works with the point-source models
+    whose strategy is the CUDA forward model (CDM, Mogi)."""
+
+    needs_fit = False
+    trained = True
+
+    def __init__(self, strides=(32, 16, 8)):
+        self.strides = tuple(int(s) for s in (strides if hasattr(strides, "__iter__") else (strides,)))
+        self.levels = len(self.strides)
+        self.level = 0
+        self.strategies = []
+
+    @property
+    def stride(self):
+        return self.strides[self.level]
+
+    def attach(self, application, model):
+        from ..models.forward import CUDA
+        from ..models.observations import Observations
+        obs = model.obs
+        self.strategies = []
+        for k in self.strides:
+            sub = Observations(obs.x[::k], obs.y[::k], obs.los[::k], obs.d[::k], obs.variance[::k] / k,
+                               None if obs.oid is None else obs.oid[::k])
+            strat = CUDA(model.strategy.kind).initialize(application=application, model=_SubsetModel(model, sub))
+            strat.norm = model.strategy.norm           # constants cancel; keep the exact model's
+            self.strategies.append(strat)
+        return self
+
+    def predict(self, theta, lo, hi, out_llk, bufs, mask=None):
+        """Coarse data log-likelihood of device θ rows into out_llk; rows flagged in mask are
+        skipped and sources above the surface are flagged there."""
+        self.strategies[self.level].forward(theta, out_llk, mask=mask, status=mask)
+        return out_llk
+
+    def buffers(self, n, p):
+        return None
 
 
 class DelayedAcceptance(Metropolis):
@@ -258,6 +318,8 @@ class DelayedAcceptance(Metropolis):
 
     def initialize(self, application):
         super().initialize(application)
+        if not self.surrogate.needs_fit:
+            self.surrogate.attach(application, application.model)
         # start the device BLAS the refits use now, so that its one-time set-up does not
         # land inside the first refit
         for dt in (torch.float32, torch.float64):
@@ -266,6 +328,9 @@ class DelayedAcceptance(Metropolis):
         return self
 
     def mode_key(self):
+        # each level of a subset surrogate reads other stations: one captured walk per level
+        if self.mode == "da" and not self.surrogate.needs_fit:
+            return f"da{self.surrogate.level}"
         return self.mode
 
     def report(self):
@@ -273,6 +338,8 @@ class DelayedAcceptance(Metropolis):
                "prepare_s": self._prepare_s}
         if self.mode == "da" and self.screened is not None:
             rep["screened"] = int(self.screened.item())
+        if self.mode == "da" and not self.surrogate.needs_fit:
+            rep["stride"] = self.surrogate.stride
         return rep
 
     # ---- per-stage host decisions (eager, before the walk graph)
@@ -299,6 +366,14 @@ class DelayedAcceptance(Metropolis):
         stride = max(1, n // (fit + chk))
         rows = torch.arange(0, n, stride, device=DEVICE)[: fit + chk]
         fit_rows, chk_rows = rows[:fit], rows[fit:fit + chk]
+        if not sur.needs_fit:
+            # nothing to fit: the coarsest level whose tempered-ratio check passes, else exact
+            self._set_bounds(step)
+            self.rms = None
+            level, self.delta = self._delta_check(annealer, step, chk_rows, levels=range(sur.levels))
+            sur.level = level
+            self.mode = "da" if self._usable() else "plain"
+            return self
         if sur.trained:
             self.rms = self._check(annealer, step, chk_rows)
             self.delta = self._delta_check(annealer, step, chk_rows)
@@ -318,10 +393,12 @@ class DelayedAcceptance(Metropolis):
         return self
 
     def _usable(self):
-        return self.rms <= self.rms_limit and self.delta <= self.delta_limit
+        return (self.rms is None or self.rms <= self.rms_limit) and self.delta <= self.delta_limit
 
-    def _delta_check(self, annealer, step, rows):
-        """Spread of β[(s(y) - s(x)) - (l(y) - l(x))] over one trial proposal per check chain."""
+    def _delta_check(self, annealer, step, rows, levels=None):
+        """Spread of β[(s(y) - s(x)) - (l(y) - l(x))] over one trial proposal per check chain.
+        levels: surrogate levels to try in order (SubsetSurrogate); returns the first level
+        whose spread is within delta_limit together with its spread, else the last one's."""
         model, strat, sur = annealer.model, annealer.model.strategy, self.surrogate
         th = step.theta.index_select(0, rows).contiguous()
         ex_x = step.data.index_select(0, rows)
@@ -338,13 +415,20 @@ class DelayedAcceptance(Metropolis):
         strat.forward(cand, ex_y, mask=mask, status=mask)
         bufs = sur.buffers(c, p)
         sx, sy = torch.empty(c, **f64), torch.empty(c, **f64)
-        sur.predict(th, self._bounds[0], self._bounds[1], sx, bufs)
-        sur.predict(cand, self._bounds[0], self._bounds[1], sy, bufs)
         ok = mask == 0
-        if int(ok.sum()) < 2:
-            return float("inf")
-        eps = step.beta * ((sy - sx) - (ex_y - ex_x))[ok]
-        return float(eps.std())
+        result = (None, float("inf"))
+        for level in (levels if levels is not None else [None]):
+            if level is not None:
+                sur.level = level
+            sur.predict(th, self._bounds[0], self._bounds[1], sx, bufs)
+            sur.predict(cand, self._bounds[0], self._bounds[1], sy, bufs)
+            if int(ok.sum()) < 2:
+                return (level, float("inf")) if levels is not None else float("inf")
+            eps = step.beta * ((sy - sx) - (ex_y - ex_x))[ok]
+            result = (level, float(eps.std()))
+            if result[1] <= self.delta_limit:
+                break
+        return result if levels is not None else result[1]
 
     def _fields(self, strat, theta):
         n = theta.shape[0]
@@ -442,7 +526,7 @@ class DelayedAcceptance(Metropolis):
                 sid = 1000 + o * self.inner + j
                 _native.call("ag_propose", st, ptr(th_s), n, p, ptr(model.lo), ptr(model.hi), self.seed, sid,
                              ptr(cand), ptr(mask), ptr(cprior), s)
-                sur.predict(cand, lo, hi, sur_cand, bufs)
+                sur.predict(cand, lo, hi, sur_cand, bufs, mask=mask)
                 _native.call("ag_accept", ctypes.byref(sst), n, p, self.seed, sid, ptr(mask), ptr(cand),
                              ptr(cprior), ptr(sur_cand), ptr(th_s), ptr(pr_s), ptr(su_s), ptr(po_s), s)
             _native.call("ag_da_moved", n, p, ptr(step.theta), ptr(th_s), ptr(passed), ptr(index), ptr(count), s)
@@ -478,7 +562,7 @@ class DelayedAcceptance(Metropolis):
         for k in range(self.steps):
             _native.call("ag_propose", st, ptr(step.theta), n, p, ptr(model.lo), ptr(model.hi), self.seed, k,
                          ptr(cand), ptr(mask), ptr(cprior), s)
-            sur.predict(cand, lo, hi, sur_cand, bufs)
+            sur.predict(cand, lo, hi, sur_cand, bufs, mask=mask)
             _native.call("ag_da_screen", st, n, self.seed, k, ptr(mask), ptr(cprior), ptr(sur_cand),
                          ptr(step.prior), ptr(sur_cur), ptr(passed), ptr(index), ptr(count), s)
             _native.call("ag_forward_llk_subset", strat.kind, ctypes.byref(strat.layout), ptr(cand), n,

@@ -243,20 +243,22 @@ def anneal(kind, X, Y, los, d, N, rank, args, seed=1234, max_stages=None):
     """One CATMIP run to β = 1 with the plain or the delayed-acceptance sampler."""
     import torch
     from altar_gb300 import Application
-    from altar_gb300.bayesian import Annealer, DelayedAcceptance, Surrogate
+    from altar_gb300.bayesian import Annealer, DelayedAcceptance, SubsetSurrogate, Surrogate
     from altar_gb300.models import CDM
     from altar_gb300.models.observations import Observations
     from altar_gb300.simulations import RNG, Job
     sampler = None
     if kind == "da":
-        sampler = DelayedAcceptance(surrogate=Surrogate(seed=5, batch=1024), rms_limit=args.rms_limit,
+        sur = (SubsetSurrogate(strides=args.subset_strides) if args.surrogate == "subset"
+               else Surrogate(seed=5, batch=1024))
+        sampler = DelayedAcceptance(surrogate=sur, rms_limit=args.rms_limit,
                                     delta_limit=args.delta_limit, epochs=args.epochs,
                                     refit_epochs=args.refit_epochs,
                                     start_beta=args.da_start_beta, stop_beta=args.da_stop_beta,
                                     inner=args.da_inner,
                                     outer=args.da_outer)
     model = CDM(cdm_psets(), observations=Observations(X, Y, los, d, SIGMA ** 2), autotune=not args.no_autotune)
-    app = Application(model, job=Job(chains=N, steps=5), rng=RNG(seed + rank),
+    app = Application(model, job=Job(chains=N, steps=args.walk_steps), rng=RNG(seed + rank),
                       controller=Annealer(sampler=sampler))
     app.initialize()
     torch.cuda.synchronize()
@@ -284,7 +286,7 @@ def anneal(kind, X, Y, los, d, N, rank, args, seed=1234, max_stages=None):
         res["prepare_s"] = [r.get("prepare_s") for r in reps]
         res["screened"] = [r.get("screened") for r in reps]
         res["refits"] = sampler.refits
-        res["train_losses_last"] = sampler.surrogate.losses[-3:]
+        res["train_losses_last"] = getattr(sampler.surrogate, "losses", [])[-3:]
     return res
 
 
@@ -565,17 +567,25 @@ def run_ours(args):
         for seed in args.seeds:
             for kind in kinds:
                 out[f"{kind}_s{seed}"] = anneal(kind, X, Y, los, d, N, rank, args, seed=seed)
+        if args.ref_walk_steps:
+            # a longer plain walk per stage: the better-mixed posterior both samplers are judged by
+            steps5 = args.walk_steps
+            args.walk_steps = args.ref_walk_steps
+            for seed in args.seeds:
+                out[f"plain{args.ref_walk_steps}_s{seed}"] = anneal("plain", X, Y, los, d, N, rank, args, seed=seed)
+            args.walk_steps = steps5
         for extra in args.da_variants:
             inner, outer = (int(v) for v in extra.split("x"))
             args.da_inner, args.da_outer = inner, outer
             out[f"da_{inner}x{outer}_s{args.seeds[0]}"] = anneal("da", X, Y, los, d, N, rank, args,
                                                                 seed=args.seeds[0])
         line = {"metric": "CDM time-to-beta=1", "unit": "s", "n_gpus": world, "higher_is_better": False,
-                "config": {"workload": "cdm-40k-obs", "chains": N, "stations": X.size, "steps_per_stage": 5,
+                "config": {"workload": "cdm-40k-obs", "chains": N, "stations": X.size, "steps_per_stage": args.walk_steps,
                            "truth": truth.tolist(), "seeds": args.seeds,
                            "da": {"inner": args.da_inner, "outer": args.da_outer,
                                   "delta_limit": args.delta_limit, "rms_limit": args.rms_limit,
-                                  "stop_beta": args.da_stop_beta}},
+                                  "stop_beta": args.da_stop_beta, "surrogate": args.surrogate,
+                                  "subset_strides": args.subset_strides}},
                 "runs": out, "untimed_warmup_s": warm}
         if args.mode == "compare":
             tp = sum(out[f"plain_s{s_}"]["time_s"] for s_ in args.seeds)
@@ -591,6 +601,17 @@ def run_ours(args):
                 diffs[str(s_)] = (np.abs(np.array(a["mean"]) - np.array(b["mean"])) /
                                   np.where(sd > 0, sd, 1)).tolist()
             line["invariant_mean_diff_in_sd"] = diffs
+            if args.ref_walk_steps:
+                # seed-averaged summaries of each sampler against the longer plain walk
+                sd = np.array(out[f"plain_s{args.seeds[0]}"]["invariants"]["sd"])
+                sd = np.where(sd > 0, sd, 1)
+                mean = lambda kind: np.mean([out[f"{kind}_s{s_}"]["invariants"]["mean"] for s_ in args.seeds], 0)
+                ref = mean(f"plain{args.ref_walk_steps}")
+                line["vs_longer_walk_in_sd"] = {"plain": ((mean("plain") - ref) / sd).tolist(),
+                                                "da": ((mean("da") - ref) / sd).tolist(),
+                                                "longer_walk_time_s": float(np.mean(
+                                                    [out[f"plain{args.ref_walk_steps}_s{s_}"]["time_s"]
+                                                     for s_ in args.seeds]))}
         else:
             line["value"] = out[f"{kinds[0]}_s{args.seeds[0]}"]["time_s"]
         if rank == 0:
@@ -755,6 +776,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--mode", default="walk", choices=["walk", "anneal", "compare", "linear", "dense", "reverso"])
     ap.add_argument("--sampler", default="plain", choices=["plain", "da"])
+    ap.add_argument("--ref-walk-steps", type=int, default=0,
+                    help="compare mode: also run plain Metropolis with this many steps per stage, the "
+                         "better-mixed posterior both samplers are measured against (0 = no)")
+    ap.add_argument("--walk-steps", type=int, default=5,
+                    help="Metropolis steps per stage of the anneal/compare runs (the workload's is 5)")
     ap.add_argument("--max-stages", type=int, default=400)
     ap.add_argument("--da-start-beta", type=float, default=0.0)
     ap.add_argument("--da-stop-beta", type=float, default=0.1)
@@ -770,6 +796,11 @@ def main():
     ap.add_argument("--seeds", type=int, nargs="+", default=[1234],
                     help="random seeds of the compare/anneal runs (one plain and one DA run per seed)")
     ap.add_argument("--rms-limit", type=float, default=0.5)
+    ap.add_argument("--surrogate", default="mlp", choices=["mlp", "subset"],
+                    help="first stage of delayed acceptance: the MLP field surrogate or the exact model "
+                         "on every k-th station (k from --subset-strides)")
+    ap.add_argument("--subset-strides", type=int, nargs="+", default=[32, 16, 8],
+                    help="station strides of the subset surrogate, coarsest first (one picked per stage)")
     ap.add_argument("--delta-limit", type=float, default=2.0)
     ap.add_argument("--refit-epochs", type=int, default=None, help="training epochs of every fit after the first")
     ap.add_argument("--epochs", type=int, default=40)

@@ -12,7 +12,7 @@ import pytest
 import torch
 
 from altar_gb300 import Application, _native
-from altar_gb300.bayesian import Annealer, DelayedAcceptance, Surrogate
+from altar_gb300.bayesian import Annealer, DelayedAcceptance, SubsetSurrogate, Surrogate
 from altar_gb300.bayesian.coolingstep import StageState
 from altar_gb300.device import ptr, stream_handle
 from altar_gb300.distributions import Uniform
@@ -238,6 +238,37 @@ def test_surrogate_transition_posterior(cuda):
                            inner=3, outer=2, stop_beta=1.0)
     dw = run(da)
     assert any(r.get("mode") == "da" for r in dw.reports)
+    tp, td = plain.step.theta.cpu().numpy(), dw.step.theta.cpu().numpy()
+    for j in range(4):
+        sd = tp[:, j].std()
+        assert abs(td[:, j].mean() - tp[:, j].mean()) < 4 * sd / np.sqrt(2048 / 8), j
+        assert abs(td[:, j].std() - sd) < 0.5 * sd, j
+
+
+def test_subset_surrogate_transition_posterior(cuda):
+    """The coarse (every k-th station) likelihood as the first stage, with the stride picked
+    per stage from three levels: the exact correction keeps the posterior of plain Metropolis."""
+    g = np.linspace(-15e3, 15e3, 32)
+    X, Y = [a.ravel() for a in np.meshgrid(g, g)]
+    los = np.tile(LOS, (X.size, 1))
+    rng = np.random.default_rng(0)
+    d = catmip.mogi_los(np.array([[0.0, 0.0, 3e3, 2e6]]), X, Y, los, 0.25, log_strength=False)[0]
+    d = d + rng.normal(0, 5e-3, X.size)
+
+    def run(sampler):
+        psets = {"location": Contiguous(2, Uniform((-1e4, 1e4))), "depth": Contiguous(1, Uniform((1e3, 8e3))),
+                 "source": Contiguous(1, Uniform((1e5, 1e7)))}
+        model = Mogi(psets, observations=Observations(X, Y, los, d, 2.5e-5), log_strength=False)
+        app = Application(model, job=Job(chains=2048, steps=5), rng=RNG(9), controller=Annealer(sampler=sampler))
+        app.run()
+        return app.controller.worker
+
+    plain = run(None)
+    sur = SubsetSurrogate(strides=(16, 8, 4))
+    da = DelayedAcceptance(surrogate=sur, delta_limit=1.0, check_chains=128, inner=10, outer=1, stop_beta=1.0)
+    dw = run(da)
+    used = [r.get("stride") for r in dw.reports if r.get("mode") == "da"]
+    assert used and set(used) <= {16, 8, 4}
     tp, td = plain.step.theta.cpu().numpy(), dw.step.theta.cpu().numpy()
     for j in range(4):
         sd = tp[:, j].std()
