@@ -238,8 +238,13 @@ class SubsetSurrogate:
     needs_fit = False
     trained = True
 
-    def __init__(self, strides=(32, 16, 8)):
+    def __init__(self, strides=(32, 16, 8), inner=None):
+        """inner: surrogate moves per exact correction at each level (None: the sampler's own
+        count at every level); finer levels cost more per move and can take fewer."""
         self.strides = tuple(int(s) for s in (strides if hasattr(strides, "__iter__") else (strides,)))
+        self.inner = None if inner is None else tuple(int(k) for k in inner)
+        if self.inner is not None and len(self.inner) != len(self.strides):
+            raise ValueError("one inner count per stride")
         self.levels = len(self.strides)
         self.level = 0
         self.strategies = []
@@ -479,6 +484,11 @@ class DelayedAcceptance(Metropolis):
         err2 = ((approx - exact) ** 2 * w).sum(1) / strat.stations.m
         return float(torch.sqrt(err2.mean()))
 
+    def _inner(self):
+        """Surrogate moves per exact correction: the surrogate's per-level count if it has one."""
+        per_level = getattr(self.surrogate, "inner", None)
+        return int(per_level[self.surrogate.level]) if per_level else self.inner
+
     # ---- walks
     def walkChains(self, annealer, step):
         if self.mode == "da":
@@ -522,8 +532,9 @@ class DelayedAcceptance(Metropolis):
             pr_s.copy_(step.prior)
             su_s.copy_(sur_cur)
             _native.call("ag_posterior", st, n, ptr(pr_s), ptr(su_s), ptr(po_s), s)
-            for j in range(self.inner):
-                sid = 1000 + o * self.inner + j
+            inner = self._inner()
+            for j in range(inner):
+                sid = 1000 + o * inner + j
                 _native.call("ag_propose", st, ptr(th_s), n, p, ptr(model.lo), ptr(model.hi), self.seed, sid,
                              ptr(cand), ptr(mask), ptr(cprior), s)
                 sur.predict(cand, lo, hi, sur_cand, bufs, mask=mask)

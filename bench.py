@@ -249,7 +249,7 @@ def anneal(kind, X, Y, los, d, N, rank, args, seed=1234, max_stages=None):
     from altar_gb300.simulations import RNG, Job
     sampler = None
     if kind == "da":
-        sur = (SubsetSurrogate(strides=args.subset_strides) if args.surrogate == "subset"
+        sur = (SubsetSurrogate(strides=args.subset_strides, inner=args.subset_inner) if args.surrogate == "subset"
                else Surrogate(seed=5, batch=1024))
         sampler = DelayedAcceptance(surrogate=sur, rms_limit=args.rms_limit,
                                     delta_limit=args.delta_limit, epochs=args.epochs,
@@ -585,7 +585,7 @@ def run_ours(args):
                            "da": {"inner": args.da_inner, "outer": args.da_outer,
                                   "delta_limit": args.delta_limit, "rms_limit": args.rms_limit,
                                   "stop_beta": args.da_stop_beta, "surrogate": args.surrogate,
-                                  "subset_strides": args.subset_strides}},
+                                  "subset_strides": args.subset_strides, "subset_inner": args.subset_inner}},
                 "runs": out, "untimed_warmup_s": warm}
         if args.mode == "compare":
             tp = sum(out[f"plain_s{s_}"]["time_s"] for s_ in args.seeds)
@@ -764,13 +764,14 @@ def run_ours(args):
         # the same run with delayed acceptance, first stage the exact model on a station subset
         # (after an untimed short run: graph captures of each level)
         saved = (args.surrogate, args.subset_strides, args.da_inner, args.da_outer, args.delta_limit,
-                 args.da_stop_beta)
+                 args.da_stop_beta, args.subset_inner)
         args.surrogate, args.subset_strides, args.da_inner, args.da_outer = "subset", [32, 16, 8], 20, 1
+        args.subset_inner = None
         args.delta_limit, args.da_stop_beta = 1.0, 1.0
         anneal("da", X, Y, los, d, N, rank, args, seed=1, max_stages=3)
         da = anneal("da", X, Y, los, d, N, rank, args)
         (args.surrogate, args.subset_strides, args.da_inner, args.da_outer, args.delta_limit,
-         args.da_stop_beta) = saved
+         args.da_stop_beta, args.subset_inner) = saved
         sd = np.array(full["invariants"]["sd"])
         line["full_run_da"] = {
             "time_s": da["time_s"], "stages": da["stages"], "final_beta": da["final_beta"],
@@ -824,6 +825,8 @@ def main():
                          "on every k-th station (k from --subset-strides)")
     ap.add_argument("--subset-strides", type=int, nargs="+", default=[32, 16, 8],
                     help="station strides of the subset surrogate, coarsest first (one picked per stage)")
+    ap.add_argument("--subset-inner", type=int, nargs="+", default=None,
+                    help="surrogate moves per exact correction at each subset level (default: --da-inner)")
     ap.add_argument("--delta-limit", type=float, default=2.0)
     ap.add_argument("--refit-epochs", type=int, default=None, help="training epochs of every fit after the first")
     ap.add_argument("--epochs", type=int, default=40)
