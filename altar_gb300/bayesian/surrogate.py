@@ -256,6 +256,8 @@ class SubsetSurrogate:
     def attach(self, application, model):
         from ..models.forward import CUDA
         from ..models.observations import Observations
+        if not isinstance(getattr(model, "strategy", None), CUDA) or getattr(model, "obs", None) is None:
+            raise TypeError("SubsetSurrogate needs a point-source model with station observations (CDM, Mogi)")
         obs = model.obs
         self.strategies = []
         for k in self.strides:
