@@ -45,6 +45,17 @@ class Bayesian:
         self.lo, self.hi, self.prep_lo, self.prep_hi = as_dev(lo), as_dev(hi), as_dev(plo), as_dev(phi)
         return self
 
+    def meta(self, path="parameters.csv"):
+        """Persist the sample layout: one row (name, count, offset) per parameter set, the
+        file the reference's models write at initialisation (models/cdm/cdm/CDM.py:358-380)."""
+        import csv
+        with open(path, mode="w", newline="") as stream:
+            writer = csv.writer(stream)
+            writer.writerow(["name", "count", "offset"])
+            for name, pset in self.psets.items():
+                writer.writerow([name, pset.count, pset.offset])
+        return self
+
     def initializeSample(self, step, attempt=0, redraw=None):
         """θ from the prep distributions (Base.py:44-54)."""
         _native.call("ag_prior_sample", step.samples, self.parameters, ptr(self.prep_lo),
