@@ -283,7 +283,7 @@ class DelayedAcceptance(Metropolis):
 
     def __init__(self, surrogate=None, rms_limit=0.5, delta_limit=2.0, fit_chains=4096, check_chains=256,
                  epochs=40, refit_epochs=None, start_beta=0.0, stop_beta=0.1, retry_every=3, spread=3.0,
-                 inner=10, outer=1, **kwds):
+                 inner=10, outer=1, screen_limit=None, **kwds):
         """rms_limit: largest RMS field error (data standard deviations) of a usable surrogate;
         delta_limit: largest spread (standard deviation over trial proposals) of the error of
         the surrogate's tempered log-posterior ratio, β[(s(y) - s(x)) - (l(y) - l(x))].  Delayed
@@ -301,6 +301,10 @@ class DelayedAcceptance(Metropolis):
         summaries matched plain Metropolis to within its own run-to-run spread."""
         super().__init__(**kwds)
         self.delta_limit = float(delta_limit)
+        # coarse-model surrogates: when no level passes delta_limit for the surrogate-transition
+        # walk but the finest passes screen_limit, the stage walks with two-stage delayed
+        # acceptance (every step screened by the coarse model, the exact model on the survivors)
+        self.screen_limit = None if screen_limit is None else float(screen_limit)
         self.delta = None
         self._prepare_s = 0.0
         self._backoff = 0
@@ -336,16 +340,16 @@ class DelayedAcceptance(Metropolis):
 
     def mode_key(self):
         # each level of a subset surrogate reads other stations: one captured walk per level
-        if self.mode == "da" and not self.surrogate.needs_fit:
-            return f"da{self.surrogate.level}"
+        if self.mode in ("da", "screen") and not self.surrogate.needs_fit:
+            return f"{self.mode}{self.surrogate.level}"
         return self.mode
 
     def report(self):
         rep = {"mode": self.mode, "rms_sigma": self.rms, "delta_sd": self.delta, "refits": self.refits,
                "prepare_s": self._prepare_s}
-        if self.mode == "da" and self.screened is not None:
+        if self.mode in ("da", "screen") and self.screened is not None:
             rep["screened"] = int(self.screened.item())
-        if self.mode == "da" and not self.surrogate.needs_fit:
+        if self.mode in ("da", "screen") and not self.surrogate.needs_fit:
             rep["stride"] = self.surrogate.stride
         return rep
 
@@ -380,6 +384,8 @@ class DelayedAcceptance(Metropolis):
             level, self.delta = self._delta_check(annealer, step, chk_rows, levels=range(sur.levels))
             sur.level = level
             self.mode = "da" if self._usable() else "plain"
+            if self.mode == "plain" and self.screen_limit is not None and self.delta <= self.screen_limit:
+                self.mode = "screen"
             return self
         if sur.trained:
             self.rms = self._check(annealer, step, chk_rows)
@@ -496,6 +502,8 @@ class DelayedAcceptance(Metropolis):
         if self.mode == "da":
             if self.inner > 1:
                 return self._walk_transition(annealer, step)
+            return self._walk_da(annealer, step)
+        if self.mode == "screen":
             return self._walk_da(annealer, step)
         return super().walkChains(annealer, step)
 

@@ -256,7 +256,7 @@ def anneal(kind, X, Y, los, d, N, rank, args, seed=1234, max_stages=None):
                                     refit_epochs=args.refit_epochs,
                                     start_beta=args.da_start_beta, stop_beta=args.da_stop_beta,
                                     inner=args.da_inner,
-                                    outer=args.da_outer)
+                                    outer=args.da_outer, screen_limit=args.screen_limit)
     model = CDM(cdm_psets(), observations=Observations(X, Y, los, d, SIGMA ** 2), autotune=not args.no_autotune)
     app = Application(model, job=Job(chains=N, steps=args.walk_steps), rng=RNG(seed + rank),
                       controller=Annealer(sampler=sampler))
@@ -825,6 +825,9 @@ def main():
                          "on every k-th station (k from --subset-strides)")
     ap.add_argument("--subset-strides", type=int, nargs="+", default=[32, 16, 8],
                     help="station strides of the subset surrogate, coarsest first (one picked per stage)")
+    ap.add_argument("--screen-limit", type=float, default=None,
+                    help="coarse-model DA: ratio spread up to which a stage that fails --delta-limit "
+                         "still screens every step on the finest level (two-stage delayed acceptance)")
     ap.add_argument("--subset-inner", type=int, nargs="+", default=None,
                     help="surrogate moves per exact correction at each subset level (default: --da-inner)")
     ap.add_argument("--delta-limit", type=float, default=2.0)
