@@ -690,13 +690,35 @@ struct ResampleHdr {
 };
 
 // sequential FP64 partial sums, as itertools.accumulate (COV.py:242-251)
-__global__ void cdf_kernel(const double* __restrict__ w, int n, double* __restrict__ edges) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+// The additions stay strictly sequential (the reference's accumulation order, so the edges
+// are bit-exact); one warp streams w through a shared-memory double buffer so that lane 0's
+// chain of dependent additions never waits on global-memory latency.
+constexpr int kCdfChunk = 1024;
+__global__ void __launch_bounds__(32) cdf_kernel(const double* __restrict__ w, int n,
+                                                 double* __restrict__ edges) {
+    __shared__ double buf[2][kCdfChunk];
+    if (blockIdx.x != 0) return;
+    const int lane = threadIdx.x;
+    const int nchunks = (n + kCdfChunk - 1) / kCdfChunk;
+    auto load = [&](int c) {
+        const int base = c * kCdfChunk;
+        for (int k = lane; k < kCdfChunk; k += 32) buf[c & 1][k] = (base + k < n) ? w[base + k] : 0.0;
+    };
     double acc = 0.0;
-    edges[0] = 0.0;
-    for (int i = 0; i < n; ++i) {
-        acc += w[i];
-        edges[i + 1] = acc;
+    if (lane == 0) edges[0] = 0.0;
+    if (nchunks > 0) load(0);
+    __syncwarp();
+    for (int c = 0; c < nchunks; ++c) {
+        if (c + 1 < nchunks) load(c + 1);            // the next chunk streams in meanwhile
+        if (lane == 0) {
+            const int base = c * kCdfChunk, len = min(kCdfChunk, n - base);
+            const double* b = buf[c & 1];
+            for (int k = 0; k < len; ++k) {
+                acc += b[k];
+                edges[base + k + 1] = acc;
+            }
+        }
+        __syncwarp();
     }
 }
 
