@@ -224,6 +224,14 @@ class _SubsetModel:
         return self._model.layout()
 
 
+def subset_observations(obs, k):
+    """Every k-th observation of obs with its variance divided by k (its misfit weight
+    multiplied by k), so that the subset's misfit sum estimates the full one."""
+    from ..models.observations import Observations
+    return Observations(obs.x[::k], obs.y[::k], obs.los[::k], obs.d[::k], obs.variance[::k] / k,
+                        None if obs.oid is None else obs.oid[::k])
+
+
 class SubsetSurrogate:
     """Coarse likelihood: the exact forward model on every ``stride``-th observation, with
     the misfit weights multiplied by ``stride``, so that its data log-likelihood estimates
@@ -255,14 +263,11 @@ class SubsetSurrogate:
 
     def attach(self, application, model):
         from ..models.forward import CUDA
-        from ..models.observations import Observations
         if not isinstance(getattr(model, "strategy", None), CUDA) or getattr(model, "obs", None) is None:
             raise TypeError("SubsetSurrogate needs a point-source model with station observations (CDM, Mogi)")
-        obs = model.obs
         self.strategies = []
         for k in self.strides:
-            sub = Observations(obs.x[::k], obs.y[::k], obs.los[::k], obs.d[::k], obs.variance[::k] / k,
-                               None if obs.oid is None else obs.oid[::k])
+            sub = subset_observations(model.obs, k)
             strat = CUDA(model.strategy.kind).initialize(application=application, model=_SubsetModel(model, sub))
             strat.norm = model.strategy.norm           # constants cancel; keep the exact model's
             self.strategies.append(strat)
