@@ -256,11 +256,12 @@ AG_DEVICE_INLINE float log2_ratio(float s, float rho) {
 // atan2(y, x): octant reduction to t = min/max in [0, 1], atan(t) = t·P(t²) with
 // P of degree 8, coefficients fitted here by iteratively reweighted least squares
 // on the relative error over [0, 1] (<= 1.9 ulp in FP32 Horner form), then
-// π/2 - r, π - r and the sign of y restore the quadrant.  atan2(0, 0) = 0.
+// π/2 - r, π - r and the sign of y restore the quadrant.  atan2(0, 0) = 0; for
+// |x|, |y| above 1e-23 the offset in the reciprocal does not change the result.
 AG_DEVICE_INLINE float atan2_poly(float y, float x) {
     const float ax = fabsf(x), ay = fabsf(y);
     const float mx = fmaxf(ax, ay), mn = fminf(ax, ay);
-    const float t = (mx > 0.0f) ? mn * fast_rcp(mx) : 0.0f;
+    const float t = mn * fast_rcp(mx + 1e-30f);      // the tiny offset makes atan2(0, 0) = 0
     const float u = t * t;
     float p = 2.903841436e-03f;
     p = fmaf(p, u, -1.628421992e-02f);
@@ -451,7 +452,10 @@ AG_DEVICE_INLINE void side_pair(const K& k, V Xr, V Yr, V& ue, V& un, V& uv, boo
     v1 = vfma(KN(K_C1M10), ndm10, v1);
     v1 = vfma(dy1ir, X1, v1);
     v1 = vfma(y1irA, dX1, v1);
-    v1 = vfma(sg, vfma(KC(K_C1Q), dLq, vmul(KC(K_C1M11), dm11)), v1);
+    // configuration-signed terms: sg Δlog(r - z3) and sg Δm11 (sg² = 1)
+    const V sgdLq = vmul(sg, dLq), sgdm11 = vmul(sg, dm11);
+    v1 = vfma(KC(K_C1Q), sgdLq, v1);
+    v1 = vfma(KC(K_C1M11), sgdm11, v1);
     V v2 = vmul(KC(K_C2F), dF);
     v2 = vfma(KC(K_C2P), dLp, v2);
     v2 = vfma(KC(K_KC2), ndm1, v2);
@@ -461,7 +465,7 @@ AG_DEVICE_INLINE void side_pair(const K& k, V Xr, V Yr, V& ue, V& un, V& uv, boo
     v2 = vfma(KC(K_B2), vfma(dy1ir, m1B, vneg(vmul(y1irA, ndm1))), v2);
     v2 = vfma(vneg(ndy2ir), X2, v2);
     v2 = vfma(y2irA, dX2, v2);
-    v2 = vfma(vmul(sg, KC(K_C2Q)), dLq, v2);
+    v2 = vfma(KC(K_C2Q), sgdLq, v2);
     V v3 = vmul(KC(K_C3F), dF);
     v3 = vfma(KN(K_KC2L), dLp, v3);
     v3 = vfma(KN(K_NB1), ndm1, v3);
@@ -469,7 +473,8 @@ AG_DEVICE_INLINE void side_pair(const K& k, V Xr, V Yr, V& ue, V& un, V& uv, boo
     v3 = vfma(KN(K_C3M10), ndm10, v3);
     v3 = vfma(ndair, X1, v3);
     v3 = vfma(nairA, dX1, v3);
-    v3 = vfma(sg, vfma(KC(K_C3Q), dLq, vmul(KC(K_C3M11), dm11)), v3);
+    v3 = vfma(KC(K_C3Q), sgdLq, v3);
+    v3 = vfma(KC(K_C3M11), sgdm11, v3);
     if (steep) {
         // Near-vertical side: the log terms are K·Q plus benign remainders (set-up), with
         //   Q = Δlog(r+a) - sg cos β Δlog(r-z3) = O(β)
@@ -497,7 +502,8 @@ AG_DEVICE_INLINE void side_pair(const K& k, V Xr, V Yr, V& ue, V& un, V& uv, boo
         v2 = vfma(KC(K_KQ2), Q, v2);
         v3 = vfma(KC(K_KQ3), Q, v3);
     }
-    // back to EFCS: columns e1 = (c, s, 0), e2 = (s, -c, 0), e3 = (0, 0, -1)
+    // back to EFCS: columns e1 = (c, s, 0), e2 = (s, -c, 0), e3 = (0, 0, -1); v3 is summed on
+    // its own before it meets the running total (finer rounding than adding term by term)
     ue = vfma(c, v1, vfma(s, v2, ue));
     un = vfma(s, v1, vfma(KN(K_C), v2, un));
     uv = vsub(uv, v3);

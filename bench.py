@@ -39,7 +39,7 @@ PRIORS = [(-1e4, 1e4), (-1e4, 1e4), (1e3, 1e4), (-50.0, 50.0), (100.0, 3000.0), 
 # parameter order: x0, y0, depth, opening, ax, ay, az, ωx, ωy, ωz
 # FP32 operations per (chain, station) pair of the fused CDM kernel (FMA = 2): per
 # rectangle side 249 (the difference-arithmetic pair of altar_gb300/csrc/cdm_side.cuh
-# including 2 x 10 for log2_ratio and 21 for atan2_poly, counted by evaluating the pair
+# including 2 x 10 for log2_ratio and 22 for atan2_poly, counted by evaluating the pair
 # with a counting number type: tests/cdm_host/cdm_host.cpp), times 12 sides, + 31 per
 # station (coordinates, LOS projection, float-float misfit); special-function unit: 13
 # per side (2 rsqrt, 9 rcp, 2 lg2)

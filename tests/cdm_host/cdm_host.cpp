@@ -79,8 +79,9 @@ inline CountF frcp(CountF x) { g_sfu += 1; return 1.0f / x.v; }
 inline CountF vrsqrt(CountF x) { g_sfu += 1; return 1.0f / std::sqrt(x.v); }
 // log2_ratio: s², 4 FMA, s·p (10 FLOP) + one base-2 logarithm
 inline CountF vlog2r(CountF s, CountF r) { g_flop += 10; g_sfu += 1; return log2_ratio(s.v, r.v); }
-// atan2_poly: mn/mx (mul), t², 8 FMA, t·p, two quadrant subtractions (21 FLOP) + one reciprocal
-inline CountF vatan2(CountF y, CountF x) { g_flop += 21; g_sfu += 1; return atan2_poly(y.v, x.v); }
+// atan2_poly: mx + 1e-30, mn/mx (mul), t², 8 FMA, t·p, two quadrant subtractions (22 FLOP)
+// + one reciprocal
+inline CountF vatan2(CountF y, CountF x) { g_flop += 22; g_sfu += 1; return atan2_poly(y.v, x.v); }
 
 extern "C" void cdm_host_side_counts(long* flop, long* sfu, long* flop_steep, long* sfu_steep) {
     SideC S;
