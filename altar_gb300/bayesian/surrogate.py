@@ -271,12 +271,15 @@ class SubsetSurrogate:
             strat = CUDA(model.strategy.kind).initialize(application=application, model=_SubsetModel(model, sub))
             strat.norm = model.strategy.norm           # constants cancel; keep the exact model's
             self.strategies.append(strat)
+        self._main = model.strategy
         return self
 
     def predict(self, theta, lo, hi, out_llk, bufs, mask=None):
         """Coarse data log-likelihood of device θ rows into out_llk; rows flagged in mask are
         skipped and sources above the surface are flagged there."""
-        self.strategies[self.level].forward(theta, out_llk, mask=mask, status=mask)
+        strat = self.strategies[self.level]
+        strat.layout.variant = self._main.layout.variant   # the exact model's (autotuned) launch shape
+        strat.forward(theta, out_llk, mask=mask, status=mask)
         return out_llk
 
     def buffers(self, n, p):

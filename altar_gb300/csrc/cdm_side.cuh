@@ -84,21 +84,26 @@ AG_CDM_FN void fill_side(SideC& S, Vec3 pa, Vec3 pb, Vec3 bvec, double nu, doubl
     const double LN2 = 0.69314718055994530942;
     Vec3 side = v_sub(pb, pa);
     double L = sqrt(v_dot(side, side));
-    double beta = acos(-side.z / L);
-    // vertical sides contribute nothing (libcdm.py:320-324)
-    const double eps = 2.220446049250313e-16;
+    const double iL = 1.0 / L;
+    double cb = -side.z * iL;                        // cos β, β in [0, π]
+    // vertical sides contribute nothing (libcdm.py:320-324: |β| or |π - β| below the double
+    // epsilon, i.e. cos β = ±1 exactly; acos of the next double below 1 is already 1.5e-8)
     steep = false;
-    if (!(L > 0.0) || fabs(beta) < eps || fabs(PI - beta) < eps) {
+    if (!(L > 0.0) || !(fabs(cb) < 1.0)) {
         active = false;
         return;
     }
     active = true;
     double hl = sqrt(side.x * side.x + side.y * side.y);
-    double c = side.x / hl, s = side.y / hl;         // e1 = (c, s, 0), e2 = (s, -c, 0)
-    double sb = hl / L, cb = -side.z / L;            // β in (0, π): sin β >= 0
-    double tb2 = (cb >= 0.0) ? sb / (1.0 + cb) : (1.0 - cb) / sb;
-    double ctb2 = 1.0 / tb2;
-    double cot = cb / sb;
+    const double ihl = 1.0 / hl;
+    double c = side.x * ihl, s = side.y * ihl;       // e1 = (c, s, 0), e2 = (s, -c, 0)
+    double sb = hl * iL;                             // sin β >= 0
+    const double isb = 1.0 / sb;
+    const double i1pc = 1.0 / (1.0 + fabs(cb));      // no cancellation in 1 + |cos β|
+    // tan(β/2) = sin β/(1 + cos β) = (1 - cos β)/sin β, cot(β/2) its inverse
+    double tb2 = (cb >= 0.0) ? sb * i1pc : (1.0 - cb) * isb;
+    double ctb2 = (cb >= 0.0) ? (1.0 + cb) * isb : sb * i1pc;
+    double cot = cb * isb;
     double k = 1.0 - 2.0 * nu;
     double rx = pa.x - x0, ry = pa.y - y0;
     double k1 = c * rx + s * ry;
@@ -119,7 +124,7 @@ AG_CDM_FN void fill_side(SideC& S, Vec3 pa, Vec3 pb, Vec3 bvec, double nu, doubl
     double C1m10 = -b1 * sb * cb + b3 * sb * sb;
     double C3m10 = -b1 * cb * cb + b3 * sb * cb;
     double C1Q = -kc2 * cot * cb;
-    double C2Q = -kc1 / sb;
+    double C2Q = -kc1 * isb;
     double C3Q = kc2 * cb;
     double C1m11 = b2 * sb;
     double C3m11 = b2 * cb;
@@ -134,7 +139,7 @@ AG_CDM_FN void fill_side(SideC& S, Vec3 pa, Vec3 pb, Vec3 bvec, double nu, doubl
     S.q[6] = make_float4((float)b1, (float)b2, (float)C1m10, (float)C3m10);
     S.q[7] = make_float4((float)(LN2 * C1Q), (float)(LN2 * C2Q), (float)(LN2 * C3Q), (float)C1m11);
     S.q[8] = make_float4((float)C3m11, (float)C1m12, (float)(aA * sb), (float)(-aA * cb));
-    const double omc = sb * sb / (1.0 + fabs(cb));   // 1 - |cos β| without cancellation
+    const double omc = sb * sb * i1pc;               // 1 - |cos β| without cancellation
     const double sgn = (cb >= 0.0) ? 1.0 : -1.0;
     S.q[9] = make_float4((float)(dy1 * cb + da * sb), (float)(dy1 * sb - da * cb), (float)(LN2 * kc2), (float)omc);
     S.q[10] = make_float4((float)(aA * omc), (float)(da * omc + sgn * dy1 * sb), (float)(sgn * sb),

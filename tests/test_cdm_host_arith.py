@@ -94,3 +94,17 @@ def test_steep_sides_without_cot2_amplification(host):
         err = np.max(np.abs(out - ref)) / np.max(np.abs(ref))
         cot = 1.0 / np.tan(np.radians(min_vertical_angle(th)))
         assert err <= 2e-5 * cot, (min_vertical_angle(th), err)
+
+
+def test_exactly_vertical_sides(host):
+    """Unrotated or axis-aligned bodies have sides exactly along the vertical, which the
+    reference drops (libcdm.py:320-324); the set-up recognises them without acos."""
+    g = np.linspace(-20e3, 20e3, 30)
+    X, Y = [np.ascontiguousarray(a.ravel()) for a in np.meshgrid(g, g)]
+    los = np.ascontiguousarray(np.tile(LOS, (X.size, 1)))
+    for omega in ((0.0, 0.0, 0.0), (0.0, 90.0, 0.0), (45.0, 0.0, 0.0)):
+        th = np.array([1000.0, -2000.0, 4000.0, 10.0, 800.0, 1200.0, 600.0, *omega])
+        ref = cdm.los_displacements(th, CDM_LAYOUT, X, Y, los, 0.25)
+        out = np.empty(X.size)
+        assert host.cdm_host_los(_dp(th), X.size, _dp(X), _dp(Y), _dp(los), 0.25, _dp(out)) == 0
+        assert np.max(np.abs(out - ref)) <= 1e-5 * np.max(np.abs(ref)), omega
