@@ -30,13 +30,13 @@ constexpr int kSides = 12;
 // logs are evaluated in base 2) and those of the Burgers-function difference
 // carry the factor 2 of Fi = 2 atan2(...).
 //
-// Near-vertical ("steep") sides, |cot β| >= kSteepCot: the coefficients of the
-// log differences grow like cot²β while the combination they multiply,
-// Q = Δlog(r+a) - sg cos β Δlog(r-z3), is O(β); evaluated as two O(1) logs
-// it cancels and FP32 rounding is amplified by cot²β.  For these sides the
-// set-up splits the log terms into Q (coefficients KQ1..KQ3) plus benign
-// remainders (C1P, C2P, C2Q replaced, C1Q, C3Q, kc2L zero), and the pair
-// evaluates Q from exact identities without the cancellation (side_pair).
+// Near-vertical ("steep") sides, |cot β| >= kSteepCot: several coefficients grow
+// like cot β and cot²β while the combinations they multiply are O(β); evaluated
+// term by term they cancel and FP32 rounding (of the terms and of the side
+// constants) is amplified by cot β.  These sides take their own evaluation
+// (side_pair with Steep = true): the ratio configuration at every station, and the
+// cancelling groups rewritten as two remainders computed without cancellation,
+// with O(1) coefficients (derivation at side_pair_t).
 struct __align__(16) SideC {
     float4 q[12];
 };
@@ -50,16 +50,17 @@ struct __align__(16) SideC {
 // q7: C1Q, C2Q, C3Q, C1m11    ln 2 × configuration-signed coefficients of Δlog(r-z3)
 // q8: C3m11, C1m12, aAsb, naAcb   aA·sin β, -aA·cos β
 // q9: dz1, dz3, kc2L, omc     Δz1, Δz3 (configuration II); ln 2 · kc2; 1 - |cos β|
-// q10: a1c, dc, ssb, KQ1      steep sides: aA·omc, Δc, sign(cos β)·sin β, ln 2 k cot²β b2
-// q11: KQ2, KQ3, 0, 0         steep sides: ln 2 k cot²β b1, -ln 2 k cot β b2
+// q10: a1c, dc, ssb, cot      steep sides: aA·omc, Δc, sign(cos β)·sin β, cot β
+// q11: kr1, kr2, t, ct2       steep sides: k cot β b2, k cot β b1, tan(β'/2), cot(β'/2)
+//                             (β' the ratio-configuration angle)
 constexpr double kSteepCot = 3.0;
 
 // Per-side constant by its position in SideC (q[i >> 2], component i & 3)
 enum : int {
     K_C = 0, K_S, K_K1, K_K2, K_DY1, K_AA, K_AB, K_DA, K_SB, K_CB, K_TB2, K_CTB2, K_DAS, K_C1F, K_C2F, K_C3F,
     K_C1P, K_C2P, K_KC1, K_KC2, K_NB1, K_NB2, K_HB1, K_HB2, K_B1, K_B2, K_C1M10, K_C3M10, K_C1Q, K_C2Q, K_C3Q,
-    K_C1M11, K_C3M11, K_C1M12, K_AASB, K_NAACB, K_DZ1, K_DZ3, K_KC2L, K_OMC, K_A1C, K_DC, K_SSB, K_KQ1,
-    K_KQ2, K_KQ3
+    K_C1M11, K_C3M11, K_C1M12, K_AASB, K_NAACB, K_DZ1, K_DZ3, K_KC2L, K_OMC, K_A1C, K_DC, K_SSB, K_COT,
+    K_KR1, K_KR2, K_T, K_CT2
 };
 
 // ---------------------------------------------------------------------------
@@ -142,18 +143,21 @@ AG_CDM_FN void fill_side(SideC& S, Vec3 pa, Vec3 pb, Vec3 bvec, double nu, doubl
     const double omc = sb * sb * i1pc;               // 1 - |cos β| without cancellation
     const double sgn = (cb >= 0.0) ? 1.0 : -1.0;
     S.q[9] = make_float4((float)(dy1 * cb + da * sb), (float)(dy1 * sb - da * cb), (float)(LN2 * kc2), (float)omc);
-    S.q[10] = make_float4((float)(aA * omc), (float)(da * omc + sgn * dy1 * sb), (float)(sgn * sb),
-                          (float)(LN2 * k * cot * cot * b2));
-    S.q[11] = make_float4((float)(LN2 * k * cot * cot * b1), (float)(-LN2 * k * cot * b2), 0.f, 0.f);
+    S.q[10] = make_float4(0.f, 0.f, 0.f, 0.f);
+    S.q[11] = make_float4(0.f, 0.f, 0.f, 0.f);
     steep = fabs(cot) >= kSteepCot;
     if (steep) {
-        // log terms as KQ·Q plus remainders (derivation at side_pair)
+        // ratio configuration: β' = β if cos β > 0, β - π otherwise; t = tan(β'/2)
+        const double t = (cb > 0.0) ? tb2 : -ctb2;
+        S.q[3].y = (float)(2.0 * b1);                  // ΔFi: the k cot²β parts are in R_F
+        S.q[3].z = (float)(2.0 * b2);
         S.q[4].x = (float)(-LN2 * 0.5 * k * b2);       // v1: -k b2/2 · Δlog(r+a)
         S.q[4].y = (float)(LN2 * 0.5 * k * b1);        // v2: k b1/2 · Δlog(r+a)
-        S.q[7].x = 0.f;                                  // v1: no Δlog(r-z3) term
         S.q[7].y = (float)(-LN2 * k * b1 * cb);        // v2: -sg k b1 cos β · Δlog(r-z3)
-        S.q[7].z = 0.f;                                  // v3: no Δlog(r-z3) term
-        S.q[9].z = 0.f;                                  // v3: no Δlog(r+a) term
+        S.q[10] = make_float4((float)(aA * omc), (float)(da * omc + sgn * dy1 * sb), (float)(sgn * sb),
+                              (float)cot);
+        S.q[11] = make_float4((float)(k * cot * b2), (float)(k * cot * b1), (float)t,
+                              (float)((cb > 0.0) ? ctb2 : -tb2));
     }
 }
 
@@ -371,8 +375,8 @@ struct ScalarSide {
 // Δr = Δ(r²)/(r_A + r_B), Δlog u from s = Δu/(u_A + u_B), the Burgers-function
 // difference as one atan2 of the rotation from A to B), so the v(B) - v(A)
 // cancellation of the reference formula never happens in floating point.
-template <class V, class K>
-AG_DEVICE_INLINE void side_pair(const K& k, V Xr, V Yr, V& ue, V& un, V& uv, bool steep) {
+template <bool Steep, class V, class K>
+AG_DEVICE_INLINE void side_pair_t(const K& k, V Xr, V Yr, V& ue, V& un, V& uv) {
     const V c = KC(K_C), s = KC(K_S);
     const V dy1 = KC(K_DY1), aA = KC(K_AA), aB = KC(K_AB), da = KC(K_DA);
     // station in the angular-dislocation frame of vertex A; y2 is the same at B
@@ -380,10 +384,19 @@ AG_DEVICE_INLINE void side_pair(const K& k, V Xr, V Yr, V& ue, V& un, V& uv, boo
     const V y2 = vfma(s, Xr, vfma(KN(K_C), Yr, KN(K_K2)));
     const V y1B = vadd(y1A, dy1);
     // artefact-free configuration (libcdm.py:342-362): I if y1A >= 0 (β - π), else II (β);
-    // sin, cos and cot(β/2) of β - π are those of β times -1
-    const auto conf1 = vge0(y1A);
-    const V sg = vsel(conf1, V(-1.0f), V(1.0f));
-    const V ct2 = vsel(conf1, KN(K_TB2), KC(K_CTB2));
+    // sin, cos and cot(β/2) of β - π are those of β times -1.  A near-vertical side takes
+    // the ratio configuration (sg = sign cos β) at every station instead: its r - z3 has no
+    // zero and its Burgers-function argument no sign change at the free surface, and both
+    // configurations give the same pair away from the other's singular ray.
+    V sg, ct2;
+    if constexpr (Steep) {
+        sg = V(k.template at<K_CB>() > 0.0f ? 1.0f : -1.0f);
+        ct2 = KC(K_CT2);
+    } else {
+        const auto conf1 = vge0(y1A);
+        sg = vsel(conf1, V(-1.0f), V(1.0f));
+        ct2 = vsel(conf1, KN(K_TB2), KC(K_CTB2));
+    }
     const V y22 = vmul(y2, y2);
     // r (rA = r2A·irA enters every sum through an FMA)
     const V r2A = vfma(y1A, y1A, vfma(aA, aA, y22));
@@ -452,8 +465,10 @@ AG_DEVICE_INLINE void side_pair(const K& k, V Xr, V Yr, V& ue, V& un, V& uv, boo
     const V dX1 = vfma(KC(K_B2), dm2, dX2);
     V v1 = vmul(KC(K_C1F), dF);
     v1 = vfma(KC(K_C1P), dLp, v1);
-    v1 = vfma(KN(K_KC1), ndm1, v1);
-    v1 = vfma(KN(K_KC2), dm2, v1);
+    if constexpr (!Steep) {
+        v1 = vfma(KN(K_KC1), ndm1, v1);
+        v1 = vfma(KN(K_KC2), dm2, v1);
+    }
     v1 = vfma(KN(K_HB2), dm35, v1);
     v1 = vfma(KC(K_HB1), dm4, v1);
     v1 = vfma(KN(K_C1M10), ndm10, v1);
@@ -461,12 +476,14 @@ AG_DEVICE_INLINE void side_pair(const K& k, V Xr, V Yr, V& ue, V& un, V& uv, boo
     v1 = vfma(y1irA, dX1, v1);
     // configuration-signed terms: sg Δlog(r - z3) and sg Δm11 (sg² = 1)
     const V sgdLq = vmul(sg, dLq), sgdm11 = vmul(sg, dm11);
-    v1 = vfma(KC(K_C1Q), sgdLq, v1);
+    if constexpr (!Steep) v1 = vfma(KC(K_C1Q), sgdLq, v1);
     v1 = vfma(KC(K_C1M11), sgdm11, v1);
     V v2 = vmul(KC(K_C2F), dF);
     v2 = vfma(KC(K_C2P), dLp, v2);
-    v2 = vfma(KC(K_KC2), ndm1, v2);
-    v2 = vfma(KN(K_KC1), dm2, v2);
+    if constexpr (!Steep) {
+        v2 = vfma(KC(K_KC2), ndm1, v2);
+        v2 = vfma(KN(K_KC1), dm2, v2);
+    }
     v2 = vfma(KC(K_HB1), dm36, v2);
     v2 = vfma(KN(K_HB2), dm4, v2);
     v2 = vfma(KC(K_B2), vfma(dy1ir, m1B, vneg(vmul(y1irA, ndm1))), v2);
@@ -474,46 +491,84 @@ AG_DEVICE_INLINE void side_pair(const K& k, V Xr, V Yr, V& ue, V& un, V& uv, boo
     v2 = vfma(y2irA, dX2, v2);
     v2 = vfma(KC(K_C2Q), sgdLq, v2);
     V v3 = vmul(KC(K_C3F), dF);
-    v3 = vfma(KN(K_KC2L), dLp, v3);
+    if constexpr (!Steep) v3 = vfma(KN(K_KC2L), dLp, v3);
     v3 = vfma(KN(K_NB1), ndm1, v3);
     v3 = vfma(KN(K_NB2), dm2, v3);
     v3 = vfma(KN(K_C3M10), ndm10, v3);
     v3 = vfma(ndair, X1, v3);
     v3 = vfma(nairA, dX1, v3);
-    v3 = vfma(KC(K_C3Q), sgdLq, v3);
+    if constexpr (!Steep) v3 = vfma(KC(K_C3Q), sgdLq, v3);
     v3 = vfma(KC(K_C3M11), sgdm11, v3);
-    if (steep) {
-        // Near-vertical side: the log terms are K·Q plus benign remainders (set-up), with
-        //   Q = Δlog(r+a) - sg cos β Δlog(r-z3) = O(β)
-        // from exact identities in p = r + a, q = r - z3, c = a (1 - |cos β|) + sign(cos β) y1 sin β:
-        //   ratio form (sg = sign cos β):   p/q = 1 + c/q,        Q = Δlog(p/q) + (1 - |cos β|) Δlog q
-        //   product form (sg = -sign cos β): p q = y1² + y2² + p c, Q = Δlog(pq) - (1 - |cos β|) Δlog q
-        // where c/q and the terms of p q carry no cancellation, and their differences come from
-        // the product rule on (value at A, difference) pairs.
+    if constexpr (Steep) {
+        // Near-vertical side, ratio configuration (β' = β or β - π, t = tan(β'/2), |t| < 0.17).
+        // The terms whose coefficients grow like cot β or cot²β form, with p = r + a, q = r - z3,
+        // m1 = y2/p, m2 = y1/p, φ = atan2(y2, p cot(β'/2) - y1) and natural logarithms,
+        //   v1: 2 b1 Δφ - k b1 cot β R_F + k b2 cot β R_Q,   v2: 2 b2 Δφ + k b2 cot β R_F + k b1 cot β R_Q,
+        //   v3: -k b2 cot β Q,
+        //   R_F = 2 cot β Δφ - Δm1,   R_Q = cot β Q - Δm2,   Q = Δlog p - |cos β| Δlog q,
+        // where R_F, R_Q and Q are O(β).  Without cancellation:
+        //   * φ = atan(t μ) + const with μ = y2/(p - t y1), and 2 cot β = (1 - t²)/t, so
+        //     k cot β R_F = k (1 - t²)/2 · [(1 - t²) Δ(μ m2 - t μ³ A(t²μ²)) - t Δm1]
+        //     with A(u) = (w - atan w)/w³ = 1/3 - u/5 + u²/7 - ... (u = w² < 0.04: three terms);
+        //   * c = p - q = a (1 - |cos β|) + sg y1 sin β and E = c/q give p = q (1 + E),
+        //     Q = Δlog(1 + E) + (1 - |cos β|) Δlog q and cot β E - m2 = E m2 + (1 - |cos β|)(a cot β - y1)/q,
+        //     R_Q = cot β Δλ + Δ(E m2) + (1 - |cos β|) (Δ((a cot β - y1)/q) + cot β Δlog q),
+        //     λ = log(1 + E) - E, Δλ = -s (E_A + E_B) + 2 s³ (1/3 + s²/5 + s⁴/7 + ...), s = ΔE/(2 + E_A + E_B);
+        // every difference from (value at A, difference) pairs.  What is left has O(1) terms:
+        // -k b1/2 = -hb1 and k b2/2 = hb2 on G = (1 - t²)[...], and k b2 cot β, k b1 cot β on R_Q = O(β).
+        const V cot = KC(K_COT), omc = KC(K_OMC), t = KC(K_T), nt = KN(K_T);
         const V cA = vfma(KC(K_SSB), y1A, KC(K_A1C));
-        const V dc = KC(K_DC), omc = KC(K_OMC);
-        const auto ratio = vgt0(vmul(sg, KC(K_CB)));
-        // ratio form: E = c/q, Δlog(1 + E) from s = ΔE/(2 + E_A + E_B), ratio 1 + ΔE/(1 + E_A)
         const V EA = vmul(cA, iqA);
-        const V dE = vfma(dc, iqB, vneg(vmul(cA, ndiq)));
-        // product form: G = y1² + y2² + p c, Δlog G from s = ΔG/(G_A + G_B), ratio 1 + ΔG/G_A
-        const V GA = vfma(pA, cA, vfma(y1A, y1A, y22));
-        const V dG = vfma(dy1, vadd(y1A, y1B), vfma(dp, vadd(cA, dc), vmul(pA, dc)));
-        // one logarithm per station, of the form its configuration needs
-        const V num = vsel(ratio, dE, dG);
-        const V den1 = vsel(ratio, vadd(vadd(V(2.0f), EA), vadd(EA, dE)), vfma(V(2.0f), GA, dG));
-        const V den2 = vsel(ratio, vadd(V(1.0f), EA), GA);
-        const V L = vlog2r(vmul(num, frcp(den1)), vfma(num, frcp(den2), V(1.0f)));
-        const V Q = vfma(vsel(ratio, omc, vneg(omc)), dLq, L);
-        v1 = vfma(KC(K_KQ1), Q, v1);
-        v2 = vfma(KC(K_KQ2), Q, v2);
-        v3 = vfma(KC(K_KQ3), Q, v3);
+        const V dE = vfma(KC(K_DC), iqB, vneg(vmul(cA, ndiq)));
+        const V EAB = vadd(vadd(EA, EA), dE);                           // E_A + E_B
+        const V sE = vmul(dE, frcp(vadd(V(2.0f), EAB)));
+        const V s2 = vmul(sE, sE);
+        V P = vfma(s2, V(1.0f / 11.0f), V(1.0f / 9.0f));
+        P = vfma(P, s2, V(1.0f / 7.0f));
+        P = vfma(P, s2, V(1.0f / 5.0f));
+        P = vfma(P, s2, V(1.0f / 3.0f));
+        const V dlam = vfma(vmul(vadd(sE, sE), s2), P, vneg(vmul(sE, EAB)));
+        const V dlnq = vmul(V(0.693147181f), dLq);
+        const V uA = vfma(aA, cot, vneg(y1A));                           // a cot β - y1 at A
+        const V du = vfma(da, cot, KN(K_DY1));
+        const V dW = vfma(du, iqB, vneg(vmul(uA, ndiq)));
+        V RQ = vfma(dE, m2B, vmul(EA, dm2));
+        RQ = vfma(cot, dlam, RQ);
+        RQ = vfma(omc, vfma(cot, dlnq, dW), RQ);
+        const V Qn = vfma(omc, dlnq, vadd(dlam, dE));
+        // μ at A and B, Δμ = -y2 (Δp - t Δy1)/(D_A D_B) with D = p - t y1 > 0
+        const V iDA = frcp(vfma(nt, y1A, pA)), iDB = frcp(vfma(nt, y1B, pB));
+        const V muA = vmul(y2, iDA), muB = vmul(y2, iDB);
+        const V dmu = vmul(vmul(vneg(y2), vfma(nt, KC(K_DY1), dp)), vmul(iDA, iDB));
+        const V dmm = vfma(dmu, m2B, vmul(muA, dm2));                   // Δ(μ m2)
+        // t μ³ A(t²μ²): an O(t) correction, differenced directly
+        auto cubic = [&](V mu) {
+            const V w = vmul(t, mu), u = vmul(w, w);
+            const V a = vfma(vfma(u, V(1.0f / 7.0f), V(-1.0f / 5.0f)), u, V(1.0f / 3.0f));
+            return vmul(vmul(w, vmul(mu, mu)), a);
+        };
+        const V omt2 = vfma(nt, t, V(1.0f));
+        const V G = vmul(omt2, vfma(omt2, vsub(dmm, vsub(cubic(muB), cubic(muA))), vmul(t, ndm1)));
+        v1 = vfma(KN(K_HB1), G, v1);
+        v2 = vfma(KC(K_HB2), G, v2);
+        v1 = vfma(KC(K_KR1), RQ, v1);
+        v2 = vfma(KC(K_KR2), RQ, v2);
+        v3 = vfma(KN(K_KR1), Qn, v3);
     }
     // back to EFCS: columns e1 = (c, s, 0), e2 = (s, -c, 0), e3 = (0, 0, -1); v3 is summed on
     // its own before it meets the running total (finer rounding than adding term by term)
     ue = vfma(c, v1, vfma(s, v2, ue));
     un = vfma(s, v1, vfma(KN(K_C), v2, un));
     uv = vsub(uv, v3);
+}
+
+// One pair, with the near-vertical evaluation for steep sides (a warp-uniform choice per side)
+template <class V, class K>
+AG_DEVICE_INLINE void side_pair(const K& k, V Xr, V Yr, V& ue, V& un, V& uv, bool steep) {
+    if (steep)
+        side_pair_t<true>(k, Xr, Yr, ue, un, uv);
+    else
+        side_pair_t<false>(k, Xr, Yr, ue, un, uv);
 }
 
 #undef KC

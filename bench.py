@@ -46,10 +46,11 @@ PRIORS = [(-1e4, 1e4), (-1e4, 1e4), (1e3, 1e4), (-50.0, 50.0), (100.0, 3000.0), 
 CDM_FLOP_PER_PAIR = 3019
 CDM_SFU_PER_SIDE = 13
 # near-vertical sides (|cot β| >= 3: ~9% of the sides of prior samples, none of the
-# workload's truth) also evaluate the cancellation-free log combination: extra FLOP and
+# workload's truth) take their own evaluation, which forms the O(β) remainders of the
+# terms with cot β and cot²β coefficients without cancellation: extra FLOP and
 # special-function operations per such side; the roofline counts the base figure only,
 # so its achieved rate is a lower bound for populations with steep sides
-CDM_STEEP_EXTRA = (45, 3)
+CDM_STEEP_EXTRA = (80, 3)
 L2_FLUSH_BYTES = 256 << 20
 
 

@@ -3,8 +3,8 @@
 tests/cdm_host/cdm_host.cpp builds altar_gb300/csrc/cdm_side.cuh with g++, the device
 intrinsics replaced by correctly rounded host operations.  Checked here:
   * the formulas against the FP64 oracle (models/cdm/cdm/libcdm.py restated in
-    oracle/cdm.py) on prior sources, with the same normwise tolerances the GPU tests use
-    for sources whose sides lie at least 10° from the vertical;
+    oracle/cdm.py) on prior sources, with one normwise tolerance for every source,
+    sources with near-vertical sides included;
   * the static FP32 operation count of one pair, which bench.py's roofline uses.
 """
 import ctypes
@@ -48,8 +48,7 @@ def test_flop_count_matches_bench_constant(host):
     flop, sfu, flop_s, sfu_s = (ctypes.c_long() for _ in range(4))
     host.cdm_host_side_counts(ctypes.byref(flop), ctypes.byref(sfu), ctypes.byref(flop_s), ctypes.byref(sfu_s))
     # 12 sides + per station: relative coordinates (6), LOS projection (5), residual (1),
-    # float-float w·r² accumulation (19); near-vertical sides add the cancellation-free
-    # log combination
+    # float-float w·r² accumulation (19); near-vertical sides take their own evaluation
     assert 12 * flop.value + 31 == bench.CDM_FLOP_PER_PAIR
     assert sfu.value == bench.CDM_SFU_PER_SIDE
     assert (flop_s.value - flop.value, sfu_s.value - sfu.value) == bench.CDM_STEEP_EXTRA
@@ -70,17 +69,16 @@ def test_side_arithmetic_against_oracle(host):
         flat.append(min_vertical_angle(th) >= 10.0)
     errs, flat = np.array(errs), np.array(flat)
     assert flat.sum() >= 16
-    assert np.all(errs[flat] <= 1e-4), errs[flat].max()
-    assert np.median(errs) <= 5e-6, np.median(errs)
-    # near-vertical sides: the error grows like cot β, not cot²β (cancellation-free logs)
-    cot = np.array([1.0 / np.tan(np.radians(min_vertical_angle(th))) for th in theta])
-    assert np.all(errs <= np.maximum(1e-4, 2e-5 * cot)), [(e, c) for e, c in zip(errs, cot) if e > max(1e-4, 2e-5 * c)]
+    # one tolerance whatever the angle of the sides (near-vertical sides included)
+    assert np.all(errs <= 3e-5), errs.max()
+    assert np.median(errs) <= 2e-6, np.median(errs)
 
 
-def test_steep_sides_without_cot2_amplification(host):
+def test_steep_sides_without_cot_amplification(host):
     """Sources with a side within 2° of the vertical (drawn from the priors): the error
-    stays within 2e-5 · cot β of the oracle, where the two-log form of the reference
-    formula loses up to cot²β · 2⁻²⁴ (0.2 at 0.03°)."""
+    stays within 2e-5 of the oracle, as for any other source.  Evaluated term by term,
+    the coefficients of order cot β and cot²β turn FP32 rounding into errors up to
+    cot²β · 2⁻²⁴ (0.2 at 0.03°); with the logarithms combined it was still ~7e-6 · cot β."""
     g = np.linspace(-20e3, 20e3, 30)
     X, Y = [np.ascontiguousarray(a.ravel()) for a in np.meshgrid(g, g)]
     los = np.ascontiguousarray(np.tile(LOS, (X.size, 1)))
@@ -92,8 +90,7 @@ def test_steep_sides_without_cot2_amplification(host):
         t = np.ascontiguousarray(th, dtype=np.float64)
         assert host.cdm_host_los(_dp(t), X.size, _dp(X), _dp(Y), _dp(los), 0.25, _dp(out)) == 0
         err = np.max(np.abs(out - ref)) / np.max(np.abs(ref))
-        cot = 1.0 / np.tan(np.radians(min_vertical_angle(th)))
-        assert err <= 2e-5 * cot, (min_vertical_angle(th), err)
+        assert err <= 2e-5, (min_vertical_angle(th), err)
 
 
 def test_exactly_vertical_sides(host):

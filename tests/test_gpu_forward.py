@@ -1,15 +1,14 @@
 """Forward models + misfit on the GPU against the oracle and the reference fixtures.
 
 Tolerances (FP32 device arithmetic against FP64 references):
-  * CDM LOS displacement, per source, normwise: |u_gpu - u_ref|_inf <= tol * |u_ref|_inf
-    with tol = max(TOL_CDM, K_STEEP · |cot β_min|), β_min the smallest angle between a
-    side and the vertical.  Near-vertical sides are ill-conditioned in the
-    angular-dislocation formula itself: its coefficients grow like cot²β.  The kernel
-    evaluates the log combination those coefficients multiply without cancellation, which
-    leaves an FP32 error growing like cot β (measured below 7e-6 · cot β over 300+ prior
-    sources in a host build of the same arithmetic); K_STEEP = 2e-5 gives 1e-4 at 11°,
-    5.7e-4 at 2°, 5.7e-3 at 0.2°.  The median error over sources must stay below
-    TOL_CDM_MEDIAN.
+  * CDM LOS displacement, per source, normwise: |u_gpu - u_ref|_inf <= TOL_CDM * |u_ref|_inf
+    for every source, whatever the angle of its sides.  Near-vertical sides are
+    ill-conditioned in the angular-dislocation formula itself (coefficients of order
+    cot β and cot²β multiplying O(β) combinations); the kernel evaluates them from
+    cancellation-free remainders, so their FP32 error no longer grows with cot β (host
+    build of the same arithmetic, 2000 prior sources: all within 1e-5 when a side is within
+    18° of the vertical, 99.5% of all sources within 1e-5).  The median error over sources
+    must stay below TOL_CDM_MEDIAN, and most sources within 1e-5 (CDM_FRAC_1E5).
   * Mogi LOS displacement: normwise 1e-5.
   * log-likelihood given the device's own FP32 residuals: 1e-9 relative (FP64 oracle sum).
 """
@@ -29,13 +28,7 @@ pytestmark = pytest.mark.gpu
 
 TOL_CDM = 1e-4
 TOL_CDM_MEDIAN = 5e-6
-K_STEEP = 2e-5
-
-
-def tol_cdm(th):
-    """Normwise tolerance of a source by the smallest angle between its sides and the vertical."""
-    a = np.radians(min_vertical_angle(th))
-    return max(TOL_CDM, K_STEEP / np.tan(a))
+CDM_FRAC_1E5 = 0.95
 G = np.load(os.path.join(os.path.dirname(__file__), "golden", "cdm_golden.npz"))
 
 
@@ -65,7 +58,7 @@ def test_cdm_matches_reference_fixtures(cuda):
     for k, u in enumerate(G["ref_u"]):
         ref = u[0] * LOS[0] + u[1] * LOS[1] + u[2] * LOS[2]
         err = np.max(np.abs(res[k] - ref)) / np.max(np.abs(ref))
-        assert err <= tol_cdm(theta[k]), (k, err)
+        assert err <= TOL_CDM, (k, err)
         errs.append(err)
     assert np.median(errs) <= TOL_CDM_MEDIAN
 
@@ -80,9 +73,8 @@ def test_cdm_matlab_goldens(cuda):
         strat, _ = cdm_strategy(X, Y, np.tile(los, (12, 1)), np.zeros(12), np.ones(12))
         _, res = _residuals(strat, th, 12)
         ref = G[comp] * 1e3                                 # displacement scales with length
-        # the Matlab source's body z axis is ~9° from the vertical: near-vertical class
-        assert np.max(np.abs(res[0] - ref)) <= tol_cdm(th[0]) * np.max(np.abs(ref)), comp
-        assert np.max(np.abs(res[0] - ref)) <= 1e-4 * np.max(np.abs(ref)), comp
+        # the Matlab source's body z axis is ~9° from the vertical: near-vertical sides
+        assert np.max(np.abs(res[0] - ref)) <= TOL_CDM * np.max(np.abs(ref)), comp
 
 
 def test_cdm_prior_sources_workload_grid(cuda):
@@ -96,11 +88,12 @@ def test_cdm_prior_sources_workload_grid(cuda):
     strat, _ = cdm_strategy(X, Y, los, np.zeros(X.size), np.full(X.size, 9e-6))
     _, res = _residuals(strat, theta, X.size)
     errs = np.max(np.abs(res - ref), 1) / np.max(np.abs(ref), 1)
-    tol = np.array([tol_cdm(t) for t in theta])
-    assert np.all(errs <= tol), [(e, t) for e, t in zip(errs, tol) if e > t]
-    assert np.median(errs) <= TOL_CDM_MEDIAN
     ang = np.array([min_vertical_angle(t) for t in theta])
-    print(f"\nCDM normwise error over {len(theta)} prior sources: median {np.median(errs):.2e}")
+    assert np.all(errs <= TOL_CDM), [(e, a) for e, a in zip(errs, ang) if e > TOL_CDM]
+    assert np.median(errs) <= TOL_CDM_MEDIAN
+    assert np.mean(errs <= 1e-5) >= CDM_FRAC_1E5, np.mean(errs <= 1e-5)
+    print(f"\nCDM normwise error over {len(theta)} prior sources: median {np.median(errs):.2e}, "
+          f"within 1e-5: {np.mean(errs <= 1e-5):.1%}")
     for lo, hi in ((10, 91), (5, 10), (2, 5), (0, 2)):
         s = (ang >= lo) & (ang < hi)
         if s.any():
