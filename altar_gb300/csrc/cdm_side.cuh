@@ -33,10 +33,10 @@ constexpr int kSides = 12;
 // Near-vertical ("steep") sides, |cot β| >= kSteepCot: several coefficients grow
 // like cot β and cot²β while the combinations they multiply are O(β); evaluated
 // term by term they cancel and FP32 rounding (of the terms and of the side
-// constants) is amplified by cot β.  These sides take their own evaluation
-// (side_pair with Steep = true): the ratio configuration at every station, and the
-// cancelling groups rewritten as two remainders computed without cancellation,
-// with O(1) coefficients (derivation at side_pair_t).
+// constants) is amplified by up to cot²β.  These sides take their own evaluation
+// (side_pair_t with Steep = true): the ratio configuration at every station, and the
+// cancelling groups rewritten as remainders computed without cancellation, with
+// O(1) coefficients (derivation in side_pair_t).
 struct __align__(16) SideC {
     float4 q[12];
 };
