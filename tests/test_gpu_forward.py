@@ -8,7 +8,9 @@ Tolerances (FP32 device arithmetic against FP64 references):
     cancellation-free remainders, so their FP32 error no longer grows with cot β (host
     build of the same arithmetic, 2000 prior sources: all within 1e-5 when a side is within
     18° of the vertical, 99.5% of all sources within 1e-5).  The median error over sources
-    must stay below TOL_CDM_MEDIAN, and most sources within 1e-5 (CDM_FRAC_1E5).
+    must stay below TOL_CDM_MEDIAN, and most sources within 1e-5 (CDM_FRAC_1E5).  The
+    300 prior sources of the workload-grid test are held to TOL_CDM_GRID (measured on a
+    GB300: max 1.4e-5, 99.3% within 1e-5).
   * Mogi LOS displacement: normwise 1e-5.
   * log-likelihood given the device's own FP32 residuals: 1e-9 relative (FP64 oracle sum).
 """
@@ -27,8 +29,9 @@ from gpu_helpers import (LOS, cdm_los_oracle, cdm_prior_rows, cdm_strategy, dev,
 pytestmark = pytest.mark.gpu
 
 TOL_CDM = 1e-4
+TOL_CDM_GRID = 3e-5
 TOL_CDM_MEDIAN = 5e-6
-CDM_FRAC_1E5 = 0.95
+CDM_FRAC_1E5 = 0.98
 G = np.load(os.path.join(os.path.dirname(__file__), "golden", "cdm_golden.npz"))
 
 
@@ -89,7 +92,7 @@ def test_cdm_prior_sources_workload_grid(cuda):
     _, res = _residuals(strat, theta, X.size)
     errs = np.max(np.abs(res - ref), 1) / np.max(np.abs(ref), 1)
     ang = np.array([min_vertical_angle(t) for t in theta])
-    assert np.all(errs <= TOL_CDM), [(e, a) for e, a in zip(errs, ang) if e > TOL_CDM]
+    assert np.all(errs <= TOL_CDM_GRID), [(e, a) for e, a in zip(errs, ang) if e > TOL_CDM_GRID]
     assert np.median(errs) <= TOL_CDM_MEDIAN
     assert np.mean(errs <= 1e-5) >= CDM_FRAC_1E5, np.mean(errs <= 1e-5)
     print(f"\nCDM normwise error over {len(theta)} prior sources: median {np.median(errs):.2e}, "
