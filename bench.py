@@ -569,7 +569,7 @@ def run_ours(args):
             for kind in kinds:
                 out[f"{kind}_s{seed}"] = anneal(kind, X, Y, los, d, N, rank, args, seed=seed)
         if args.ref_walk_steps:
-            # a longer plain walk per stage: the better-mixed posterior both samplers are judged by
+            # a longer plain walk per stage: the better-mixed posterior both samplers are compared with
             steps5 = args.walk_steps
             args.walk_steps = args.ref_walk_steps
             for seed in args.seeds:
