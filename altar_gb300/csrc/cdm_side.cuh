@@ -204,41 +204,39 @@ AG_CDM_FN bool cdm_corners(const double* th, const Layout& L, Vec3 V[3][4]) {
     return above;
 }
 
-// Does rectangle r take part (libcdm.py:226-242: a zero semi-axis leaves only the
-// rectangle spanned by the other two)
-AG_CDM_FN bool cdm_rectangle_used(double ax, double ay, double az, int r) {
-    if (ax == 0.0 && ay == 0.0 && az == 0.0) return false;
-    if (ax == 0.0 && ay != 0.0 && az != 0.0) return r == 0;
-    if (ax != 0.0 && ay == 0.0 && az != 0.0) return r == 1;
-    if (ax != 0.0 && ay != 0.0 && az == 0.0) return r == 2;
-    return true;
-}
-
-// Constants of side e of rectangle r of a chain whose corners V lie below the surface
-template <class Layout>
-AG_CDM_FN void cdm_one_side(const double* th, const Layout& L, const Vec3 V[3][4], double x0, double y0,
-                            int r, int e, SideC& side, bool& act, bool& steep) {
-    act = steep = false;
-    if (!cdm_rectangle_used(th[L.axes_idx], th[L.axes_idx + 1], th[L.axes_idx + 2], r)) return;
-    // slip: the opening along the rectangle's unit normal
-    Vec3 nrm = v_cross(v_sub(V[r][1], V[r][0]), v_sub(V[r][3], V[r][0]));
-    nrm = v_scale(nrm, 1.0 / sqrt(v_dot(nrm, nrm)));
-    const Vec3 b = v_scale(nrm, th[L.strength_idx]);
-    fill_side(side, V[r][e], V[r][(e + 1) & 3], b, L.nu, x0, y0, act, steep);
-}
-
 // Constants of the active sides of a chain whose corners V lie below the surface;
 // returns the mask of active sides (bit 4r + e: side e of rectangle r) and of the
 // steep ones among them (bit 12 + 4r + e)
 template <class Layout>
 AG_CDM_FN uint32_t cdm_sides(const double* th, const Layout& L, const Vec3 V[3][4], double x0, double y0,
                              SideC* side) {
+    // which rectangles take part (libcdm.py:226-242)
+    const double ax = th[L.axes_idx], ay = th[L.axes_idx + 1], az = th[L.axes_idx + 2];
+    bool use[3];
+    if (ax == 0.0 && ay == 0.0 && az == 0.0) {
+        use[0] = use[1] = use[2] = false;
+    } else if (ax == 0.0 && ay != 0.0 && az != 0.0) {
+        use[0] = true; use[1] = use[2] = false;
+    } else if (ax != 0.0 && ay == 0.0 && az != 0.0) {
+        use[1] = true; use[0] = use[2] = false;
+    } else if (ax != 0.0 && ay != 0.0 && az == 0.0) {
+        use[2] = true; use[0] = use[1] = false;
+    } else {
+        use[0] = use[1] = use[2] = true;
+    }
+    const double opening = th[L.strength_idx];
     uint32_t mask = 0u;
-    for (int k = 0; k < kSides; ++k) {
-        bool act, steep;
-        cdm_one_side(th, L, V, x0, y0, k / 4, k % 4, side[k], act, steep);
-        if (act) mask |= 1u << k;
-        if (act && steep) mask |= 1u << (kSides + k);
+    for (int r = 0; r < 3; ++r) {
+        if (!use[r]) continue;
+        Vec3 nrm = v_cross(v_sub(V[r][1], V[r][0]), v_sub(V[r][3], V[r][0]));
+        nrm = v_scale(nrm, 1.0 / sqrt(v_dot(nrm, nrm)));
+        Vec3 b = v_scale(nrm, opening);
+        for (int e = 0; e < 4; ++e) {
+            bool act, steep;
+            fill_side(side[r * 4 + e], V[r][e], V[r][(e + 1) & 3], b, L.nu, x0, y0, act, steep);
+            if (act) mask |= 1u << (r * 4 + e);
+            if (act && steep) mask |= 1u << (kSides + r * 4 + e);
+        }
     }
     return mask;
 }

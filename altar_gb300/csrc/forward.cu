@@ -51,56 +51,44 @@ struct __align__(16) ChainC {
 };
 static_assert(sizeof(ChainC) % 16 == 0, "ChainC must be a whole number of float4");
 
-// Sixteen lanes per requested chain (all n, or the first *count_in of index_in), one per
-// rectangle side (lanes 12-15 only write per-dataset offsets): the FP64 set-up of a chain is
-// latency-bound, and twelve sides in parallel hide it.  Chains that are masked or lie above the
-// free surface get their status and nothing else; every other chain takes the next compacted
-// slot (slot order is the order of the atomic, which does not affect any chain's result) and
-// writes its constants there, so the likelihood kernel's CTAs hold only chains with work.
-constexpr int kSetupLanes = 16;
-static_assert(kMaxOffsets == kSetupLanes && kSides <= kSetupLanes, "one lane per side and per offset");
-
-__global__ void __launch_bounds__(128)
-cdm_setup_kernel(ag_layout L, const double* __restrict__ theta, int n, const uint32_t* __restrict__ mask_in,
-                 ChainC* __restrict__ out, uint32_t* __restrict__ chain_status, int noffsets,
-                 const int32_t* __restrict__ index_in, const int32_t* __restrict__ count_in,
-                 int32_t* __restrict__ index_out, int32_t* __restrict__ count_out) {
-    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    const int g = (int)(t / kSetupLanes), r = (int)(t % kSetupLanes);
-    const int lead = threadIdx.x & 16;                     // this group's first lane in the warp
-    const unsigned gmask = 0xFFFFu << lead;
-    // every early return below is taken by the whole group of sixteen lanes
-    if (g >= n) return;
-    int i = g;
+// One thread per requested chain (all n, or the first *count_in of index_in).  Chains that
+// are masked or lie above the free surface get their status and nothing else; every other
+// chain takes the next compacted slot (slot order is the order of the atomic, which does not
+// affect any chain's result) and writes its constants there, so the likelihood kernel's CTAs
+// hold only chains with work.
+__global__ void cdm_setup_kernel(ag_layout L, const double* __restrict__ theta, int n,
+                                 const uint32_t* __restrict__ mask_in, ChainC* __restrict__ out,
+                                 uint32_t* __restrict__ chain_status, int noffsets,
+                                 const int32_t* __restrict__ index_in, const int32_t* __restrict__ count_in,
+                                 int32_t* __restrict__ index_out, int32_t* __restrict__ count_out) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    int i = t;
     if (index_in) {
-        if (g >= *count_in) return;
-        i = index_in[g];
+        if (t >= *count_in) return;
+        i = index_in[t];
     }
     if (mask_in && mask_in[i]) return;
     const double* th = theta + (size_t)i * L.nparams;
     Vec3 V[3][4];
-    if (cdm_corners(th, L, V)) {
-        if (r == 0 && chain_status) chain_status[i] |= CHAIN_ABOVE_SURFACE;
+    const bool above = cdm_corners(th, L, V);
+    if (above) {
+        if (chain_status) chain_status[i] |= CHAIN_ABOVE_SURFACE;
         return;
     }
-    int slot = 0;
-    if (r == 0) slot = atomicAdd(count_out, 1);
-    slot = __shfl_sync(gmask, slot, lead);
+    const int slot = atomicAdd(count_out, 1);
+    index_out[slot] = i;
     ChainC& C = out[slot];
+    C.side_mask = 0u;
+    C.status = 0u;
     const double x0 = th[L.x_idx], y0 = th[L.x_idx + 1];
-    bool act = false, steep = false;
-    if (r < kSides) cdm_one_side(th, L, V, x0, y0, r / 4, r % 4, C.side[r], act, steep);
-    const uint32_t active = (__ballot_sync(gmask, act) >> lead) & 0x0FFFu;
-    const uint32_t steep_sides = (__ballot_sync(gmask, act && steep) >> lead) & 0x0FFFu;
-    C.off[r] = (r < noffsets) ? (float)th[L.offset_idx + r] : 0.f;
-    if (r == 0) {
-        index_out[slot] = i;
-        C.status = 0u;
-        split_hilo(x0, C.hdr.x, C.hdr.y);
-        split_hilo(y0, C.hdr.z, C.hdr.w);
-        // a chain with no active side still needs a llk: bit 31 marks "evaluate"
-        C.side_mask = active | (steep_sides << kSides) | 0x80000000u;
-    }
+    split_hilo(x0, C.hdr.x, C.hdr.y);
+    split_hilo(y0, C.hdr.z, C.hdr.w);
+    for (int k = 0; k < kMaxOffsets; ++k)
+        C.off[k] = (k < noffsets) ? (float)th[L.offset_idx + k] : 0.f;
+    const uint32_t mask = cdm_sides(th, L, V, x0, y0, C.side);
+    // a chain with no active side still needs a llk: keep bit 31 as "evaluate"
+    C.side_mask = mask | 0x80000000u;
 }
 
 __global__ void cdm_check_kernel(ag_layout L, const double* __restrict__ theta, int n,
@@ -436,8 +424,7 @@ static int forward_llk(int model, const ag_layout* layout, const double* theta, 
                                                      al256((size_t)n * sizeof(int32_t)));
         rc = cuda_status(cudaMemsetAsync(nslots, 0, sizeof(int32_t), s), "cudaMemsetAsync(slot count)");
         if (rc) return rc;
-        cdm_setup_kernel<<<(int)(((long)n * kSetupLanes + 127) / 128), 128, 0, s>>>(L, theta, n, mask_in, chains,
-                                                                              chain_status, noffsets,
+        cdm_setup_kernel<<<(n + 127) / 128, 128, 0, s>>>(L, theta, n, mask_in, chains, chain_status, noffsets,
                                                          index, count, slot_chain, nslots);
         rc = launch_status("cdm_setup_kernel");
         if (rc) return rc;
