@@ -30,7 +30,7 @@ import numpy as np
 import torch
 
 from .. import _native
-from ..device import DEVICE, ptr, stream_handle, workspace
+from ..device import DEVICE, ptr, stream_handle
 from .metropolis import Metropolis
 
 

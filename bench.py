@@ -22,7 +22,6 @@ import statistics
 import subprocess
 import sys
 import tempfile
-import threading
 import time
 
 import numpy as np
@@ -546,7 +545,6 @@ def run_ours(args):
     rank, world, local, dist = dist_setup()
     torch.cuda.set_device(local)
     from altar_gb300 import Application, _native
-    from altar_gb300.device import ptr, stream_handle
     from altar_gb300.distributions import Uniform
     from altar_gb300.models import CDM, Contiguous
     from altar_gb300.models.observations import Observations

@@ -21,7 +21,7 @@ import pytest
 import torch
 
 from altar_gb300 import _native
-from oracle import catmip, cdm
+from oracle import catmip
 
 from gpu_helpers import (LOS, cdm_los_oracle, cdm_prior_rows, cdm_strategy, dev, min_vertical_angle,
                          mogi_strategy)

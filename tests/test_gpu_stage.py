@@ -4,7 +4,6 @@ Exactness: resampling counts and row order are bit-exact for identical weights
 and uniforms; proposals, covariance and the β schedule agree to FP64
 round-off (1e-12 relative); the initial prior sample to one ulp.
 """
-import ctypes
 
 import numpy as np
 import pytest
