@@ -132,6 +132,7 @@ _SIGNATURES = {
     "ag_forward_variants": (c_int32, [c_int]),
     "ag_forward_llk": (c_int, [c_int, P, P, c_int32, P, c_double, P, P, P, P, P, c_size_t, P]),
     "ag_cdm_check": (c_int, [P, P, c_int32, P, P]),
+    "ag_cdm_work": (c_int, [P, P, c_int32, P, P, P]),
     "ag_forward_llk_subset": (c_int, [c_int, P, P, c_int32, P, c_double, P, P, P, P, P, P, c_size_t, P]),
     "ag_linear_kpad": (c_int32, [c_int32]),
     "ag_linear_prepare": (c_int, [P, c_int32, c_int32, P, P]),

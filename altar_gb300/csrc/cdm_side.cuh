@@ -7,9 +7,16 @@
 // Reference: models/cdm/cdm/libcdm.py:174-242 (corners, active rectangles),
 // libcdm.py:310-372 (angular-dislocation pair of one side, artefact-free
 // configurations I and II), libcdm.py:375-430 (AngDisDisp terms).
+//
+// A rectangle far from the free surface compared with its size is evaluated
+// instead as the integral of point tensile dislocations over its area
+// (Gauss-Legendre product rule, QuadC below): the same field without the
+// cancellation between its four sides.
 #pragma once
 #include <math.h>
 #include <stdint.h>
+
+#include "gauss_legendre.cuh"
 
 #ifndef AG_DEVICE_INLINE
 #define AG_DEVICE_INLINE __device__ __forceinline__
@@ -79,22 +86,30 @@ AG_CDM_FN void split_hilo(double v, float& hi, float& lo) {
     lo = (float)(v - (double)hi);
 }
 
-AG_CDM_FN void fill_side(SideC& S, Vec3 pa, Vec3 pb, Vec3 bvec, double nu, double x0, double y0,
-                         bool& active, bool& steep) {
+// Whether a side takes part and whether it is near-vertical.  Vertical sides contribute
+// nothing (libcdm.py:320-324: |β| or |π - β| below the double epsilon, i.e. cos β = ±1
+// exactly; acos of the next double below 1 is already 1.5e-8).
+AG_CDM_FN void side_class(Vec3 pa, Vec3 pb, bool& active, bool& steep) {
+    const Vec3 side = v_sub(pb, pa);
+    const double L = sqrt(v_dot(side, side));
+    const double iL = 1.0 / L;
+    const double cb = -side.z * iL;
+    active = (L > 0.0) && (fabs(cb) < 1.0);
+    steep = false;
+    if (active) {
+        const double sb = sqrt(side.x * side.x + side.y * side.y) * iL;
+        steep = fabs(cb * (1.0 / sb)) >= kSteepCot;
+    }
+}
+
+// Constants of an active side (side_class: active); steep selects the near-vertical set
+AG_CDM_FN void fill_side(SideC& S, Vec3 pa, Vec3 pb, Vec3 bvec, double nu, double x0, double y0, bool steep) {
     const double PI = 3.14159265358979323846;
     const double LN2 = 0.69314718055994530942;
     Vec3 side = v_sub(pb, pa);
     double L = sqrt(v_dot(side, side));
     const double iL = 1.0 / L;
     double cb = -side.z * iL;                        // cos β, β in [0, π]
-    // vertical sides contribute nothing (libcdm.py:320-324: |β| or |π - β| below the double
-    // epsilon, i.e. cos β = ±1 exactly; acos of the next double below 1 is already 1.5e-8)
-    steep = false;
-    if (!(L > 0.0) || !(fabs(cb) < 1.0)) {
-        active = false;
-        return;
-    }
-    active = true;
     double hl = sqrt(side.x * side.x + side.y * side.y);
     const double ihl = 1.0 / hl;
     double c = side.x * ihl, s = side.y * ihl;       // e1 = (c, s, 0), e2 = (s, -c, 0)
@@ -145,7 +160,6 @@ AG_CDM_FN void fill_side(SideC& S, Vec3 pa, Vec3 pb, Vec3 bvec, double nu, doubl
     S.q[9] = make_float4((float)(dy1 * cb + da * sb), (float)(dy1 * sb - da * cb), (float)(LN2 * kc2), (float)omc);
     S.q[10] = make_float4(0.f, 0.f, 0.f, 0.f);
     S.q[11] = make_float4(0.f, 0.f, 0.f, 0.f);
-    steep = fabs(cot) >= kSteepCot;
     if (steep) {
         // ratio configuration: β' = β if cos β > 0, β - π otherwise; t = tan(β'/2)
         const double t = (cb > 0.0) ? tb2 : -ctb2;
@@ -204,13 +218,59 @@ AG_CDM_FN bool cdm_corners(const double* th, const Layout& L, Vec3 V[3][4]) {
     return above;
 }
 
-// Constants of the active sides of a chain whose corners V lie below the surface;
-// returns the mask of active sides (bit 4r + e: side e of rectangle r) and of the
-// steep ones among them (bit 12 + 4r + e)
+// ---------------------------------------------------------------------------
+// Far-field rectangles: quadrature of point tensile dislocations.
+//
+// A rectangle of uniform opening is the superposition of point tensile dislocations
+// over its area, each with the half-space surface displacement of Okada (1985, BSSA
+// 75(4), point source, tensile component): in the strike frame of the plane (x along
+// strike, the plane dipping by δ towards -y), for a point at depth d and a station at
+// horizontal offset (x, y),
+//     R² = x² + y² + d²,  q = y sin δ - d cos δ,  k = 1 - 2ν,
+//     I1 = k y [1/(R(R+d)²) - x²(3R+d)/(R³(R+d)³)],  I2 = the same with x and y swapped,
+//     I3 = k x/R³ - I2,  I5 = k [1/(R(R+d)) - x²(2R+d)/(R³(R+d)²)],
+//     (ux, uy, uz) = P/(2π) (3x q²/R⁵ - I3 sin²δ, 3y q²/R⁵ - I1 sin²δ, 3d q²/R⁵ - I5 sin²δ)
+// for potency P (opening × area).  (Its sign convention agrees with the angular-dislocation
+// rectangles of libcdm.py:250-273, of which it is the limit for a vanishing rectangle;
+// checked in the CPU tests.)  q is the same for every point of the plane.
+//
+// The rectangle's field is the integral of that kernel over the rectangle, taken with an
+// n1 × n2 Gauss-Legendre product rule.  The integrand is analytic in each coordinate; its
+// singularities lie where the station-to-point distance vanishes, at least D (the depth of
+// the rectangle's shallowest corner) from every point of the rectangle, so the error of
+// an n-point rule along a side of half-length h falls like ρ^(-2n), ρ = D/h + sqrt((D/h)² + 1)
+// (the Bernstein ellipse through the nearest singularity).  Each direction gets the
+// smallest n with ρ^(-2n) <= kQuadTol; the rectangle is integrated when n1 n2 <= kQuadBudget
+// (its four sides cost about as much as 20 nodes) and evaluated by its sides otherwise (a
+// rectangle close to the surface, where its sides do not cancel much).  The nodes are
+// summed in FP32 without cancellation: for a rectangle whose distance from the stations is
+// many times its size, the FP32 sum of its four sides loses the factor distance/size in
+// accuracy, the quadrature does not.
+constexpr double kQuadTol = 1e-7;
+constexpr int kQuadBudget = 32;
+constexpr int kQuadMaxNodes = 46;
+
+struct __align__(16) QuadC {
+    float4 h0;                    // strike direction (a, b) = (cos, sin), sin δ, q offset Q0
+    float4 h1;                    // -k sin²δ, node count (integer bits), 0, 0
+    float4 node[kQuadMaxNodes];   // x, y (strike frame, relative to the source centre), depth, weight
+};
+static_assert(sizeof(QuadC) <= 4 * sizeof(SideC), "a rectangle's quadrature block overlays its four sides");
+static_assert(kQuadBudget <= kQuadMaxNodes, "quadrature node budget");
+
+// smallest n with ρ^(-2n) <= kQuadTol, ρ = δ + sqrt(δ² + 1), δ = distance / half-length
+AG_CDM_FN int quad_points(double delta) {
+    const double rho = delta + sqrt(delta * delta + 1.0);
+    const double n = ceil(log(1.0 / kQuadTol) / (2.0 * log(rho)));
+    return (n < 1.0) ? 1 : (n > (double)kGaussMax ? kGaussMax + 1 : (int)n);
+}
+
+// Per-chain plan shared by the set-up kernel and the work count: bits 0-11 sides evaluated
+// as angular-dislocation pairs, 12-23 which of them are near-vertical, 24-26 rectangles
+// integrated by quadrature (their node counts in nq).  Rectangles that take part follow
+// libcdm.py:226-242 (a zero semi-axis leaves only the rectangle spanned by the other two).
 template <class Layout>
-AG_CDM_FN uint32_t cdm_sides(const double* th, const Layout& L, const Vec3 V[3][4], double x0, double y0,
-                             SideC* side) {
-    // which rectangles take part (libcdm.py:226-242)
+AG_CDM_FN uint32_t cdm_plan(const double* th, const Layout& L, const Vec3 V[3][4], int nq[3][2]) {
     const double ax = th[L.axes_idx], ay = th[L.axes_idx + 1], az = th[L.axes_idx + 2];
     bool use[3];
     if (ax == 0.0 && ay == 0.0 && az == 0.0) {
@@ -224,21 +284,118 @@ AG_CDM_FN uint32_t cdm_sides(const double* th, const Layout& L, const Vec3 V[3][
     } else {
         use[0] = use[1] = use[2] = true;
     }
-    const double opening = th[L.strength_idx];
     uint32_t mask = 0u;
     for (int r = 0; r < 3; ++r) {
+        nq[r][0] = nq[r][1] = 0;
         if (!use[r]) continue;
-        Vec3 nrm = v_cross(v_sub(V[r][1], V[r][0]), v_sub(V[r][3], V[r][0]));
-        nrm = v_scale(nrm, 1.0 / sqrt(v_dot(nrm, nrm)));
-        Vec3 b = v_scale(nrm, opening);
+        const Vec3 e1 = v_sub(V[r][1], V[r][0]), e2 = v_sub(V[r][3], V[r][0]);
+        const double h1 = 0.5 * sqrt(v_dot(e1, e1)), h2 = 0.5 * sqrt(v_dot(e2, e2));
+        double D = -V[r][0].z;
+        for (int e = 1; e < 4; ++e) D = fmin(D, -V[r][e].z);
+        if (h1 > 0.0 && h2 > 0.0 && D > 0.0) {
+            const int n1 = quad_points(D / h1), n2 = quad_points(D / h2);
+            if (n1 <= kGaussMax && n2 <= kGaussMax && n1 * n2 <= kQuadBudget) {
+                nq[r][0] = n1;
+                nq[r][1] = n2;
+                mask |= 1u << (24 + r);
+                continue;
+            }
+        }
         for (int e = 0; e < 4; ++e) {
             bool act, steep;
-            fill_side(side[r * 4 + e], V[r][e], V[r][(e + 1) & 3], b, L.nu, x0, y0, act, steep);
+            side_class(V[r][e], V[r][(e + 1) & 3], act, steep);
             if (act) mask |= 1u << (r * 4 + e);
             if (act && steep) mask |= 1u << (kSides + r * 4 + e);
         }
     }
     return mask;
+}
+
+// Quadrature constants of rectangle P1..P4 (P2 - P1 and P4 - P1 its edges) for n1 × n2 nodes
+AG_CDM_FN void fill_quad(QuadC& Q, const Vec3 P[4], double opening, double nu, double x0, double y0, int n1,
+                         int n2) {
+    const double PI = 3.14159265358979323846;
+    const Vec3 e1 = v_sub(P[1], P[0]), e2 = v_sub(P[3], P[0]);
+    Vec3 nrm = v_cross(e1, e2);
+    const double area = sqrt(v_dot(nrm, nrm));
+    nrm = v_scale(nrm, 1.0 / area);
+    if (nrm.z < 0.0) nrm = v_scale(nrm, -1.0);      // the field does not depend on the normal's sense
+    const double sd = sqrt(nrm.x * nrm.x + nrm.y * nrm.y), cd = nrm.z;
+    // strike (a, b): horizontal, perpendicular to the normal's horizontal part, with the
+    // plane dipping towards -y of the strike frame (y = (-b, a))
+    double a = 1.0, b = 0.0;
+    if (sd > 0.0) {
+        a = -nrm.y / sd;
+        b = nrm.x / sd;
+    }
+    const Vec3 c = v_add(P[0], v_scale(v_add(e1, e2), 0.5));
+    const double yc = -b * (c.x - x0) + a * (c.y - y0);
+    Q.h0 = make_float4((float)a, (float)b, (float)sd, (float)(yc * sd + (-c.z) * cd));
+    Q.h1 = make_float4((float)(-(1.0 - 2.0 * nu) * sd * sd), __int_as_float(n1 * n2), 0.f, 0.f);
+    const double scale = 0.25 * area * opening / (2.0 * PI);
+    int k = 0;
+    for (int i = 0; i < n1; ++i) {
+        const double s = kGaussX[gauss_offset(n1) + i], ws = kGaussW[gauss_offset(n1) + i];
+        for (int j = 0; j < n2; ++j) {
+            const double t = kGaussX[gauss_offset(n2) + j], wt = kGaussW[gauss_offset(n2) + j];
+            const Vec3 xi = v_add(P[0], v_add(v_scale(e1, 0.5 * (1.0 + s)), v_scale(e2, 0.5 * (1.0 + t))));
+            const double dx = xi.x - x0, dy = xi.y - y0;
+            Q.node[k++] = make_float4((float)(a * dx + b * dy), (float)(-b * dx + a * dy), (float)(-xi.z),
+                                      (float)(ws * wt * scale));
+        }
+    }
+    for (; k < kQuadMaxNodes; ++k) Q.node[k] = make_float4(0.f, 0.f, 1.f, 0.f);
+}
+
+// Constants of a chain whose corners V lie below the surface, following the plan: the
+// active sides of the rectangles evaluated by their sides, the nodes of the others (a
+// QuadC in place of the rectangle's four SideC).  Returns the plan's mask.
+template <class Layout>
+AG_CDM_FN uint32_t cdm_sides(const double* th, const Layout& L, const Vec3 V[3][4], double x0, double y0,
+                             SideC* side) {
+    int nq[3][2];
+    const uint32_t mask = cdm_plan(th, L, V, nq);
+    const double opening = th[L.strength_idx];
+    for (int r = 0; r < 3; ++r) {
+        if (mask >> (24 + r) & 1u) {
+            fill_quad(*reinterpret_cast<QuadC*>(&side[r * 4]), V[r], opening, L.nu, x0, y0, nq[r][0], nq[r][1]);
+            continue;
+        }
+        if (!(mask >> (4 * r) & 0xFu)) continue;
+        Vec3 nrm = v_cross(v_sub(V[r][1], V[r][0]), v_sub(V[r][3], V[r][0]));
+        nrm = v_scale(nrm, 1.0 / sqrt(v_dot(nrm, nrm)));
+        const Vec3 b = v_scale(nrm, opening);
+        for (int e = 0; e < 4; ++e)
+            if (mask >> (r * 4 + e) & 1u)
+                fill_side(side[r * 4 + e], V[r][e], V[r][(e + 1) & 3], b, L.nu, x0, y0,
+                          (mask >> (kSides + r * 4 + e)) & 1u);
+    }
+    return mask;
+}
+
+// FP32 work per station of a chain with this plan (FMA = 2): the counts of the pair and
+// quadrature code below, checked against a counting evaluation in the CPU tests
+constexpr int kFlopSide = 251;          // one angular-dislocation pair
+constexpr int kFlopSteepExtra = 78;     // near-vertical pair: remainders of the cot β terms
+constexpr int kFlopQuadRect = 19;       // quadrature rectangle: strike frame, q, back to EFCS
+constexpr int kFlopQuadNode = 48;       // one point tensile dislocation, weighted sum
+constexpr int kFlopStation = 31;        // coordinates, LOS projection, residual, float-float misfit
+constexpr int kSfuSide = 13, kSfuSteepExtra = 3, kSfuQuadNode = 2;
+AG_CDM_FN void cdm_work(uint32_t mask, const int nq[3][2], uint32_t& flop, uint32_t& sfu) {
+    uint32_t f = kFlopStation, u = 0;
+    for (int k = 0; k < kSides; ++k) {
+        if (!(mask >> k & 1u)) continue;
+        const bool st = (mask >> (kSides + k)) & 1u;
+        f += kFlopSide + (st ? kFlopSteepExtra : 0);
+        u += kSfuSide + (st ? kSfuSteepExtra : 0);
+    }
+    for (int r = 0; r < 3; ++r) {
+        if (!(mask >> (24 + r) & 1u)) continue;
+        f += kFlopQuadRect + kFlopQuadNode * nq[r][0] * nq[r][1];
+        u += kSfuQuadNode * nq[r][0] * nq[r][1];
+    }
+    flop = f;
+    sfu = u;
 }
 
 // ---------------------------------------------------------------------------
@@ -381,17 +538,24 @@ AG_DEVICE_INLINE void side_pair_t(const K& k, V Xr, V Yr, V& ue, V& un, V& uv) {
     const V y1A = vfma(c, Xr, vfma(s, Yr, KN(K_K1)));
     const V y2 = vfma(s, Xr, vfma(KN(K_C), Yr, KN(K_K2)));
     const V y1B = vadd(y1A, dy1);
-    // artefact-free configuration (libcdm.py:342-362): I if y1A >= 0 (β - π), else II (β);
-    // sin, cos and cot(β/2) of β - π are those of β times -1.  A near-vertical side takes
-    // the ratio configuration (sg = sign cos β) at every station instead: its r - z3 has no
-    // zero and its Burgers-function argument no sign change at the free surface, and both
-    // configurations give the same pair away from the other's singular ray.
+    // Artefact-free configuration: II (β) or I (β - π; sin, cos and cot(β/2) of β - π are
+    // those of β times -1), libcdm.py:342-362.  Both give the same pair away from the other's
+    // singular ray (where r - z3 vanishes at the surface); the reference picks I where
+    // y1A >= 0.  Here each station takes the configuration whose legs point away from it:
+    // with u = y1 sin β - a cos β (z3 of configuration II; u_B = u_A + Δz3, Δz3 = -L), II if
+    // u_A + u_B <= 0, else I, so z3 <= 0 and r - z3 >= r at both vertices whenever the
+    // station's projection on the side's line falls outside the side.  The reference's rule
+    // can leave a leg pointing at a station near a shallow vertex, where r - z3 << r and the
+    // large terms cancel in FP32.  A near-vertical side takes the ratio configuration
+    // (sg = sign cos β) at every station: its r - z3 has no zero and its Burgers-function
+    // argument no sign change at the free surface.
     V sg, ct2;
+    const V u3A = vfma(y1A, KC(K_SB), KC(K_NAACB));
     if constexpr (Steep) {
         sg = V(k.template at<K_CB>() > 0.0f ? 1.0f : -1.0f);
         ct2 = KC(K_CT2);
     } else {
-        const auto conf1 = vge0(y1A);
+        const auto conf1 = vgt0(vfma(V(2.0f), u3A, KC(K_DZ3)));
         sg = vsel(conf1, V(-1.0f), V(1.0f));
         ct2 = vsel(conf1, KN(K_TB2), KC(K_CTB2));
     }
@@ -411,7 +575,7 @@ AG_DEVICE_INLINE void side_pair_t(const K& k, V Xr, V Yr, V& ue, V& un, V& uv) {
     const V z1A = vmul(sg, vfma(y1A, KC(K_CB), KC(K_AASB)));
     const V dz1 = vmul(sg, KC(K_DZ1));
     const V z1B = vadd(z1A, dz1);
-    const V z3A = vmul(sg, vfma(y1A, KC(K_SB), KC(K_NAACB)));
+    const V z3A = vmul(sg, u3A);
     const V dz3 = vmul(sg, KC(K_DZ3));
     const V z3B = vadd(z3A, dz3);
     // r - z3, cancellation-free: (z1² + y2²)/(r + z3) when z3 > 0, else (r + z3) - 2 z3
@@ -567,6 +731,53 @@ AG_DEVICE_INLINE void side_pair(const K& k, V Xr, V Yr, V& ue, V& un, V& uv, boo
         side_pair_t<true>(k, Xr, Yr, ue, un, uv);
     else
         side_pair_t<false>(k, Xr, Yr, ue, un, uv);
+}
+
+// One rectangle by its quadrature nodes (QuadC; the point tensile dislocation above).
+// Per station: the strike-frame coordinates and q once, then per node
+//   R² = x² + y² + d², A = 1/(R(R+d)²), E = 1/(R³(R+d)²), B = (3R+d) E/(R+d), T = 3q²/R⁵,
+//   ux = x [T - k s² (1/R³ - (A - y² B))],  uy = y [T - k s² (A - x² B)],
+//   uz = d T - k s² (1/(R(R+d)) - x²(2R+d) E),
+// weighted and summed in FP32 (the nodes' terms vary smoothly: no cancellation).
+template <class V>
+AG_DEVICE_INLINE void rect_quad(const QuadC& Q, V Xr, V Yr, V& ue, V& un, V& uv) {
+    const V a = V(Q.h0.x), b = V(Q.h0.y);
+    const V xs = vfma(a, Xr, vmul(b, Yr));
+    const V ys = vfma(a, Yr, vneg(vmul(b, Xr)));
+    const V q = vfma(ys, V(Q.h0.z), V(-Q.h0.w));
+    const V q3 = vmul(vmul(q, q), V(3.0f));
+    const V nks2 = V(Q.h1.x);
+    const int nn = __float_as_int(Q.h1.y);
+    V sx(0.0f), sy(0.0f), sz(0.0f);
+#pragma unroll 2
+    for (int k = 0; k < nn; ++k) {
+        const float4 nd = Q.node[k];
+        const V x = vsub(xs, V(nd.x)), y = vsub(ys, V(nd.y)), d = V(nd.z), w = V(nd.w);
+        const V R2 = vfma(x, x, vfma(y, y, vmul(d, d)));
+        const V iR = vrsqrt(R2);
+        const V R = vmul(R2, iR);
+        const V iRd = frcp(vadd(R, d));
+        const V iR2 = vmul(iR, iR), iR3 = vmul(iR2, iR);
+        const V T = vmul(q3, vmul(iR3, iR2));
+        const V iRd2 = vmul(iRd, iRd);
+        const V A = vmul(iR, iRd2);
+        const V E = vmul(iR3, iRd2);
+        const V B = vmul(vmul(vfma(V(3.0f), R, d), E), iRd);
+        const V x2 = vmul(x, x), y2 = vmul(y, y);
+        const V G1 = vfma(vneg(x2), B, A);
+        const V G2 = vfma(vneg(y2), B, A);
+        const V ux = vmul(x, vfma(nks2, vsub(iR3, G2), T));
+        const V uy = vmul(y, vfma(nks2, G1, T));
+        const V I5 = vfma(vneg(vmul(x2, vfma(V(2.0f), R, d))), E, vmul(iR, iRd));
+        const V uz = vfma(nks2, I5, vmul(d, T));
+        sx = vfma(w, ux, sx);
+        sy = vfma(w, uy, sy);
+        sz = vfma(w, uz, sz);
+    }
+    // back to EFCS: x̂ = (a, b), ŷ = (-b, a)
+    ue = vfma(a, sx, vfma(vneg(b), sy, ue));
+    un = vfma(b, sx, vfma(a, sy, un));
+    uv = vadd(uv, sz);
 }
 
 #undef KC

@@ -99,6 +99,23 @@ __global__ void cdm_check_kernel(ag_layout L, const double* __restrict__ theta, 
     if (cdm_corners(theta + (size_t)i * L.nparams, L, V)) chain_status[i] |= CHAIN_ABOVE_SURFACE;
 }
 
+// FP32 operations per station the likelihood kernel executes for each chain (its plan:
+// sides and quadrature nodes); 0 for chains above the free surface, which it skips
+__global__ void cdm_work_kernel(ag_layout L, const double* __restrict__ theta, int n,
+                                uint32_t* __restrict__ flop, uint32_t* __restrict__ sfu) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double* th = theta + (size_t)i * L.nparams;
+    Vec3 V[3][4];
+    uint32_t f = 0u, u = 0u;
+    if (!cdm_corners(th, L, V)) {
+        int nq[3][2];
+        cdm_work(cdm_plan(th, L, V, nq), nq, f, u);
+    }
+    flop[i] = f;
+    if (sfu) sfu[i] = u;
+}
+
 // ---------------------------------------------------------------------------
 // CDM likelihood.  One warp per compacted chain slot, lanes over stations.
 // Station tiles stream through a ring of kStages shared-memory buffers filled
@@ -206,6 +223,13 @@ cdm_llk_kernel(const ChainC* __restrict__ chains, const int32_t* __restrict__ sl
                         msk &= msk - 1;
                         side_pair<SV<SPL>>(ScalarSide(C.side[sidx]), Xr, Yr, ue, un, uv, (smask >> (kSides + sidx)) & 1u);
                     }
+                    uint32_t qm = (smask >> 24) & 7u;
+#pragma unroll 1
+                    while (qm) {
+                        const int r = __ffs(qm) - 1;
+                        qm &= qm - 1;
+                        rect_quad<SV<SPL>>(*reinterpret_cast<const QuadC*>(&C.side[4 * r]), Xr, Yr, ue, un, uv);
+                    }
 #pragma unroll
                     for (int q = 0; q < SPL; ++q) finish(ue.v[q], un.v[q], uv.v[q], j0 + 32 * q);
                 }
@@ -221,6 +245,13 @@ cdm_llk_kernel(const ChainC* __restrict__ chains, const int32_t* __restrict__ sl
                         const int sidx = __ffs(msk) - 1;
                         msk &= msk - 1;
                         side_pair<float>(ScalarSide(C.side[sidx]), Xr, Yr, ue, un, uv, (smask >> (kSides + sidx)) & 1u);
+                    }
+                    uint32_t qm = (smask >> 24) & 7u;
+#pragma unroll 1
+                    while (qm) {
+                        const int r = __ffs(qm) - 1;
+                        qm &= qm - 1;
+                        rect_quad<float>(*reinterpret_cast<const QuadC*>(&C.side[4 * r]), Xr, Yr, ue, un, uv);
                     }
                     finish(ue, un, uv, j);
                 }
@@ -483,6 +514,17 @@ extern "C" int ag_forward_llk_subset(int model, const ag_layout* layout, const d
     AG_REQUIRE(index != nullptr && count != nullptr, "index and count must not be NULL");
     return forward_llk(model, layout, theta, n, st, norm, nullptr, index, count, llk, chain_status,
                        residuals, workspace, workspace_bytes, stream);
+}
+
+extern "C" int ag_cdm_work(const ag_layout* layout, const double* theta, int32_t n, uint32_t* flop_per_station,
+                           uint32_t* sfu_per_station, void* stream) {
+    AG_REQUIRE(layout && theta && flop_per_station && n > 0, "invalid arguments");
+    const ag_layout L = *layout;
+    AG_REQUIRE(L.nparams > 0 && L.axes_idx >= 0 && L.axes_idx + 2 < L.nparams && L.omega_idx >= 0 &&
+                   L.omega_idx + 2 < L.nparams,
+               "invalid CDM layout");
+    cdm_work_kernel<<<(n + 127) / 128, 128, 0, as_stream(stream)>>>(L, theta, n, flop_per_station, sfu_per_station);
+    return launch_status("cdm_work_kernel");
 }
 
 extern "C" int ag_cdm_check(const ag_layout* layout, const double* theta, int32_t n,

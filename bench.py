@@ -36,20 +36,11 @@ LOS = (0.38, -0.08, 0.92)
 PRIORS = [(-1e4, 1e4), (-1e4, 1e4), (1e3, 1e4), (-50.0, 50.0), (100.0, 3000.0), (100.0, 3000.0),
           (100.0, 3000.0), (-90.0, 90.0), (-90.0, 90.0), (-90.0, 90.0)]
 # parameter order: x0, y0, depth, opening, ax, ay, az, ωx, ωy, ωz
-# FP32 operations per (chain, station) pair of the fused CDM kernel (FMA = 2): per
-# rectangle side 249 (the difference-arithmetic pair of altar_gb300/csrc/cdm_side.cuh
-# including 2 x 10 for log2_ratio and 22 for atan2_poly, counted by evaluating the pair
-# with a counting number type: tests/cdm_host/cdm_host.cpp), times 12 sides, + 31 per
-# station (coordinates, LOS projection, float-float misfit); special-function unit: 13
-# per side (2 rsqrt, 9 rcp, 2 lg2)
-CDM_FLOP_PER_PAIR = 3019
-CDM_SFU_PER_SIDE = 13
-# near-vertical sides (|cot β| >= 3: ~9% of the sides of prior samples, none of the
-# workload's truth) take their own evaluation, which forms the O(β) remainders of the
-# terms with cot β and cot²β coefficients without cancellation: extra FLOP and
-# special-function operations per such side; the roofline counts the base figure only,
-# so its achieved rate is a lower bound for populations with steep sides
-CDM_STEEP_EXTRA = (80, 3)
+# FP32 work of the fused CDM kernel: per (chain, station) pair it is the chain's plan, summed
+# by the library (ag_cdm_work): 251 FLOP (FMA = 2) and 13 special-function operations per
+# rectangle side evaluated as an angular-dislocation pair (78 FLOP and 3 more for a
+# near-vertical side), 19 + 48 per node for a rectangle integrated by quadrature, + 31 per
+# station; the constants are counted from the source by tests/cdm_host/cdm_host.cpp
 L2_FLUSH_BYTES = 256 << 20
 
 
@@ -682,10 +673,15 @@ def run_ours(args):
         torch.cuda.synchronize()
         t_fwd = sum(a.elapsed_time(b) for a, b in fev) / len(fev) / 1e3
         pairs = n * X.size
-        achieved = pairs * CDM_FLOP_PER_PAIR / t_fwd / 1e12
+        flop_chain, sfu_chain = model.strategy.work(th_all, stream=stream)
+        torch.cuda.synchronize()
+        flop_launch = float(flop_chain.double().sum().item()) * X.size
+        evaluated_pairs = int((flop_chain > 0).sum().item()) * X.size
+        achieved = flop_launch / t_fwd / 1e12
         pk = peaks()
         sm_max = float(pk.get("sm_max_mhz", 2070.0))
-        fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12   # FMA lanes x 2 FLOP x max SM clock
+        sms = torch.cuda.get_device_properties(local).multi_processor_count
+        fp32_peak = sms * 128 * 2 * sm_max * 1e6 / 1e12   # FMA lanes x 2 FLOP x max SM clock
 
         # end to end through host buffers: the same stages again from the saved state, with θ and
         # the three log-likelihood vectors copied in from pinned host memory and back every stage
@@ -740,8 +736,11 @@ def run_ours(args):
                    "likelihoods_evaluated": evaluated},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved / fp32_peak, "traffic": profile_traffic,
-                     "kernel": "cdm_setup_kernel + cdm_llk_kernel", "flop_per_pair": CDM_FLOP_PER_PAIR,
-                     "pairs_per_launch": pairs, "ms_per_launch": t_fwd * 1e3,
+                     "kernel": "cdm_setup_kernel + cdm_llk_kernel",
+                     "flop_per_launch": flop_launch, "flop_per_pair": flop_launch / max(1, evaluated_pairs),
+                     "flop_source": "per-chain plan summed by ag_cdm_work (sides and quadrature nodes)",
+                     "pairs_per_launch": pairs, "evaluated_pairs_per_launch": evaluated_pairs,
+                     "ms_per_launch": t_fwd * 1e3, "sms": sms,
                      "peak_source": "nominal FP32 FMA rate at the measured max SM clock "
                                     "(MEASURED_PEAKS.json has no FP32 figure)"},
         "e2e": {"value": world * N * S / t_e2e, "unit": "chain-steps/s", "h2d_bytes_per_step": io_bytes,
@@ -754,6 +753,9 @@ def run_ours(args):
                                    f"{cpu_dt:.1f} s (FP64 C restatement of models/cdm/cdm/libcdm.py)"},
         "clocks": clk.summary(),
         "pair_evals_per_s": value * X.size * evaluated,
+        # the rate of full likelihood evaluations (the chain-steps whose proposal stayed in the
+        # prior and below the surface): the unit the CPU baseline times
+        "likelihoods_per_s": value * evaluated,
     }
     if args.full_run:
         # the whole plain run to β = 1 from the prior (time-to-β=1 and its mean chain-step rate)

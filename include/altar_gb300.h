@@ -131,6 +131,16 @@ int ag_forward_llk_subset(int model, const ag_layout* layout, const double* thet
                           float* residuals, void* workspace, size_t workspace_bytes, void* stream);
 
 /*
+ * Work of the CDM likelihood kernel per station for each chain: the FP32
+ * operations (FMA = 2) and special-function operations its plan executes
+ * (rectangles evaluated by their sides or, far from the free surface, by
+ * quadrature nodes); 0 for chains above the free surface.  For roofline
+ * accounting; sfu_per_station may be NULL.  No counterpart in the reference.
+ */
+int ag_cdm_work(const ag_layout* layout, const double* theta, int32_t n, uint32_t* flop_per_station,
+                uint32_t* sfu_per_station, void* stream);
+
+/*
  * CDM geometry check only: chain_status[i] |= AG_CHAIN_ABOVE_SURFACE where a
  * corner of the CDM lies above the free surface (models/cdm/cdm/libcdm.py:219-224).
  */

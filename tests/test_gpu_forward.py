@@ -1,16 +1,14 @@
 """Forward models + misfit on the GPU against the oracle and the reference fixtures.
 
 Tolerances (FP32 device arithmetic against FP64 references):
-  * CDM LOS displacement, per source, normwise: |u_gpu - u_ref|_inf <= TOL_CDM * |u_ref|_inf
-    for every source, whatever the angle of its sides.  Near-vertical sides are
-    ill-conditioned in the angular-dislocation formula itself (coefficients of order
-    cot β and cot²β multiplying O(β) combinations); the kernel evaluates them from
-    cancellation-free remainders, so their FP32 error no longer grows with cot β (host
-    build of the same arithmetic, 2000 prior sources: all within 1e-5 when a side is within
-    18° of the vertical, 99.5% of all sources within 1e-5).  The median error over sources
-    must stay below TOL_CDM_MEDIAN, and most sources within 1e-5 (CDM_FRAC_1E5).  The
-    300 prior sources of the workload-grid test are held to TOL_CDM_GRID (measured on a
-    GB300: max 1.4e-5, 99.3% within 1e-5).
+  * CDM LOS displacement, per source, normwise: |u_gpu - u_ref|_inf <= 1e-5 |u_ref|_inf
+    for every source (the benchmark spec's bound), whatever the angle of its sides and its
+    depth.  Rectangles whose sides would cancel (deep relative to their size) are
+    integrated by quadrature of point tensile dislocations; near shallow vertices each
+    station takes the configuration whose legs point away from it; near-vertical sides are
+    evaluated from cancellation-free remainders.  Host build of the same arithmetic: 1,300
+    prior sources, max 2.5e-6, median 3e-7; GB300: 300 sources, max 3.4e-6.  The median
+    over sources must stay below TOL_CDM_MEDIAN.
   * Mogi LOS displacement: normwise 1e-5.
   * log-likelihood given the device's own FP32 residuals: 1e-9 relative (FP64 oracle sum).
 """
@@ -28,10 +26,8 @@ from gpu_helpers import (LOS, cdm_los_oracle, cdm_prior_rows, cdm_strategy, dev,
 
 pytestmark = pytest.mark.gpu
 
-TOL_CDM = 1e-4
-TOL_CDM_GRID = 3e-5
-TOL_CDM_MEDIAN = 5e-6
-CDM_FRAC_1E5 = 0.98
+TOL_CDM = 1e-5
+TOL_CDM_MEDIAN = 1e-6
 G = np.load(os.path.join(os.path.dirname(__file__), "golden", "cdm_golden.npz"))
 
 
@@ -92,16 +88,47 @@ def test_cdm_prior_sources_workload_grid(cuda):
     _, res = _residuals(strat, theta, X.size)
     errs = np.max(np.abs(res - ref), 1) / np.max(np.abs(ref), 1)
     ang = np.array([min_vertical_angle(t) for t in theta])
-    assert np.all(errs <= TOL_CDM_GRID), [(e, a) for e, a in zip(errs, ang) if e > TOL_CDM_GRID]
-    assert np.median(errs) <= TOL_CDM_MEDIAN
-    assert np.mean(errs <= 1e-5) >= CDM_FRAC_1E5, np.mean(errs <= 1e-5)
     print(f"\nCDM normwise error over {len(theta)} prior sources: median {np.median(errs):.2e}, "
-          f"within 1e-5: {np.mean(errs <= 1e-5):.1%}")
+          f"max {errs.max():.2e}")
+    assert np.all(errs <= TOL_CDM), [(e, a) for e, a in zip(errs, ang) if e > TOL_CDM]
+    assert np.median(errs) <= TOL_CDM_MEDIAN
     for lo, hi in ((10, 91), (5, 10), (2, 5), (0, 2)):
         s = (ang >= lo) & (ang < hi)
         if s.any():
             print(f"  smallest side angle [{lo}, {hi}) deg: {s.sum()} sources, median {np.median(errs[s]):.2e}, "
                   f"max {errs[s].max():.2e}")
+
+
+def test_cdm_work_count_matches_host_plan(cuda):
+    """ag_cdm_work (the roofline's FLOP count) follows the same per-chain plan as the set-up
+    kernel: against the host build of that plan, and 0 for a source above the surface."""
+    import ctypes
+    import shutil
+    import subprocess
+    import tempfile
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("g++ not available")
+    so = os.path.join(tempfile.mkdtemp(), "cdm_host.so")
+    here = os.path.dirname(os.path.abspath(__file__))
+    subprocess.run([cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared",
+                    os.path.join(here, "cdm_host", "cdm_host.cpp"), "-o", so], check=True)
+    host = ctypes.CDLL(so)
+    P = ctypes.POINTER
+    theta = cdm_prior_rows(200, seed=31)
+    theta = np.concatenate([theta, [[0, 0, 200.0, 1.0, 2000, 2000, 2000, 0, 0, 0]]])
+    X = np.linspace(-1e3, 1e3, 8)
+    strat, _ = cdm_strategy(X, X, np.tile(LOS, (X.size, 1)), np.zeros(X.size), np.ones(X.size))
+    flop, sfu = strat.work(dev(theta))
+    flop = flop.cpu().numpy()
+    assert flop[-1] == 0
+    for k, th in enumerate(theta[:-1]):
+        m, f, u = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32()
+        nq = (ctypes.c_int * 6)()
+        t = np.ascontiguousarray(th)
+        assert host.cdm_host_plan(t.ctypes.data_as(P(ctypes.c_double)), ctypes.c_double(0.25), ctypes.byref(m),
+                                  nq, ctypes.byref(f), ctypes.byref(u)) == 0
+        assert flop[k] == f.value, k
 
 
 def test_cdm_launch_variants_identical(cuda):
