@@ -1116,8 +1116,12 @@ extern "C" int ag_adapt_scaling(const ag_stage_state* st, double aw, double rw, 
 // cudaMalloc and cudaFree may synchronise the device.  This entry point
 // needs no caller workspace: its scratch (the schedule state and the
 // per-block partial moments) lives in a file-scope device array of fixed
-// size, reserved when the library is loaded on a device and held by every
-// device that loads the library until the process exits.
+// size, reserved when this file's module is loaded on a device and held by
+// every device that loads it until the process exits.  Under CUDA's default
+// lazy module loading the module is loaded by the first use of any kernel or
+// symbol of this file (the first call of this entry point, ag_cov_schedule,
+// ag_resample, ...), which may then enter the driver's allocator once:
+// callers make such a call during start-up.
 //
 // * Limit: n <= kNoAllocMaxChains chains; larger n is rejected.
 // * All calls share the one array, and it keeps the last call's contents:

@@ -3,7 +3,10 @@
  *
  * Every pointer argument is a DEVICE pointer owned by the caller unless the
  * comment says otherwise; the library allocates nothing and keeps no global
- * mutable state apart from a per-thread error string.  Every call is
+ * mutable state apart from a per-thread error string, with one exception:
+ * ag_cov_schedule_noalloc keeps its scratch in a fixed device array inside the
+ * library (about 45 KB per device) and caches that array's address per
+ * device.  Every call is
  * asynchronous on the given stream (a cudaStream_t passed as void*, NULL =
  * legacy default stream) and returns AG_OK or an error code; the message of
  * the last error of the calling thread is available from ag_last_error().
@@ -239,6 +242,11 @@ int ag_cov_schedule_brent(const ag_stage_state* st, const double* data_llk, int3
  * AG_ERR_SIZE.  All calls share that array: calls that overlap on the GPU
  * race, so issue them in order on one stream.  The first call on a device
  * looks up the array's address and should come before any stream capture.
+ * The array is reserved when the library's stage module is loaded on a device:
+ * under CUDA's default lazy module loading that happens at the first call into
+ * any of the stage entry points (this one, ag_cov_schedule, ag_resample, ...),
+ * which may then enter the driver's allocator once; make such a call during
+ * start-up so that later calls allocate nothing.
  */
 int ag_cov_schedule_noalloc(const ag_stage_state* st, const double* data_llk, int32_t n,
                             double target, double tol, void* stream);

@@ -43,6 +43,18 @@ def test_noalloc_schedule_matches_workspace_version(cuda):
         np.testing.assert_allclose(got_w, ref_w, rtol=1e-12, atol=1e-300)
 
 
+def test_noalloc_at_the_chain_limit(cuda):
+    """At ag_cov_schedule_noalloc_max_chains() chains the per-block partials fill the whole
+    fixed scratch array (an undersized array would show here first)."""
+    n = _native.load().ag_cov_schedule_noalloc_max_chains()
+    llk = np.random.default_rng(5).normal(-2e4, 3e2, n)
+    for beta0 in (0.0, 0.3):                       # two calls in a row at the limit
+        ref_s, ref_w = _run("ag_cov_schedule", llk, beta0, n)
+        got_s, got_w = _run("ag_cov_schedule_noalloc", llk, beta0, n)
+        np.testing.assert_allclose(got_s, ref_s, rtol=1e-12, atol=0)
+        np.testing.assert_allclose(got_w, ref_w, rtol=1e-12, atol=1e-300)
+
+
 def test_noalloc_rejects_too_many_chains(cuda):
     lib = _native.load()
     big = lib.ag_cov_schedule_noalloc_max_chains() + 1
