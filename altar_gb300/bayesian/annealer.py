@@ -32,7 +32,8 @@ class Annealer:
         self.scheduler.initialize(application=application)
         if self.archiver is not None:
             self.archiver.initialize(application=application)
-        self.worker = CUDAAnnealing(annealer=self, graphs=self.graphs).initialize(application)
+        wid = torch.distributed.get_rank() if torch.distributed.is_initialized() else 0
+        self.worker = CUDAAnnealing(annealer=self, graphs=self.graphs, wid=wid).initialize(application)
         for monitor in getattr(application, "monitors", {}).values():
             monitor.initialize(application=application)
             self.dispatcher.register(monitor=monitor)

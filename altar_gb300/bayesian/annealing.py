@@ -21,9 +21,10 @@ log = logging.getLogger("altar_gb300")
 
 
 class CUDAAnnealing:
-    def __init__(self, annealer, graphs=True):
+    def __init__(self, annealer, graphs=True, wid=0):
         self.annealer = annealer
         self.graphs = bool(graphs)
+        self.wid = wid                              # worker id (the rank), as in the reference's workers
         self.step = None
         self.iteration = 0
         self.stream = None
@@ -56,9 +57,14 @@ class CUDAAnnealing:
         annealer.model.top(step=self.step)
         return self
 
+    def _eager(self):
+        # a monitor that times the phases inside a stage (the Profiler) needs them launched one
+        # by one: a replayed graph does not call back into the host
+        return not self.graphs or getattr(self.annealer.dispatcher, "eager", False)
+
     def _phase(self, name, fn):
         """Run fn eagerly the first time (allocating its buffers), as a captured graph afterwards."""
-        if not self.graphs or name not in self._eager_done:
+        if self._eager() or name not in self._eager_done:
             self._eager_done.add(name)
             return fn()
         ex = self._graphs.get(name)

@@ -144,3 +144,25 @@ def test_cdm_annealing_runs(cuda):
     assert reps[-1]["beta"] > reps[0]["beta"]
     th = app.controller.worker.step.theta.cpu().numpy()
     assert np.all(np.isfinite(th)) and np.all(np.isfinite(app.controller.worker.step.data.cpu().numpy()))
+
+
+def test_profiler_times_the_phases(cuda, tmp_path):
+    """A run with the Profiler registered (phases launched one by one, timed with CUDA
+    events) writes the reference's profile file and ends where the captured-graph run ends."""
+    import csv
+
+    from altar_gb300.bayesian import Profiler
+    app = mogi_app(chains=256, steps=2)
+    prof = Profiler(directory=str(tmp_path))
+    app.monitors["profiler"] = prof
+    app.run()
+    assert prof.filename.endswith(f"prof-00000-{prof.beta:03d}x004x000256x002.csv")
+    with open(prof.filename, newline="") as f:
+        rows = {r[0]: r[1:] for r in csv.reader(f)}
+    t = {k: float(v[0]) for k, v in rows.items() if v and k not in ("beta steps", "parameters", "chains", "steps")}
+    assert t["simulation"] >= t["beta"] >= t["walk"] >= t["samplePosterior"] > 0
+    assert t["data"] > 0 and t["verify"] > 0 and t["accept"] > 0 and t["resample"] > 0
+    ref = mogi_app(chains=256, steps=2)
+    ref.run()
+    np.testing.assert_array_equal(app.controller.worker.step.theta.cpu().numpy(),
+                                  ref.controller.worker.step.theta.cpu().numpy())
