@@ -283,3 +283,41 @@ def test_host_buffer_call_pattern(cuda):
     out = torch.empty(10, dtype=torch.float64, device="cuda")
     strat.forward(dev(theta), out)
     np.testing.assert_array_equal(step.data, out.cpu().numpy())
+
+
+def test_cdm_dense_cd_from_case_files(cuda, tmp_path):
+    """A case directory with a dense cd.txt (models/cdm/cdm/CDM.py:275-355): the reader keeps
+    Cd dense, the fused kernel writes residual rows and the tcgen05 whitening adds
+    -1/2 rᵀ Cd⁻¹ r; against the FP64 oracle llk = -1/2 (M log 2π + log det Cd + rᵀ Cd⁻¹ r)
+    within 1e-4 relative (FP32 forward model, split-BF16 whitening)."""
+    import math
+
+    from altar_gb300.models.forward import CUDA
+    from altar_gb300.models.observations import Observations
+    from gpu_helpers import Shim
+    from test_observations_cpu import write_case
+
+    rng = np.random.default_rng(4)
+    m = 300
+    x, y = rng.uniform(-2e4, 2e4, m), rng.uniform(-2e4, 2e4, m)
+    th_los, ph_los = np.full(m, 0.4), np.full(m, -1.2)
+    los = np.stack([np.sin(th_los) * np.cos(ph_los), np.sin(th_los) * np.sin(ph_los), np.cos(th_los)], 1)
+    dist = np.hypot(x[:, None] - x[None, :], y[:, None] - y[None, :])
+    cd = 9e-6 * np.exp(-dist / 2e3) + 1e-9 * np.eye(m)
+    truth = cdm_prior_rows(1, seed=40)
+    d = cdm_los_oracle(truth, x, y, los)[0] + np.linalg.cholesky(cd) @ rng.normal(size=m)
+    write_case(tmp_path, x, y, d, th_los, ph_los, cd)
+    obs = Observations.read(str(tmp_path))
+    assert obs.dense
+    lay = _native.Layout(10, 0, 2, 3, 4, 7, -1, 0, 1, 0, nu=0.25)
+    strat = CUDA(_native.AG_MODEL_CDM).initialize(None, Shim(obs, lay))
+    theta = np.concatenate([truth + rng.normal(size=(32, 10)) * [50, 50, 50, 0.5, 20, 20, 20, 1, 1, 1],
+                            cdm_prior_rows(32, seed=41)])
+    out = torch.empty(theta.shape[0], dtype=torch.float64, device="cuda")
+    strat.forward(dev(theta), out)
+    torch.cuda.synchronize()
+    r = cdm_los_oracle(theta, x, y, los) - d[None, :]
+    sign, logdet = np.linalg.slogdet(cd)
+    ref = -0.5 * (m * math.log(2 * math.pi) + logdet) - 0.5 * np.einsum("ij,ji->i", r, np.linalg.solve(cd, r.T))
+    got = out.cpu().numpy()
+    assert np.all(np.abs(got - ref) <= 1e-4 * np.abs(ref) + 1e-3), np.max(np.abs(got - ref) / np.abs(ref))
