@@ -121,7 +121,8 @@ class MLP(ctypes.Structure):
 class StageState(ctypes.Structure):
     _fields_ = [("beta", c_void_p), ("dbeta_cov", c_void_p), ("scaling", c_void_p),
                 ("sigma", c_void_p), ("chol", c_void_p), ("w", c_void_p),
-                ("counters", c_void_p), ("epoch", c_void_p), ("dev_flags", c_void_p)]
+                ("counters", c_void_p), ("epoch", c_void_p), ("dev_flags", c_void_p),
+                ("chain0", c_int32), ("reserved", c_int32)]
 
 
 P = c_void_p

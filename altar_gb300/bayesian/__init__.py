@@ -7,7 +7,9 @@ from .brent import Brent
 from .cov import COV
 from .annealing import CUDAAnnealing
 from .annealer import Annealer
+from .sharding import ChainShards, ShardedAnnealing
 from .surrogate import DelayedAcceptance, SubsetSurrogate, Surrogate
 
 __all__ = ["CoolingStep", "StageState", "Notifier", "Profiler", "Metropolis", "Grid", "Brent", "COV",
-           "CUDAAnnealing", "Annealer", "DelayedAcceptance", "Surrogate", "SubsetSurrogate"]
+           "CUDAAnnealing", "Annealer", "ChainShards", "ShardedAnnealing", "DelayedAcceptance", "Surrogate",
+           "SubsetSurrogate"]

@@ -13,9 +13,10 @@ from .notifier import Notifier
 
 class Annealer:
     def __init__(self, sampler=None, scheduler=None, dispatcher=None, archiver=None, graphs=True,
-                 checkpoint=None, resume=None):
+                 checkpoint=None, resume=None, shards=None):
         """checkpoint: a simulations.Checkpoint written after every ``every`` stages;
-        resume: path of a checkpoint to continue from instead of sampling the prior."""
+        resume: path of a checkpoint to continue from instead of sampling the prior;
+        shards: a bayesian.ChainShards to split the population's walk across ranks."""
         self.sampler = sampler if sampler is not None else Metropolis()
         self.scheduler = scheduler if scheduler is not None else COV()
         self.dispatcher = dispatcher if dispatcher is not None else Notifier()
@@ -23,6 +24,7 @@ class Annealer:
         self.graphs = graphs
         self.checkpoint = checkpoint
         self.resume = resume
+        self.shards = shards
         self.worker = None
         self.model = None
 
@@ -32,8 +34,12 @@ class Annealer:
         self.scheduler.initialize(application=application)
         if self.archiver is not None:
             self.archiver.initialize(application=application)
-        wid = torch.distributed.get_rank() if torch.distributed.is_initialized() else 0
-        self.worker = CUDAAnnealing(annealer=self, graphs=self.graphs, wid=wid).initialize(application)
+        if self.shards is not None:
+            from .sharding import ShardedAnnealing
+            self.worker = ShardedAnnealing(self, self.shards, graphs=self.graphs).initialize(application)
+        else:
+            wid = torch.distributed.get_rank() if torch.distributed.is_initialized() else 0
+            self.worker = CUDAAnnealing(annealer=self, graphs=self.graphs, wid=wid).initialize(application)
         for monitor in getattr(application, "monitors", {}).values():
             monitor.initialize(application=application)
             self.dispatcher.register(monitor=monitor)

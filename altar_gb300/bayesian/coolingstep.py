@@ -5,6 +5,7 @@ and posterior log-likelihoods, and Σ.  β and the sampler's per-stage scalars
 live in a small device block (``StageState``) so that the stage kernels, and
 CUDA graphs of them, never need the host.
 """
+import copy
 import ctypes
 
 import torch
@@ -16,7 +17,9 @@ from ..device import DEVICE, ptr
 class StageState:
     """Device block behind ``ag_stage_state``."""
 
-    def __init__(self, samples, parameters):
+    def __init__(self, samples, parameters, chain0=0):
+        """chain0: global index of the first row when the population is split across ranks
+        (the proposal and accept streams are keyed by the global chain index)."""
         f64 = dict(dtype=torch.float64, device=DEVICE)
         self.scalars = torch.zeros(8, **f64)          # β, δβ, cov, scaling
         self.beta = self.scalars[0:1]
@@ -28,9 +31,20 @@ class StageState:
         self.counters = torch.zeros(3, dtype=torch.int64, device=DEVICE)
         self.epoch = torch.zeros(1, dtype=torch.int32, device=DEVICE)
         self.flags = torch.zeros(1, dtype=torch.int32, device=DEVICE)
-        self._s = _native.StageState(*(t.data_ptr() for t in (
+        self.chain0 = int(chain0)
+        self._s = self._struct(self.chain0)
+
+    def _struct(self, chain0):
+        return _native.StageState(*(t.data_ptr() for t in (
             self.beta, self.dbeta_cov, self.scaling, self.sigma, self.chol, self.w, self.counters,
-            self.epoch, self.flags)))
+            self.epoch, self.flags)), chain0, 0)
+
+    def view(self, chain0):
+        """The same device block, described to the kernels as starting at global chain chain0."""
+        v = copy.copy(self)
+        v.chain0 = int(chain0)
+        v._s = self._struct(v.chain0)
+        return v
 
     @property
     def struct(self):

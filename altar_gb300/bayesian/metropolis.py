@@ -37,6 +37,8 @@ class Metropolis:
     # hooks of the annealing worker: host-side decisions before a walk, and the
     # key under which the walk's launch sequence is captured
     capturable = True
+    # each chain's walk depends on its own row and global index only: a rank can walk a block
+    shardable = True
 
     def prepare(self, annealer, step):
         return self

@@ -66,14 +66,14 @@ __global__ void propose_kernel(const double* __restrict__ theta, int n, int p,
                                const double* __restrict__ chol, const double* __restrict__ lo,
                                const double* __restrict__ hi, uint64_t seed, uint32_t step,
                                const uint32_t* __restrict__ epoch, double* __restrict__ cand,
-                               uint32_t* __restrict__ mask, double* __restrict__ cprior) {
+                               uint32_t* __restrict__ mask, double* __restrict__ cprior, int chain0) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t ep = *epoch;
     double z[kMaxP];
     for (int j = 0; j < p; j += 2) {
         double z0, z1;
-        normal_pair(draw(seed, (uint32_t)i, (uint32_t)(j >> 1), STREAM_PROPOSAL, step, ep), z0, z1);
+        normal_pair(draw(seed, (uint32_t)(chain0 + i), (uint32_t)(j >> 1), STREAM_PROPOSAL, step, ep), z0, z1);
         z[j] = z0;
         if (j + 1 < p) z[j + 1] = z1;
     }
@@ -101,7 +101,7 @@ __global__ void __launch_bounds__(kProposeWarps * 32)
 propose_warp_kernel(const double* __restrict__ theta, int n, int p, const double* __restrict__ chol,
                     const double* __restrict__ lo, const double* __restrict__ hi, uint64_t seed,
                     uint32_t step, const uint32_t* __restrict__ epoch, double* __restrict__ cand,
-                    uint32_t* __restrict__ mask, double* __restrict__ cprior) {
+                    uint32_t* __restrict__ mask, double* __restrict__ cprior, int chain0) {
     extern __shared__ double sz[];                 // [kProposeWarps][p] normals
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int i = blockIdx.x * kProposeWarps + warp;
@@ -110,7 +110,7 @@ propose_warp_kernel(const double* __restrict__ theta, int n, int p, const double
     const uint32_t ep = *epoch;
     for (int q = lane; 2 * q < p; q += 32) {
         double z0, z1;
-        normal_pair(draw(seed, (uint32_t)i, (uint32_t)q, STREAM_PROPOSAL, step, ep), z0, z1);
+        normal_pair(draw(seed, (uint32_t)(chain0 + i), (uint32_t)q, STREAM_PROPOSAL, step, ep), z0, z1);
         z[2 * q] = z0;
         if (2 * q + 1 < p) z[2 * q + 1] = z1;
     }
@@ -143,7 +143,7 @@ __global__ void accept_kernel(int n, int p, const double* __restrict__ beta, uin
                               const double* __restrict__ cprior, const double* __restrict__ cdata,
                               double* __restrict__ theta, double* __restrict__ prior,
                               double* __restrict__ data, double* __restrict__ post,
-                              unsigned long long* __restrict__ counters) {
+                              unsigned long long* __restrict__ counters, int chain0) {
     __shared__ unsigned int s_cnt[3];
     if (threadIdx.x < 3) s_cnt[threadIdx.x] = 0u;
     __syncthreads();
@@ -154,7 +154,7 @@ __global__ void accept_kernel(int n, int p, const double* __restrict__ beta, uin
         } else {
             const double b = *beta;
             const double cp = cprior[i] + b * cdata[i];
-            u32x4 r = draw(seed, (uint32_t)i, 0u, STREAM_ACCEPT, step, *epoch);
+            u32x4 r = draw(seed, (uint32_t)(chain0 + i), 0u, STREAM_ACCEPT, step, *epoch);
             const double u = u01_open_closed(r.x, r.y);
             if (log(u) > cp - post[i]) {
                 atomicAdd(&s_cnt[2], 1u);
@@ -874,6 +874,7 @@ static int check_state(const ag_stage_state* st) {
     AG_REQUIRE(st && st->beta && st->dbeta_cov && st->scaling && st->sigma && st->chol && st->w &&
                    st->counters && st->epoch && st->dev_flags,
                "stage state has a NULL member");
+    AG_REQUIRE(st->chain0 >= 0, "stage state chain0 must be >= 0 (got %d)", st->chain0);
     return AG_OK;
 }
 
@@ -903,7 +904,7 @@ extern "C" int ag_propose(const ag_stage_state* st, const double* theta, int32_t
     cudaStream_t s = as_stream(stream);
     if (p <= kMaxP) {
         propose_kernel<<<blocks(n, 128), 128, 0, s>>>(theta, n, p, st->chol, lo, hi, seed, step, st->epoch, cand,
-                                                       mask, cprior);
+                                                       mask, cprior, st->chain0);
         return launch_status("propose_kernel");
     }
     const size_t smem = (size_t)kProposeWarps * p * sizeof(double);
@@ -914,7 +915,7 @@ extern "C" int ag_propose(const ag_stage_state* st, const double* theta, int32_t
         if (rc) return rc;
     }
     propose_warp_kernel<<<blocks(n, kProposeWarps), kProposeWarps * 32, smem, s>>>(
-        theta, n, p, st->chol, lo, hi, seed, step, st->epoch, cand, mask, cprior);
+        theta, n, p, st->chol, lo, hi, seed, step, st->epoch, cand, mask, cprior, st->chain0);
     return launch_status("propose_warp_kernel");
 }
 
@@ -928,7 +929,7 @@ extern "C" int ag_accept(const ag_stage_state* st, int32_t n, int32_t p, uint64_
                "invalid arguments");
     accept_kernel<<<blocks(n, 256), 256, 0, as_stream(stream)>>>(
         n, p, st->beta, seed, step, st->epoch, mask, cand, cprior, cdata, theta, prior, data, post,
-        st->counters);
+        st->counters, st->chain0);
     return launch_status("accept_kernel");
 }
 

@@ -611,7 +611,12 @@ def run_ours(args):
     forced = args.variant is not None
     model = CDM(psets, observations=Observations(X, Y, los, d, SIGMA ** 2),
                 autotune=not (args.no_autotune or forced), variant=args.variant if forced else 0)
-    app = Application(model, job=Job(chains=N, steps=5), rng=RNG(1234 + rank))
+    # N > 1 GPUs: one population of N chains per GPU (weak scaling), each rank walking its
+    # block of chains; blocks and acceptance counters exchanged once per stage (ChainShards)
+    from altar_gb300.bayesian import Annealer, ChainShards
+    shards = ChainShards(dist) if dist is not None else None
+    app = Application(model, job=Job(chains=N * world, steps=5), rng=RNG(1234),
+                      controller=Annealer(shards=shards))
     app.initialize()
     ann = app.controller
     worker = ann.worker
@@ -656,12 +661,14 @@ def run_ours(args):
         t_stage = max_over_ranks(t_stage, dist, device="cuda")
         value = world * N * S / t_stage
         reps = worker.reports[-args.steps:]
-        evaluated = sum(r["accepted"] + r["unlikely"] for r in reps) / max(1, N * S * len(reps))
+        # the stage reports count the whole population's proposals (summed over the GPUs)
+        evaluated = sum(r["accepted"] + r["unlikely"] for r in reps) / max(1, N * world * S * len(reps))
         step = worker.step
-        n = step.samples
+        n = N                                              # chains of this GPU's block
 
         # roofline: the fused forward model on every chain (no mask), CUDA events on its stream
-        th_all = step.theta.clone()
+        c0 = rank * N if shards is not None else 0
+        th_all = step.theta[c0:c0 + N].clone()           # this GPU's block
         out = torch.empty(n, dtype=torch.float64, device="cuda")
         model.strategy.forward(th_all, out)
         fev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(3)]
@@ -724,7 +731,8 @@ def run_ours(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_stage * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "cdm-40k-obs", "chains": N, "stations": X.size, "params": 10,
-                   "steps_per_stage": S, "parallelism": "replicas" if world > 1 else "single-gpu",
+                   "steps_per_stage": S, "parallelism": f"chains sharded over {world} GPUs" if world > 1 else "single-gpu",
+                   "population": N * world,
                    "step": "one annealing stage: COV beta + Sigma + resample, 5 Metropolis steps, scaling",
                    "l2": "flushed (256 MB write) between timed iterations",
                    "graphs": "one CUDA graph per phase (cool, walk, resample)",

@@ -180,6 +180,10 @@ typedef struct ag_stage_state {
     unsigned long long* counters; /* [3] accepted, rejected, unlikely of the current stage */
     uint32_t* epoch;       /* [1] stage counter feeding the random streams */
     uint32_t* dev_flags;   /* [1] AG_DEV_ERR_* bits */
+    int32_t chain0;        /* global index of the first chain these rows hold: the proposal and
+                              accept streams are keyed by chain0 + row, so a population split
+                              across ranks draws what one process would (0 = unsplit) */
+    int32_t reserved;
 } ag_stage_state;
 
 /*

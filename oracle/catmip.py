@@ -280,7 +280,11 @@ class Annealing:
             theta[bad] = redo[bad]
         raise RuntimeError("no valid initial sample")
 
-    def run(self, max_stages=1000):
+    def run(self, max_stages=1000, shards=None):
+        """shards: an exchange with ``bounds(n) -> (first row, rows)``, ``gather(*arrays)`` and
+        ``sum(array)`` (torch tensors sharing the numpy arrays' memory): each rank walks its
+        block of rows with the streams of their global indices, then the blocks and the
+        accept counters are exchanged and the cool phase runs on the whole population."""
         n, p = self.n, self.p
         theta, data = self.initial()
         prior = uniform_log_prior(theta, self.lo, self.hi)
@@ -295,21 +299,30 @@ class Annealing:
             theta, prior, data = theta[src].copy(), prior[src].copy(), data[src].copy()
             post = prior + beta * data
             L = cholesky_scaled(sigma, scaling)
+            c0, m = (0, n) if shards is None else shards.bounds(n)
+            rows = slice(c0, c0 + m)
+            th, pr, da, po = theta[rows], prior[rows], data[rows], post[rows]    # views
             acc = rej = unl = 0
             for k in range(self.steps):
-                z = philox.proposal_normals(self.seed, n, p, k, epoch)
-                cand = theta + z @ L.T
+                z = philox.proposal_normals(self.seed, n, p, k, epoch)[rows]
+                cand = th + z @ L.T
                 bad = uniform_verify(cand, self.lo, self.hi)
-                cand[bad] = theta[bad]
+                cand[bad] = th[bad]
                 cprior = uniform_log_prior(cand, self.lo, self.hi)
                 cdata, invalid = self.data_llk(cand)
                 bad = bad | invalid
                 cpost = cprior + beta * cdata
-                u = philox.accept_uniforms(self.seed, n, k, epoch)
-                unlikely = ~bad & (np.log(u) > cpost - post)
+                u = philox.accept_uniforms(self.seed, n, k, epoch)[rows]
+                unlikely = ~bad & (np.log(u) > cpost - po)
                 ok = ~bad & ~unlikely
-                theta[ok], prior[ok], data[ok], post[ok] = cand[ok], cprior[ok], cdata[ok], cpost[ok]
+                th[ok], pr[ok], da[ok], po[ok] = cand[ok], cprior[ok], cdata[ok], cpost[ok]
                 acc += int(ok.sum()); rej += int(bad.sum()); unl += int(unlikely.sum())
+            if shards is not None:
+                import torch
+                shards.gather(*(torch.from_numpy(a) for a in (theta, prior, data, post)))
+                c = torch.tensor([acc, rej, unl], dtype=torch.int64)
+                shards.sum(c)
+                acc, rej, unl = (int(v) for v in c)
             scaling = adapt_scaling(acc, rej, unl)
             epoch += 1
             stages.append(dict(beta=beta, dbeta=dbeta, cov=cov, accepted=acc, rejected=rej,

@@ -34,7 +34,7 @@ def test_struct_layouts_match_header(tmp_path):
         '#include <stdio.h>\n#include <stddef.h>\n#include "altar_gb300.h"\n'
         "int main(void){printf(\"%zu %zu %zu %zu %zu %zu\\n\", sizeof(ag_station_set),"
         " sizeof(ag_layout), sizeof(ag_stage_state), offsetof(ag_layout, nu),"
-        " offsetof(ag_station_set, m), offsetof(ag_stage_state, dev_flags));"
+        " offsetof(ag_station_set, m), offsetof(ag_stage_state, dev_flags)); printf(\"%zu\\n\", offsetof(ag_stage_state, chain0));"
         " printf(\"%zu %zu %zu\\n\", sizeof(ag_reverso_model), offsetof(ag_reverso_model, east_cos),"
         " offsetof(ag_reverso_model, G)); return 0;}\n")
     exe = tmp_path / "probe"
@@ -42,7 +42,7 @@ def test_struct_layouts_match_header(tmp_path):
     got = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True).stdout.split()]
     want = [ctypes.sizeof(_native.StationSet), ctypes.sizeof(_native.Layout),
             ctypes.sizeof(_native.StageState), _native.Layout.nu.offset, _native.StationSet.m.offset,
-            _native.StageState.dev_flags.offset, ctypes.sizeof(_native.ReversoModel),
+            _native.StageState.dev_flags.offset, _native.StageState.chain0.offset, ctypes.sizeof(_native.ReversoModel),
             _native.ReversoModel.east_cos.offset, _native.ReversoModel.G.offset]
     assert got == want
 
