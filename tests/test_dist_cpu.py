@@ -1,8 +1,7 @@
 """Multi-process host logic of the benchmark on CPU (gloo, two ranks).
 
-Each GPU runs an independent replica of the chain population (replicas only: the
-path has no data exchange between ranks); the whole-job time is the slowest
-rank's, reduced with an all-reduce MAX.
+The whole-job time of a multi-GPU run is the slowest rank's, reduced with an
+all-reduce MAX (the chain exchange itself is tested in test_sharding_cpu.py).
 """
 import os
 import socket
