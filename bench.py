@@ -339,6 +339,17 @@ def run_linear(args):
     torch.cuda.synchronize()
     t64 = sum(a.elapsed_time(b) for a, b in e64) / len(e64) / 1e3
     model.tensor_cores = True
+    # error of the tensor-core evaluation against the FP64 CUDA-core one (which matches the
+    # numpy FP64 oracle to 1e-10 in the tests): the timed prior draws and draws near the truth
+    errs = {}
+    post = torch.from_numpy(np.clip(truth[None, :] + 1e-3 * rng.normal(size=(N, P)), -1, 1)).cuda()
+    for name, th in (("prior_draws", theta), ("near_truth", post)):
+        tc, f64 = torch.empty_like(out), torch.empty_like(out)
+        model.forward(th, tc)
+        model.tensor_cores = False
+        model.forward(th, f64)
+        model.tensor_cores = True
+        errs[name] = float(((tc - f64).abs() / f64.abs()).max().item())
     if rank == 0:
         print(json.dumps({
             "metric": "linear-model llk evaluations/s", "value": world * N / t, "unit": "chain-llk/s",
@@ -352,6 +363,8 @@ def run_linear(args):
                          "executed_frac": executed / t / 1e12 / peak,
                          "note": "achieved counts 2·M·P·N; the split-BF16 GEMM executes 3x that"},
             "fp64_cuda_cores_ms": t64 * 1e3,
+            "llk_max_rel_err_vs_fp64": dict(errs, reference="FP64 CUDA-core evaluation of every chain "
+                                                            "(ag_linear_llk_fp64)"),
             "clocks": clk.summary()}))
     return 0
 
@@ -511,6 +524,17 @@ def run_dense(args):
     t = sum(a.elapsed_time(b) for a, b in evs) / len(evs) / 1e3
     t = max_over_ranks(t, dist, device="cuda")
     assert int(model.flags.item()) == 0, "device wait timed out"
+    # error of the split-BF16 whitening against FP64 (W r with the FP64 W and the same FP32
+    # residual rows) on 256 evenly spaced chains
+    model.forward(theta, out)
+    sub = torch.arange(0, N, max(1, N // 256), device=dev)[:256]
+    r = model._resid[sub].double()
+    ref = torch.full((sub.numel(),), model.normalization, dtype=torch.float64, device=dev)
+    for (W, _), blk in zip(model._w, model.blocks):
+        z = r[:, blk.col0:blk.col0 + blk.m] @ W.T
+        ref -= 0.5 * (z * z).sum(1)
+    torch.cuda.synchronize()
+    whiten_err = float(((out[sub] - ref).abs() / ref.abs()).max().item())
     whiten = sum(2.0 * m * m * N for m in sizes)                 # W (r - r̄) per dataset block
     pk = peaks()
     peak = float(pk.get("bf16_tflops", 1900.0))
@@ -527,6 +551,9 @@ def run_dense(args):
                          "frac": whiten / t / 1e12 / peak,
                          "note": "achieved counts the whitening 2·Σ M_k²·N; the split-BF16 GEMM executes 3x "
                                  "that, and the time includes the Mogi forward launch"},
+            "llk_max_rel_err_vs_fp64": {"whitening": whiten_err, "chains": int(sub.numel()),
+                                        "reference": "-1/2 |W r|^2 in FP64 (FP64 W = L^-1, the kernel's "
+                                                     "FP32 residual rows)"},
             "clocks": clk.summary()}))
     return 0
 

@@ -49,7 +49,9 @@ def oracle_llk(G, d, Cd, theta):
 
 # the last case has 1,024 tiles of 128 chains x 256 observations: each persistent CTA takes
 # several tiles and reuses both TMEM accumulators
-@pytest.mark.parametrize("m,p,n", [(512, 64, 384), (1024, 256, 1024), (777, 100, 300), (2048, 64, 16384)])
+# (4096, 256, 16384) is the linear-Gaussian workload's size
+@pytest.mark.parametrize("m,p,n", [(512, 64, 384), (1024, 256, 1024), (777, 100, 300), (2048, 64, 16384),
+                                   (4096, 256, 16384)])
 def test_linear_llk_tensor_cores(cuda, m, p, n):
     G, d, Cd, truth = problem(m, p)
     rng = np.random.default_rng(1)
@@ -115,3 +117,53 @@ def test_dense_cd_two_source_mogi(cuda):
         ref += -0.5 * (m * math.log(2 * math.pi) + logdet) - 0.5 * np.einsum("ij,ji->i", r, np.linalg.solve(ds["cd"], r.T))
     err = np.abs(out.cpu().numpy() - ref)
     assert np.all(err <= 1e-4 * np.abs(ref) + 0.5), (err.max(), np.abs(ref).min())
+
+
+def test_dense_cd_workload_size(cuda):
+    """The batched two-source Mogi workload at its stated size: three datasets of 12,000 /
+    30,000 / 7,500 stations with dense exponential Cd and 65,536 chains, evaluated in one
+    forward launch plus the tcgen05 whitening of each block; 256 evenly spaced chains are
+    checked against the FP64 oracle (numpy Mogi, FP64 Cholesky solves) within 1e-4 relative."""
+    from altar_gb300.models import DenseMogi
+    from oracle import catmip
+    rng = np.random.default_rng(5)
+    sizes, loss = (12000, 30000, 7500), ([0.38, -0.08, 0.92], [-0.61, 0.11, 0.78], [0.09, 0.56, 0.82])
+    truth = np.array([-4e3, 1e3, 3e3, 6.3, 3e3, -2e3, 4e3, 6.1])
+    datasets = []
+    for m, l in zip(sizes, loss):
+        xy = torch.from_numpy(rng.uniform(-25e3, 25e3, (m, 2))).cuda()
+        cd = 1.6e-5 * torch.exp(-torch.cdist(xy, xy) / 2e3) + 1e-9 * torch.eye(m, dtype=torch.float64, device="cuda")
+        xy = xy.cpu().numpy()
+        u = catmip.mogi_los(truth[None, :], xy[:, 0], xy[:, 1], np.tile(l, (m, 1)), 0.25, log_strength=True,
+                            nsources=2, stride=4)[0]
+        noise = (torch.linalg.cholesky(cd) @ torch.from_numpy(rng.normal(size=m)).cuda()).cpu().numpy()
+        datasets.append(dict(x=xy[:, 0], y=xy[:, 1], los=l, d=u + noise, cd=cd))
+    psets = {}
+    for sidx in range(2):
+        psets[f"location{sidx}"] = Contiguous(2, Uniform((-1e4, 1e4)))
+        psets[f"depth{sidx}"] = Contiguous(1, Uniform((1e3, 8e3)))
+        psets[f"source{sidx}"] = Contiguous(1, Uniform((5.0, 7.0)))
+    model = DenseMogi(psets, datasets)
+    n = 65536
+    app = _App()
+    app.job.chains = n
+    model.initialize(app)
+    theta = truth[None, :] + rng.normal(size=(n, 8)) * np.tile([500, 500, 300, 0.05], 2)
+    out = torch.empty(n, dtype=torch.float64, device="cuda")
+    model.forward(torch.from_numpy(theta).cuda(), out)
+    torch.cuda.synchronize()
+    assert int(model.flags.item()) == 0
+    sub = np.arange(0, n, n // 256)[:256]
+    ref = np.zeros(sub.size)
+    for ds, m in zip(datasets, sizes):
+        u = catmip.mogi_los(theta[sub], ds["x"], ds["y"], np.tile(ds["los"], (m, 1)), 0.25, log_strength=True,
+                            nsources=2, stride=4)
+        r = torch.from_numpy(u - ds["d"][None, :]).cuda()
+        L = torch.linalg.cholesky(ds["cd"])
+        z = torch.linalg.solve_triangular(L, r.T, upper=False)
+        logdet = 2.0 * torch.log(torch.diagonal(L)).sum()
+        ref += (-0.5 * (m * math.log(2 * math.pi) + logdet) - 0.5 * (z * z).sum(0)).cpu().numpy()
+    got = out.cpu().numpy()[sub]
+    rel = np.abs(got - ref) / np.abs(ref)
+    print(f"\ndense-Cd workload size: max rel llk error vs FP64 over {sub.size} chains {rel.max():.2e}")
+    assert np.all(rel <= 1e-4), rel.max()
