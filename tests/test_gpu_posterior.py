@@ -1,0 +1,89 @@
+"""Posterior parity with the oracle CATMIP loop within 2 Monte Carlo standard errors.
+
+The reference (tests/golden/posterior_golden.npz, written by
+tests/golden/make_posterior_golden.py) holds, for seeds 1..K, the summaries of the
+final population of the FP64 oracle loop (oracle/catmip.py, the reference's
+Annealer/COV/Metropolis restated, drawing from the device's Philox streams):
+mean and standard deviation of each parameter (Mogi) or of the mode-independent
+CDM quantities (centroid, depth, opening, sorted semi-axes).
+
+MCSE.  The standard deviation of a summary over the K oracle seeds is the Monte
+Carlo standard error of one run: it is what one run's estimate actually varies
+by, resampling correlation included, with no effective-sample-size assumption.
+The device runs the same K seeds on the same inputs.  For each summary q the
+mean over the K device runs must lie within 2 standard errors of the mean over
+the K oracle runs, the standard error of that difference being
+MCSE(q) · sqrt(2 / K).  (Runs with the same seed share their random streams, so
+device and oracle runs are positively correlated and the bound is conservative.)
+"""
+import os
+
+import numpy as np
+import pytest
+
+from altar_gb300 import Application
+from altar_gb300.bayesian import Annealer
+from altar_gb300.distributions import Uniform
+from altar_gb300.models import CDM, Contiguous, Mogi
+from altar_gb300.models.observations import Observations
+from altar_gb300.simulations import RNG, Job
+
+pytestmark = pytest.mark.gpu
+
+G = np.load(os.path.join(os.path.dirname(__file__), "golden", "posterior_golden.npz"))
+LOS = np.array([0.38, -0.08, 0.92])
+
+
+def _compare(name, labels, gpu, ref):
+    K = ref.shape[0]
+    mcse = ref.std(0, ddof=1)
+    se = mcse * np.sqrt(2.0 / K)
+    z = (gpu.mean(0) - ref.mean(0)) / se
+    print(f"\n{name}: K = {K} seeds per side; difference of the seed means in standard errors:")
+    for lab, zz, m, g, r in zip(labels, z, mcse, gpu.mean(0), ref.mean(0)):
+        print(f"  {lab:>14s}  device {g: .6e}  oracle {r: .6e}  MCSE {m:.3e}  z {zz:+.2f}")
+    return z
+
+
+def test_mogi_posterior_within_2_mcse(cuda):
+    X, Y, d = G["mogi_X"], G["mogi_Y"], G["mogi_d"]
+    ref = G["mogi_summaries"]
+    psets = {"location": Contiguous(2, Uniform((-1e4, 1e4))), "depth": Contiguous(1, Uniform((1e3, 8e3))),
+             "source": Contiguous(1, Uniform((1e5, 1e7)))}
+    rows, stages = [], []
+    for seed in range(1, ref.shape[0] + 1):
+        model = Mogi(psets, observations=Observations(X, Y, np.tile(LOS, (X.size, 1)), d, 2.5e-5),
+                     log_strength=False)
+        app = Application(model, job=Job(chains=1024, steps=5), rng=RNG(seed), controller=Annealer())
+        app.run()
+        th = app.controller.worker.step.theta.cpu().numpy()
+        assert app.controller.worker.step.beta == 1.0
+        rows.append(np.concatenate([th.mean(0), th.std(0)]))
+        stages.append(len(app.controller.worker.reports))
+    labels = [f"mean {p}" for p in ("x", "y", "depth", "dV")] + [f"sd {p}" for p in ("x", "y", "depth", "dV")]
+    z = _compare("Mogi workload", labels, np.array(rows), ref)
+    print(f"  stages: device {np.mean(stages):.1f}, oracle {G['mogi_stages'].mean():.1f}")
+    assert np.all(np.abs(z) <= 2.0), z
+
+
+def test_cdm_posterior_within_2_mcse(cuda):
+    X, Y, d = G["cdm_X"], G["cdm_Y"], G["cdm_d"]
+    ref = G["cdm_summaries"]
+    psets = {"location": Contiguous(2, Uniform((-1e4, 1e4))), "depth": Contiguous(1, Uniform((1e3, 1e4))),
+             "opening": Contiguous(1, Uniform((-50, 50))), "a": Contiguous(3, Uniform((100, 3000))),
+             "omega": Contiguous(3, Uniform((-90, 90)))}
+    rows, stages = [], []
+    for seed in range(1, ref.shape[0] + 1):
+        model = CDM(psets, observations=Observations(X, Y, np.tile(LOS, (X.size, 1)), d, 9e-6))
+        app = Application(model, job=Job(chains=2048, steps=5), rng=RNG(seed), controller=Annealer())
+        app.run()
+        th = app.controller.worker.step.theta.cpu().numpy()
+        assert app.controller.worker.step.beta == 1.0
+        q = np.concatenate([th[:, 0:4], np.sort(th[:, 4:7], axis=1)], axis=1)
+        rows.append(np.concatenate([q.mean(0), q.std(0)]))
+        stages.append(len(app.controller.worker.reports))
+    names = ("x", "y", "depth", "opening", "a_min", "a_mid", "a_max")
+    labels = [f"mean {p}" for p in names] + [f"sd {p}" for p in names]
+    z = _compare("CDM, 576 stations, 2,048 chains", labels, np.array(rows), ref)
+    print(f"  stages: device {np.mean(stages):.1f}, oracle {G['cdm_stages'].mean():.1f}")
+    assert np.all(np.abs(z) <= 2.0), z
