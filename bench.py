@@ -558,6 +558,60 @@ def run_dense(args):
     return 0
 
 
+def run_sweep(args, X, Y, los, d, N, rank):
+    """Time to β = 1 at equal posterior.  Plain Metropolis with each of --sweep-steps steps
+    per stage and the coarse-model delayed-acceptance sampler (stage 1 the exact CDM on every
+    32nd/16th/8th station, two rounds of 10 stage-1 moves and an exact correction per stage)
+    run over --seeds.  The reference posterior is the longest plain walk.  For each sampler
+    and each mode-independent summary (the means of centroid, depth, opening and sorted
+    semi-axes), z = (seed mean - reference seed mean) / sqrt(s²/K + s_ref²/K), s the spread
+    of the summary over a sampler's K seeds (one run's Monte Carlo standard error).  A sampler
+    reaches the posterior when every |z| <= 2; the speed-up is the time of the cheapest plain
+    walk that reaches it over the delayed-acceptance time."""
+    import torch
+    seeds = args.seeds
+    anneal("plain", X, Y, los, d, N, rank, args, seed=1, max_stages=3)        # one-time costs
+    runs = {}
+    for steps in args.sweep_steps:
+        args.walk_steps = steps
+        runs[f"plain{steps}"] = [anneal("plain", X, Y, los, d, N, rank, args, seed=sd) for sd in seeds]
+    args.walk_steps = 5
+    args.surrogate, args.subset_strides, args.da_inner, args.da_outer = "subset", [32, 16, 8], 10, 2
+    args.subset_inner, args.delta_limit, args.da_stop_beta = None, 1.0, 1.0
+    anneal("da", X, Y, los, d, N, rank, args, seed=1, max_stages=3)
+    runs["da"] = [anneal("da", X, Y, los, d, N, rank, args, seed=sd) for sd in seeds]
+    torch.cuda.synchronize()
+    names = runs["da"][0]["invariants"]["names"]
+    stats = {}
+    for key, rs in runs.items():
+        m = np.array([r["invariants"]["mean"] for r in rs])
+        stats[key] = (m.mean(0), m.std(0, ddof=1) if len(rs) > 1 else np.zeros(m.shape[1]),
+                      float(np.mean([r["time_s"] for r in rs])), float(np.mean([r["stages"] for r in rs])))
+    ref_key = f"plain{max(args.sweep_steps)}"
+    mref, sref, _, _ = stats[ref_key]
+    K = len(seeds)
+    out = {}
+    for key, (m, sdev, t, st) in stats.items():
+        z = (m - mref) / np.sqrt((sdev ** 2 + sref ** 2) / K + 1e-300)
+        out[key] = {"time_s": t, "stages": st, "z": z.tolist(),
+                    "reaches": bool(key == ref_key or np.all(np.abs(z) <= 2.0)),
+                    "times_s": [r["time_s"] for r in runs[key]]}
+    plain_ok = [k for k in out if k.startswith("plain") and out[k]["reaches"]]
+    cheapest = min(plain_ok, key=lambda k: out[k]["time_s"])
+    line = {"metric": "CDM time-to-beta=1 at equal posterior", "unit": "s", "higher_is_better": False,
+            "value": out["da"]["time_s"], "n_gpus": 1, "data": "synthetic",
+            "config": {"workload": "cdm-40k-obs", "chains": N, "stations": X.size, "seeds": seeds,
+                       "plain_steps_per_stage": args.sweep_steps, "reference": ref_key,
+                       "summaries": names, "criterion": "every |z| <= 2 against the reference's seed mean"},
+            "samplers": out, "cheapest_plain_at_equal_posterior": cheapest,
+            "da_reaches_equal_posterior": out["da"]["reaches"],
+            "speedup_da_vs_plain_at_equal_posterior": out[cheapest]["time_s"] / out["da"]["time_s"],
+            "speedup_da_vs_plain5": out["plain5"]["time_s"] / out["da"]["time_s"] if "plain5" in out else None}
+    if rank == 0:
+        print(json.dumps(line))
+    return 0
+
+
 def run_ours(args):
     import torch
     rank, world, local, dist = dist_setup()
@@ -634,6 +688,9 @@ def run_ours(args):
         if rank == 0:
             print(json.dumps(line))
         return 0
+
+    if args.mode == "sweep":
+        return run_sweep(args, X, Y, los, d, N, rank)
 
     forced = args.variant is not None
     model = CDM(psets, observations=Observations(X, Y, los, d, SIGMA ** 2),
@@ -834,7 +891,10 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--mode", default="walk", choices=["walk", "anneal", "compare", "linear", "dense", "reverso"])
+    ap.add_argument("--mode", default="walk",
+                    choices=["walk", "anneal", "compare", "sweep", "linear", "dense", "reverso"])
+    ap.add_argument("--sweep-steps", type=int, nargs="+", default=[5, 10, 15, 20],
+                    help="sweep mode: Metropolis steps per stage of the plain walks (the longest is the reference)")
     ap.add_argument("--sampler", default="plain", choices=["plain", "da"])
     ap.add_argument("--ref-walk-steps", type=int, default=0,
                     help="compare mode: also run plain Metropolis with this many steps per stage, the "
