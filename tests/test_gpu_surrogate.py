@@ -274,3 +274,51 @@ def test_subset_surrogate_transition_posterior(cuda):
         sd = tp[:, j].std()
         assert abs(td[:, j].mean() - tp[:, j].mean()) < 4 * sd / np.sqrt(2048 / 8), j
         assert abs(td[:, j].std() - sd) < 0.5 * sd, j
+
+
+def test_trained_network_gain(cuda):
+    """What training the network gains.  Two-stage delayed acceptance screens every proposal
+    with the network's log-likelihood and runs the exact model only on the survivors, so its
+    exact cost per accepted move is (exact evaluations) / (accepted moves); plain Metropolis
+    evaluates every proposal inside the prior.  On the Mogi workload, with the network trained
+    on the sampler's own exact evaluations the DA spends fewer exact evaluations per accepted
+    move than plain Metropolis while keeping most of its acceptance; the same sampler with the
+    untrained network (no training passes) screens at random and loses most accepted moves."""
+    g = np.linspace(-15e3, 15e3, 32)
+    X, Y = [a.ravel() for a in np.meshgrid(g, g)]
+    los = np.tile(LOS, (X.size, 1))
+    rng = np.random.default_rng(0)
+    d = catmip.mogi_los(np.array([[0.0, 0.0, 3e3, 2e6]]), X, Y, los, 0.25, log_strength=False)[0]
+    d = d + rng.normal(0, 5e-3, X.size)
+
+    def run(sampler):
+        psets = {"location": Contiguous(2, Uniform((-1e4, 1e4))), "depth": Contiguous(1, Uniform((1e3, 8e3))),
+                 "source": Contiguous(1, Uniform((1e5, 1e7)))}
+        model = Mogi(psets, observations=Observations(X, Y, los, d, 2.5e-5), log_strength=False)
+        app = Application(model, job=Job(chains=2048, steps=5), rng=RNG(7), controller=Annealer(sampler=sampler))
+        app.run()
+        return app.controller.worker.reports
+
+    def da(epochs):
+        sur = Surrogate((4, 128, 128, 32), seed=2, batch=512, lr=2e-3)
+        return DelayedAcceptance(surrogate=sur, rms_limit=1e9, delta_limit=float("inf"), fit_chains=1024,
+                                 check_chains=128, epochs=epochs, refit_epochs=epochs, inner=1, outer=None,
+                                 stop_beta=1.0)
+
+    def figures(reps, mode=None):
+        sel = [r for r in reps if mode is None or r.get("mode") == mode]
+        acc = sum(r["accepted"] for r in sel)
+        prop = sum(r["accepted"] + r["rejected"] + r["unlikely"] for r in sel)
+        exact = sum(r["screened"] for r in sel) if mode else sum(r["accepted"] + r["unlikely"] for r in sel)
+        return exact / max(acc, 1), acc / max(prop, 1), len(sel)
+
+    plain = figures(run(None))
+    trained = figures(run(da(20)), "da")
+    untrained = figures(run(da(0)), "da")
+    print(f"\nexact evaluations per accepted move / acceptance / stages: plain {plain[0]:.2f} / {plain[1]:.3f} / "
+          f"{plain[2]}, trained {trained[0]:.2f} / {trained[1]:.3f} / {trained[2]}, untrained {untrained[0]:.2f} / "
+          f"{untrained[1]:.3f} / {untrained[2]}")
+    assert trained[2] > 0 and untrained[2] > 0
+    assert trained[0] < 0.8 * plain[0]                  # fewer exact evaluations per useful move
+    assert trained[1] > 0.5 * plain[1]                  # most of plain's acceptance kept
+    assert untrained[1] < 0.5 * trained[1]              # without training the screen discards good moves
