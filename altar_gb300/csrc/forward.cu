@@ -51,16 +51,34 @@ struct __align__(16) ChainC {
 };
 static_assert(sizeof(ChainC) % 16 == 0, "ChainC must be a whole number of float4");
 
-// One thread per requested chain (all n, or the first *count_in of index_in).  Chains that
-// are masked or lie above the free surface get their status and nothing else; every other
-// chain takes the next compacted slot (slot order is the order of the atomic, which does not
-// affect any chain's result) and writes its constants there, so the likelihood kernel's CTAs
-// hold only chains with work.
-__global__ void cdm_setup_kernel(ag_layout L, const double* __restrict__ theta, int n,
-                                 const uint32_t* __restrict__ mask_in, ChainC* __restrict__ out,
-                                 uint32_t* __restrict__ chain_status, int noffsets,
-                                 const int32_t* __restrict__ index_in, const int32_t* __restrict__ count_in,
-                                 int32_t* __restrict__ index_out, int32_t* __restrict__ count_out) {
+// Chain slots ordered by cost.  The chains of one CTA share its ring of station tiles, so a
+// CTA advances at the pace of its most expensive chain; with rectangles integrated by
+// quadrature the work of a chain ranges from ~1,500 to ~3,300 FLOP per station.  The set-up
+// therefore runs in two passes: cdm_cost_kernel classifies every requested chain (masked,
+// above the free surface, or the cost bucket of its plan) and counts the chains per bucket;
+// cdm_setup_kernel gives each chain the next slot of its bucket, buckets in decreasing cost,
+// so the CTAs hold chains of similar cost and the expensive ones are scheduled first.
+constexpr int kCostBuckets = 64;
+constexpr int kCostBucketFlop = 96;      // FLOP per station per bucket
+
+struct SetupHdr {                        // in the workspace, cleared before each set-up
+    int32_t nslots;
+    int32_t pad[31];
+    int32_t hist[kCostBuckets];          // chains per cost bucket
+    int32_t fill[kCostBuckets];          // slots handed out per bucket
+};
+
+__device__ __forceinline__ int cost_bucket(uint32_t flop) {
+    const int b = (int)(flop / kCostBucketFlop);
+    return b < kCostBuckets - 1 ? b : kCostBuckets - 1;
+}
+
+// One thread per requested chain (all n, or the first *count_in of index_in): -1 for a masked
+// chain, -2 (and the status bit) for one above the free surface, else its cost bucket
+__global__ void cdm_cost_kernel(ag_layout L, const double* __restrict__ theta, int n,
+                                const uint32_t* __restrict__ mask_in, uint32_t* __restrict__ chain_status,
+                                const int32_t* __restrict__ index_in, const int32_t* __restrict__ count_in,
+                                int8_t* __restrict__ key, SetupHdr* __restrict__ hdr) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
     int i = t;
@@ -68,15 +86,55 @@ __global__ void cdm_setup_kernel(ag_layout L, const double* __restrict__ theta, 
         if (t >= *count_in) return;
         i = index_in[t];
     }
-    if (mask_in && mask_in[i]) return;
-    const double* th = theta + (size_t)i * L.nparams;
-    Vec3 V[3][4];
-    const bool above = cdm_corners(th, L, V);
-    if (above) {
-        if (chain_status) chain_status[i] |= CHAIN_ABOVE_SURFACE;
+    if (mask_in && mask_in[i]) {
+        key[t] = -1;
         return;
     }
-    const int slot = atomicAdd(count_out, 1);
+    const double* th = theta + (size_t)i * L.nparams;
+    Vec3 V[3][4];
+    if (cdm_corners(th, L, V)) {
+        if (chain_status) chain_status[i] |= CHAIN_ABOVE_SURFACE;
+        key[t] = -2;
+        return;
+    }
+    int nq[3][2];
+    uint32_t flop, sfu;
+    cdm_work(cdm_plan(th, L, V, nq), nq, flop, sfu);
+    const int b = cost_bucket(flop);
+    key[t] = (int8_t)b;
+    atomicAdd(&hdr->hist[b], 1);
+}
+
+// Every chain with work takes the next slot of its cost bucket (buckets in decreasing cost;
+// the order inside a bucket is that of the atomic, which does not affect any chain's result)
+// and writes its constants there, so the likelihood kernel's CTAs hold only chains with work.
+__global__ void cdm_setup_kernel(ag_layout L, const double* __restrict__ theta, int n,
+                                 const int8_t* __restrict__ key, ChainC* __restrict__ out, int noffsets,
+                                 const int32_t* __restrict__ index_in, const int32_t* __restrict__ count_in,
+                                 int32_t* __restrict__ index_out, SetupHdr* __restrict__ hdr) {
+    __shared__ int s_start[kCostBuckets];
+    if (threadIdx.x == 0) {
+        int acc = 0;
+        for (int b = kCostBuckets - 1; b >= 0; --b) {
+            s_start[b] = acc;
+            acc += hdr->hist[b];
+        }
+        if (blockIdx.x == 0) hdr->nslots = acc;
+    }
+    __syncthreads();
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    int i = t;
+    if (index_in) {
+        if (t >= *count_in) return;
+        i = index_in[t];
+    }
+    const int b = key[t];
+    if (b < 0) return;
+    const double* th = theta + (size_t)i * L.nparams;
+    Vec3 V[3][4];
+    cdm_corners(th, L, V);
+    const int slot = s_start[b] + atomicAdd(&hdr->fill[b], 1);
     index_out[slot] = i;
     ChainC& C = out[slot];
     C.side_mask = 0u;
@@ -397,12 +455,14 @@ static constexpr int kMogiChains = 16;
 
 extern "C" int32_t ag_forward_variants(int model) { return model == AG_MODEL_CDM ? kCdmVariantCount : 1; }
 
-// CDM workspace: compacted chain constants, the chain of each slot, the slot count
+// CDM workspace: compacted chain constants, the chain of each slot, the set-up header (slot
+// count and cost histogram), each requested chain's cost bucket
 static size_t al256(size_t b) { return (b + 255) / 256 * 256; }
 
 extern "C" size_t ag_forward_workspace_bytes(int model, int32_t n) {
     if (model == AG_MODEL_CDM && n > 0)
-        return al256((size_t)n * sizeof(ChainC)) + al256((size_t)n * sizeof(int32_t)) + 256;
+        return al256((size_t)n * sizeof(ChainC)) + al256((size_t)n * sizeof(int32_t)) + al256(sizeof(SetupHdr)) +
+               al256((size_t)n);
     return 0;
 }
 
@@ -451,12 +511,17 @@ static int forward_llk(int model, const ag_layout* layout, const double* theta, 
         ChainC* chains = reinterpret_cast<ChainC*>(workspace);
         int32_t* slot_chain = reinterpret_cast<int32_t*>(static_cast<char*>(workspace) +
                                                          al256((size_t)n * sizeof(ChainC)));
-        int32_t* nslots = reinterpret_cast<int32_t*>(reinterpret_cast<char*>(slot_chain) +
-                                                     al256((size_t)n * sizeof(int32_t)));
-        rc = cuda_status(cudaMemsetAsync(nslots, 0, sizeof(int32_t), s), "cudaMemsetAsync(slot count)");
+        SetupHdr* hdr = reinterpret_cast<SetupHdr*>(reinterpret_cast<char*>(slot_chain) +
+                                                    al256((size_t)n * sizeof(int32_t)));
+        int8_t* key = reinterpret_cast<int8_t*>(reinterpret_cast<char*>(hdr) + al256(sizeof(SetupHdr)));
+        int32_t* nslots = &hdr->nslots;
+        rc = cuda_status(cudaMemsetAsync(hdr, 0, sizeof(SetupHdr), s), "cudaMemsetAsync(set-up header)");
         if (rc) return rc;
-        cdm_setup_kernel<<<(n + 127) / 128, 128, 0, s>>>(L, theta, n, mask_in, chains, chain_status, noffsets,
-                                                         index, count, slot_chain, nslots);
+        cdm_cost_kernel<<<(n + 127) / 128, 128, 0, s>>>(L, theta, n, mask_in, chain_status, index, count, key, hdr);
+        rc = launch_status("cdm_cost_kernel");
+        if (rc) return rc;
+        cdm_setup_kernel<<<(n + 127) / 128, 128, 0, s>>>(L, theta, n, key, chains, noffsets, index, count,
+                                                         slot_chain, hdr);
         rc = launch_status("cdm_setup_kernel");
         if (rc) return rc;
         const int v = L.variant;
