@@ -56,13 +56,19 @@ class Annealer:
             while worker.beta + tolerance < 1 and stages < max_stages:
                 d.notify(event=d.betaStart, controller=self)
                 worker.top(annealer=self)
-                worker.cool(annealer=self)
-                d.notify(event=d.walkChainsStart, controller=self)
-                statistics = worker.walk(annealer=self)
-                d.notify(event=d.walkChainsFinish, controller=self)
-                d.notify(event=d.resampleStart, controller=self)
-                worker.resample(annealer=self, statistics=statistics)
-                d.notify(event=d.resampleFinish, controller=self)
+                if worker.fusable(self):
+                    # the whole stage replays as one graph; the phase events mark its launch
+                    worker.stage(annealer=self)
+                    for ev in (d.walkChainsStart, d.walkChainsFinish, d.resampleStart, d.resampleFinish):
+                        d.notify(event=ev, controller=self)
+                else:
+                    worker.cool(annealer=self)
+                    d.notify(event=d.walkChainsStart, controller=self)
+                    statistics = worker.walk(annealer=self)
+                    d.notify(event=d.walkChainsFinish, controller=self)
+                    d.notify(event=d.resampleStart, controller=self)
+                    worker.resample(annealer=self, statistics=statistics)
+                    d.notify(event=d.resampleFinish, controller=self)
                 worker.bottom(annealer=self)
                 d.notify(event=d.betaFinish, controller=self)
                 stages += 1

@@ -4,8 +4,11 @@ AnnealingMethod.py:55-147).
 Each phase of a stage (cool, walk, resample) is a fixed sequence of C-ABI
 launches whose stage-dependent inputs (β, scaling, Σ, the random-stream
 epoch) live on the device.  After one eager stage has allocated every
-buffer, each phase is captured once into a CUDA graph and replayed for all
-later stages; the host only reads β (and the stage report) once per stage.
+buffer, the launches are captured into CUDA graphs and replayed for all
+later stages: the whole stage as one graph when the sampler's walk is the
+same every stage (plain Metropolis), else one graph per phase (the
+delayed-acceptance walks change with per-stage host decisions).  The host
+only reads β (and the stage report) once per stage.
 """
 import ctypes
 import logging
@@ -30,6 +33,7 @@ class CUDAAnnealing:
         self.stream = None
         self._graphs = {}
         self._eager_done = set()
+        self._last_bufs = None
         self.reports = []
 
     def initialize(self, application):
@@ -82,6 +86,35 @@ class CUDAAnnealing:
             ex = self._graphs[name] = handle
         _native.call("ag_graph_launch", ex, stream_handle())
         return None
+
+    def fusable(self, annealer):
+        """Whether the whole stage can replay as one graph."""
+        return (not self._eager() and getattr(annealer.sampler, "static_walk", False)
+                and ("cool" in self._eager_done or "stage" in self._graphs))
+
+    def stage(self, annealer):
+        """cool, walk and resample; one captured graph for the whole stage where possible."""
+        if not self.fusable(annealer):
+            self.cool(annealer)
+            stats = self.walk(annealer)
+            self.resample(annealer, stats)
+            return self
+        st = self.step.state
+        if self._last_bufs is None:
+            self._last_bufs = (st.scalars.clone(), st.counters.clone(), st.flags.clone())
+
+        def run():
+            annealer.scheduler.update(step=self.step)
+            annealer.sampler.samplePosterior(annealer=annealer, step=self.step)
+            for dst, src in zip(self._last_bufs, (st.scalars, st.counters, st.flags)):
+                dst.copy_(src)
+            annealer.sampler.resample(annealer=annealer, statistics=st.counters)
+
+        self._eager_done.add("stage")           # the first fused stage is captured directly
+        self._phase("stage", run)
+        self._last = self._last_bufs
+        self.iteration += 1
+        return self
 
     def cool(self, annealer):
         self._phase("cool", lambda: annealer.scheduler.update(step=self.step))

@@ -39,6 +39,8 @@ class Metropolis:
     capturable = True
     # each chain's walk depends on its own row and global index only: a rank can walk a block
     shardable = True
+    # the walk's launches are the same every stage: a whole stage can replay as one graph
+    static_walk = True
 
     def prepare(self, annealer, step):
         return self

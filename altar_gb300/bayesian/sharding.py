@@ -19,13 +19,9 @@ reproduces it bit for bit.  (The reference instead seeds each worker's
 generator separately, MPIAnnealing.py:39-41.)  The collectives work on any
 torch.distributed backend: NCCL for device tensors, gloo for host tensors.
 """
-import ctypes
-
 import torch
 
-from .. import _native
 from .annealing import CUDAAnnealing
-from .coolingstep import CoolingStep
 
 
 class ChainShards:
@@ -106,6 +102,9 @@ class ShardedAnnealing(CUDAAnnealing):
         super().__init__(annealer, graphs=graphs, wid=shards.rank)
         self.shards = shards
         self.block = None
+
+    def fusable(self, annealer):
+        return False                            # the walk is followed by collectives
 
     def start(self, annealer):
         super().start(annealer)

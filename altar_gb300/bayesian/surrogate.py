@@ -289,6 +289,10 @@ class SubsetSurrogate:
 class DelayedAcceptance(Metropolis):
     """Metropolis with a surrogate screen (stage 1) before the exact model (stage 2)."""
 
+    # the walk changes with per-stage host decisions; it does not shard
+    static_walk = False
+    shardable = False
+
     def __init__(self, surrogate=None, rms_limit=0.5, delta_limit=2.0, fit_chains=4096, check_chains=256,
                  epochs=40, refit_epochs=None, start_beta=0.0, stop_beta=0.1, retry_every=3, spread=3.0,
                  inner=10, outer=1, screen_limit=None, **kwds):

@@ -713,9 +713,7 @@ def run_ours(args):
         worker.start(annealer=ann)
 
         def stage():
-            worker.cool(annealer=ann)
-            stats = worker.walk(annealer=ann)
-            worker.resample(annealer=ann, statistics=stats)
+            worker.stage(annealer=ann)              # one graph per stage after the first
 
         flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
         for _ in range(args.warmup):                 # first stage eager, then captured graphs
@@ -837,9 +835,9 @@ def run_ours(args):
                                     "(MEASURED_PEAKS.json has no FP32 figure)"},
         "e2e": {"value": world * N * S / t_e2e, "unit": "chain-steps/s", "h2d_bytes_per_step": io_bytes,
                 "d2h_bytes_per_step": io_bytes},
-        # per stage: 28 COV schedule + 3 Σ + 5 resampling + cholesky + adapt, and per Metropolis
-        # step propose, CDM set-up, CDM likelihood, accept
-        "gpu_launches": (38 + 4 * S) * args.steps,
+        # per stage (one CUDA graph): 28 COV schedule + 3 Σ + 5 resampling + cholesky + adapt, and
+        # per Metropolis step propose, CDM cost classes, CDM set-up, CDM likelihood, accept
+        "gpu_launches": (38 + 5 * S) * args.steps,
         "cpu_baseline": {"value": cpu_rate, "unit": "chain-steps/s", "cores": cores, "kind": "port",
                          "sample": f"{args.cpu_chains} chains x {X.size} stations, likelihood only, "
                                    f"{cpu_dt:.1f} s (FP64 C restatement of models/cdm/cdm/libcdm.py)"},
