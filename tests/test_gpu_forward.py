@@ -289,9 +289,9 @@ def test_cdm_dense_cd_from_case_files(cuda, tmp_path):
     """A case directory with a dense cd.txt (models/cdm/cdm/CDM.py:275-355): the reader keeps
     Cd dense, the fused kernel writes residual rows and the tcgen05 whitening adds
     -1/2 rᵀ Cd⁻¹ r.  Checked against FP64: (1) given the kernel's own FP32 residual rows,
-    llk = -1/2 (M log 2π + log det Cd + rᵀ Cd⁻¹ r) within 1e-5 relative for a population near
-    the truth and 1e-4 for prior draws (the split-BF16 whitening); (2) end to end for prior
-    draws within 1e-4 relative.  Near the
+    llk = -1/2 (M log 2π + log det Cd + rᵀ Cd⁻¹ r) within 1e-5 relative + 0.05 for a population
+    near the truth and 1e-4 relative for prior draws (the split-BF16 whitening, as the linear
+    model's tests); (2) end to end for prior draws within 1e-4 relative.  Near the
     truth the misfit is small and the FP32 forward error (~3e-6 of the field) amplified by
     L⁻¹ dominates the end-to-end difference, so those chains are held to (1)."""
     import math
@@ -325,14 +325,15 @@ def test_cdm_dense_cd_from_case_files(cuda, tmp_path):
 
     # one population per call, as the sampler evaluates them (the whitening centres the residual
     # rows on the population's mean before the split-BF16 product)
-    for theta, rel_given in ((near, 1e-5), (prior, 1e-4)):
+    for theta, rel_given, abs_given in ((near, 1e-5, 0.05), (prior, 1e-4, 0.0)):
         out = torch.empty(theta.shape[0], dtype=torch.float64, device="cuda")
         res = torch.zeros(theta.shape[0], strat.stations.m_padded, dtype=torch.float32, device="cuda")
         strat.forward(dev(theta), out, residuals=res)
         torch.cuda.synchronize()
         got = out.cpu().numpy()
         given = llk(res.cpu().numpy()[:, :m].astype(np.float64))
-        assert np.all(np.abs(got - given) <= rel_given * np.abs(given)), np.max(np.abs(got - given) / np.abs(given))
+        assert np.all(np.abs(got - given) <= rel_given * np.abs(given) + abs_given), \
+            np.max(np.abs(got - given) / np.abs(given))
     e2e = llk(cdm_los_oracle(prior, x, y, los) - d[None, :])
     rel = np.abs(got - e2e) / np.abs(e2e)
     assert np.all(rel <= 1e-4), rel.max()
