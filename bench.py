@@ -138,8 +138,9 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def cpu_llk_rate(X, Y, los, d, chains, seed=7, threads=None):
-    """C restatement of the reference likelihood on the host cores: chain-steps/s."""
+def cpu_llk_rate(X, Y, los, d, chains, seed=7, threads=None, norm=0.0, values=False):
+    """C restatement of the reference likelihood on the host cores: chain-steps/s (and, with
+    values, the sample and its FP64 log-likelihoods)."""
     from oracle import cdm, cref
     rng = np.random.default_rng(seed)
     rows = []
@@ -153,8 +154,10 @@ def cpu_llk_rate(X, Y, los, d, chains, seed=7, threads=None):
     w = np.full(X.size, 1.0 / SIGMA ** 2)
     cref.load()
     t0 = time.perf_counter()
-    cref.llk(2, theta, lay, X, Y, los, d, w, 0.0, nthreads=threads)
+    llk, _ = cref.llk(2, theta, lay, X, Y, los, d, w, norm, nthreads=threads)
     dt = time.perf_counter() - t0
+    if values:
+        return chains / dt, threads, dt, theta, llk
     return chains / dt, threads, dt
 
 
@@ -801,7 +804,13 @@ def run_ours(args):
 
     if rank != 0:
         return 0
-    cpu_rate, cores, cpu_dt = cpu_llk_rate(X, Y, los, d, args.cpu_chains)
+    cpu_rate, cores, cpu_dt, cpu_theta, cpu_llk = cpu_llk_rate(X, Y, los, d, args.cpu_chains,
+                                                                norm=model.strategy.norm, values=True)
+    # the device's log-likelihoods of the same sample against these FP64 ones (the FP32
+    # forward model's error carried through the misfit)
+    gpu_llk = torch.empty(cpu_theta.shape[0], dtype=torch.float64, device="cuda")
+    model.strategy.forward(torch.from_numpy(cpu_theta).cuda(), gpu_llk)
+    rel = np.abs(gpu_llk.cpu().numpy() - cpu_llk) / np.abs(cpu_llk)
     profile_traffic = None
     try:
         with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
@@ -842,6 +851,9 @@ def run_ours(args):
                          "sample": f"{args.cpu_chains} chains x {X.size} stations, likelihood only, "
                                    f"{cpu_dt:.1f} s (FP64 C restatement of models/cdm/cdm/libcdm.py)"},
         "clocks": clk.summary(),
+        "llk_rel_err_vs_fp64": {"max": float(rel.max()), "median": float(np.median(rel)),
+                                "chains": int(rel.size),
+                                "reference": "FP64 C restatement of libcdm.py (the cpu_baseline sample)"},
         "pair_evals_per_s": value * X.size * evaluated,
         # the rate of full likelihood evaluations (the chain-steps whose proposal stayed in the
         # prior and below the surface): the unit the CPU baseline times
