@@ -152,6 +152,10 @@ _SIGNATURES = {
     "ag_adam_step": (c_int, [ctypes.c_int64, P, P, P, P, c_int32, ctypes.c_float, ctypes.c_float,
                              ctypes.c_float, ctypes.c_float, P, P]),
     "ag_to_bf16": (c_int, [ctypes.c_int64, P, P, P]),
+    "ag_mlp_tc_pack_bytes": (c_size_t, [P]),
+    "ag_mlp_tc_pack": (c_int, [P, P, P, P]),
+    "ag_mlp_tc_workspace_bytes": (c_size_t, [P, c_int32]),
+    "ag_mlp_forward_tc": (c_int, [P, P, P, P, c_int32, P, P, P, c_size_t, P, P]),
     "ag_surrogate_llk": (c_int, [c_int32, c_int32, P, P, P, P, c_double, c_double, P, P]),
     "ag_da_screen": (c_int, [P, c_int32, c_uint64, c_uint32, P, P, P, P, P, P, P, P, P]),
     "ag_da_moved": (c_int, [c_int32, c_int32, P, P, P, P, P, P]),

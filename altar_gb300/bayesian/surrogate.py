@@ -30,7 +30,7 @@ import numpy as np
 import torch
 
 from .. import _native
-from ..device import DEVICE, ptr, stream_handle
+from ..device import DEVICE, ptr, stream_handle, workspace
 from .metropolis import Metropolis
 
 
@@ -54,6 +54,10 @@ class Surrogate:
         self.net = _native.MLP(len(self.sizes) - 1, (ctypes.c_int32 * 9)(*self.sizes))
         self.seed, self.lr, self.batch = seed, lr, batch
         self.params = self.pbf = self.m = self.v = self.grads = None
+        # the tensor-core forward (prediction) needs layer widths that are multiples of 64
+        self.tc = all(s % 64 == 0 for s in self.sizes[1:])
+        self.wpack = None
+        self._tc_flags = None
         self.step_count = 0
         self.basis = None
         self.trained = False
@@ -77,11 +81,26 @@ class Surrogate:
         self.grads = torch.zeros_like(self.params)
         _native.call("ag_to_bf16", p.size, ptr(self.params), ptr(self.pbf), stream_handle())
         self.step_count = 0
+        self.pack()
         return self
 
     def set_params(self, flat):
         self.params.copy_(torch.as_tensor(flat, dtype=torch.float32))
         _native.call("ag_to_bf16", self.params.numel(), ptr(self.params), ptr(self.pbf), stream_handle())
+        self.pack()
+
+    def pack(self):
+        """Weights of the tensor-core forward ([W | W] per layer) from the BF16 copy; the buffer
+        keeps its device address, so captured graphs that predict stay valid."""
+        if not self.tc:
+            return self
+        lib = _native.load()
+        net = ctypes.byref(self.net)
+        if self.wpack is None:
+            self.wpack = workspace(lib.ag_mlp_tc_pack_bytes(net))
+            self._tc_flags = torch.zeros(1, dtype=torch.int32, device=DEVICE)
+        _native.call("ag_mlp_tc_pack", net, ptr(self.pbf), ptr(self.wpack), stream_handle())
+        return self
 
     # ---- PCA basis of the LOS fields
     def fit_basis(self, fields, weight, d, norm, oversample=8):
@@ -183,6 +202,7 @@ class Surrogate:
                 tot += rowloss.double().mean()
             self.losses.append(float(tot) / max(1, n_all // B))
         self.trained = True
+        self.pack()
         return self.losses
 
     # ---- inference
@@ -195,18 +215,25 @@ class Surrogate:
         s = stream_handle()
         b = self.basis
         _native.call("ag_normalize_inputs", ptr(theta), n, p, ptr(lo), ptr(hi), ptr(x), s)
-        _native.call("ag_mlp_forward", ctypes.byref(self.net), ptr(self.params), ptr(self.pbf), ptr(x), n,
-                     ptr(coeff), ptr(acts), s)
+        if self.tc:
+            # tcgen05 layers (split-BF16 activations, FP32 accumulation); no activations kept
+            ws = bufs[3]
+            _native.call("ag_mlp_forward_tc", ctypes.byref(self.net), ptr(self.params), ptr(self.wpack), ptr(x),
+                         n, ptr(coeff), None, ptr(ws), ws.numel(), ptr(self._tc_flags), s)
+        else:
+            _native.call("ag_mlp_forward", ctypes.byref(self.net), ptr(self.params), ptr(self.pbf), ptr(x), n,
+                         ptr(coeff), ptr(acts), s)
         _native.call("ag_surrogate_llk", n, self.k, ptr(coeff), ptr(b["scale"]), ptr(b["G"]), ptr(b["h"]),
                      b["q0"], b["norm"], ptr(out_llk), s)
         return out_llk
 
     def buffers(self, n, p):
         lib = _native.load()
+        net = ctypes.byref(self.net)
         return (torch.empty(n, p, dtype=torch.float32, device=DEVICE),
                 torch.empty(n, self.k, dtype=torch.float32, device=DEVICE),
-                torch.empty(lib.ag_mlp_activation_floats(ctypes.byref(self.net), n), dtype=torch.float32,
-                            device=DEVICE))
+                torch.empty(lib.ag_mlp_activation_floats(net, n), dtype=torch.float32, device=DEVICE),
+                workspace(lib.ag_mlp_tc_workspace_bytes(net, n)) if self.tc else None)
 
     def reconstruct(self, coeff_norm):
         b = self.basis

@@ -23,6 +23,7 @@
 
 #include "common.cuh"
 #include "internal.h"
+#include "tcgen05.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -141,6 +142,225 @@ __global__ void __launch_bounds__(256) gemm_kernel(int M, int N, int K, const fl
         store(m0 + mm, n0 + nn, v);
     }
     cluster.sync();                                     // partial tiles stay alive until all have read them
+}
+
+
+// ---------------------------------------------------------------------------
+// Network layers on the tcgen05 tensor cores (inference).  A layer is
+//     C (n x fo) = X Wᵀ,  then + b and GELU (all but the last layer),
+// with X held as split BF16 rows [x_hi | x_lo] (x ≈ x_hi + x_lo, K' = 2 kp, kp = fi rounded
+// up to 64) and W packed as [W | W] (fo x K', zeros past fi), so one BF16 GEMM over K' gives
+// x_hi W + x_lo W in FP32 accumulators: the activations keep ~16 bits beyond BF16 and the
+// weights are the BF16 copy the SIMT layers read too.  The kernel is the linear model's
+// persistent tcgen05 structure (TMA ring of 128B-swizzled K-major tiles, one thread issuing
+// tcgen05.mma into one of two TMEM accumulators, four epilogue warps reading the other with
+// tcgen05.ld); the epilogue adds the bias, applies GELU and writes the next layer's split
+// BF16 input directly, plus the FP32 pre-activation Z and output Y where asked.
+constexpr int kMlpThreads = 192;
+
+template <int BN>
+struct MlpTc {
+    static constexpr uint32_t B_BYTES = BN * TC_BK * 2;
+    static constexpr uint32_t STAGE = TC_A_BYTES + B_BYTES;
+    static constexpr uint32_t SMEM = TC_STAGES * STAGE + 1024 + 256;
+};
+
+template <int BN>
+__global__ void __launch_bounds__(kMlpThreads, 1)
+mlp_layer_tc_kernel(const __grid_constant__ CUtensorMap map_x,   // n  x K' split BF16 activations
+                    const __grid_constant__ CUtensorMap map_w,   // fo x K' packed BF16 weights
+                    int n, int fo, int kblocks, int mtiles, int ntiles, const float* __restrict__ bias,
+                    int gelu_on, float* __restrict__ Z, float* __restrict__ Y,
+                    __nv_bfloat16* __restrict__ xnext, int kp_next, uint32_t* __restrict__ flags) {
+    constexpr uint32_t STAGE = MlpTc<BN>::STAGE;
+    extern __shared__ uint8_t smem_raw[];
+    const uint32_t raw = smem_addr(smem_raw);
+    const uint32_t base = (raw + 1023u) & ~1023u;
+    uint8_t* gbase = smem_raw + (base - raw);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(gbase + TC_STAGES * STAGE);
+    uint64_t* full = bars;
+    uint64_t* empty = bars + TC_STAGES;
+    uint64_t* tfull = bars + 2 * TC_STAGES;
+    uint64_t* tempty = bars + 2 * TC_STAGES + 2;
+    uint64_t* drain = bars + 2 * TC_STAGES + 4;
+    __shared__ uint32_t s_tmem;
+    __shared__ int s_abort;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int total = mtiles * ntiles;
+    if (threadIdx.x == 0) {
+        for (int st = 0; st < TC_STAGES; ++st) {
+            mbar_init(&full[st], 1);
+            mbar_init(&empty[st], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&tfull[b], 1);
+            mbar_init(&tempty[b], 4);
+        }
+        mbar_init(drain, 1);
+        fence_mbar_init();
+        s_abort = 0;
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     ::"r"(smem_addr(&s_tmem)), "r"(2 * BN) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = s_tmem;
+    auto aborted = [&]() { return *(volatile int*)&s_abort != 0; };
+
+    int issued = 0;
+    if (warp == 0 && lane == 0) {
+        for (int t = blockIdx.x; t < total && !aborted(); t += gridDim.x) {
+            const int mt = t % mtiles, nt = t / mtiles;
+            for (int kb = 0; kb < kblocks; ++kb, ++issued) {
+                const int st = issued % TC_STAGES;
+                if (issued >= TC_STAGES &&
+                    !mbar_wait_bounded(&empty[st], (uint32_t)((issued / TC_STAGES) - 1) & 1u, TC_WAIT)) {
+                    atomicExch(&s_abort, 1);
+                    break;
+                }
+                if (aborted()) break;
+                const uint32_t sa = base + st * STAGE;
+                mbar_arrive_expect_tx(&full[st], STAGE);
+                tma_load_2d(sa, &map_x, kb * TC_BK, mt * TC_BM, smem_addr(&full[st]));
+                tma_load_2d(sa + TC_A_BYTES, &map_w, kb * TC_BK, nt * BN, smem_addr(&full[st]));
+            }
+        }
+    } else if (warp == 1 && lane == 0) {
+        const uint32_t idesc = idesc_bf16(TC_BM, BN);
+        int it = 0, local = 0;
+        for (int t = blockIdx.x; t < total && !aborted(); t += gridDim.x, ++local) {
+            const int b = local & 1;
+            if (local >= 2 && !mbar_wait_bounded(&tempty[b], (uint32_t)((local >> 1) - 1) & 1u, TC_WAIT)) {
+                atomicExch(&s_abort, 1);
+                break;
+            }
+            tc_fence_after();
+            const uint32_t acc_addr = tmem + (uint32_t)(b * BN);
+            bool ok = true;
+            for (int kb = 0; kb < kblocks; ++kb, ++it) {
+                const int st = it % TC_STAGES;
+                if (!mbar_wait_bounded(&full[st], (uint32_t)(it / TC_STAGES) & 1u, TC_WAIT)) {
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t sa = base + st * STAGE;
+                const uint64_t adesc = sw128_desc(sa), bdesc = sw128_desc(sa + TC_A_BYTES);
+#pragma unroll
+                for (int k = 0; k < TC_BK / 16; ++k)
+                    mma_bf16(acc_addr, adesc + 2 * k, bdesc + 2 * k, idesc, (kb > 0 || k > 0) ? 1u : 0u);
+                mma_commit(smem_addr(&empty[st]));
+            }
+            if (!ok) {
+                atomicExch(&s_abort, 1);
+                break;
+            }
+            mma_commit(smem_addr(&tfull[b]));
+        }
+        mma_commit(smem_addr(drain));
+    } else if (warp >= 2) {
+        // epilogue: thread = row of the tile (TMEM lane quarter of this warp)
+        const int quarter = warp & 3;
+        const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
+        int local = 0;
+        for (int t = blockIdx.x; t < total; t += gridDim.x, ++local) {
+            const int b = local & 1;
+            const bool ok = __all_sync(0xffffffffu,
+                                       mbar_wait_bounded(&tfull[b], (uint32_t)(local >> 1) & 1u, TC_WAIT));
+            if (!ok || aborted()) {
+                if (lane == 0) atomicExch(&s_abort, 1);
+                break;
+            }
+            tc_fence_after();
+            const int mt = t % mtiles, nt = t / mtiles;
+            const int n0 = nt * BN;
+            const int row = mt * TC_BM + quarter * 32 + lane;
+            const bool live = row < n;
+#pragma unroll 1
+            for (int c0 = 0; c0 < BN; c0 += 32) {
+                uint32_t r[32];
+                tmem_ld32_nowait(tmem + lane_base + (uint32_t)(b * BN + c0), r);
+                const float bl = __ldg(bias + n0 + c0 + lane);        // fo is a multiple of BN
+                tmem_wait_ld();
+                float z[32], y[32];
+#pragma unroll
+                for (int i = 0; i < 32; ++i) {
+                    z[i] = __uint_as_float(r[i]) + __shfl_sync(0xffffffffu, bl, i);
+                    y[i] = gelu_on ? gelu(z[i]) : z[i];
+                }
+                if (!live) continue;
+                const size_t o = (size_t)row * fo + n0 + c0;
+                if (Z) {
+#pragma unroll
+                    for (int i = 0; i < 32; i += 4)
+                        *reinterpret_cast<float4*>(Z + o + i) = make_float4(z[i], z[i + 1], z[i + 2], z[i + 3]);
+                }
+                if (Y) {
+#pragma unroll
+                    for (int i = 0; i < 32; i += 4)
+                        *reinterpret_cast<float4*>(Y + o + i) = make_float4(y[i], y[i + 1], y[i + 2], y[i + 3]);
+                }
+                if (xnext) {
+                    __nv_bfloat16* hi = xnext + (size_t)row * (2 * kp_next) + n0 + c0;
+                    __nv_bfloat16* lo = hi + kp_next;
+#pragma unroll
+                    for (int i = 0; i < 32; i += 8) {
+                        __align__(16) __nv_bfloat16 h8[8], l8[8];
+#pragma unroll
+                        for (int q = 0; q < 8; ++q) {
+                            h8[q] = __float2bfloat16_rn(y[i + q]);
+                            l8[q] = __float2bfloat16_rn(y[i + q] - __bfloat162float(h8[q]));
+                        }
+                        *reinterpret_cast<uint4*>(hi + i) = *reinterpret_cast<const uint4*>(h8);
+                        *reinterpret_cast<uint4*>(lo + i) = *reinterpret_cast<const uint4*>(l8);
+                    }
+                }
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&tempty[b]);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && aborted()) raise_flag(flags, DEV_ERR_TIMEOUT);
+    if (warp == 0 && lane == 0 && aborted()) {
+        for (int k = (issued > TC_STAGES ? issued - TC_STAGES : 0); k < issued; ++k)
+            mbar_wait_bounded(&full[k % TC_STAGES], (uint32_t)(k / TC_STAGES) & 1u, TC_WAIT);
+    }
+    if (warp == 1) mbar_wait_bounded(drain, 0, TC_WAIT);
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * BN) : "memory");
+    }
+}
+
+// x (n x fi FP32) -> split BF16 rows [x_hi | 0 .. | x_lo | 0 ..] of width 2 kp
+__global__ void split_rows_kernel(const float* __restrict__ x, int n, int fi, int kp,
+                                  __nv_bfloat16* __restrict__ xs) {
+    const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (long)n * kp) return;
+    const int r = (int)(e / kp), k = (int)(e % kp);
+    const float v = (k < fi) ? x[(size_t)r * fi + k] : 0.f;
+    const __nv_bfloat16 h = __float2bfloat16_rn(v);
+    xs[(size_t)r * 2 * kp + k] = h;
+    xs[(size_t)r * 2 * kp + kp + k] = __float2bfloat16_rn(v - __bfloat162float(h));
+}
+
+// W (fo x fi BF16) -> [W | W] of width 2 kp, zeros past fi
+__global__ void pack_weights_kernel(const __nv_bfloat16* __restrict__ w, int fo, int fi, int kp,
+                                    __nv_bfloat16* __restrict__ out) {
+    const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (long)fo * kp) return;
+    const int o = (int)(e / kp), k = (int)(e % kp);
+    const __nv_bfloat16 v = (k < fi) ? w[(size_t)o * fi + k] : __float2bfloat16_rn(0.f);
+    out[(size_t)o * 2 * kp + k] = v;
+    out[(size_t)o * 2 * kp + kp + k] = v;
 }
 
 // θ (FP64, N x p) -> x = 2 (θ - lo)/(hi - lo) - 1 (FP32); optional index list
@@ -426,6 +646,116 @@ extern "C" int ag_mlp_forward(const ag_mlp* net, const float* params, const uint
         if (rc) return rc;
         in = Y;
         a += 2 * (int64_t)n * fo;
+    }
+    return AG_OK;
+}
+
+// ---- tensor-core forward (inference)
+static int mlp_kp(int f) { return (f + 63) / 64 * 64; }
+
+static int check_net_tc(const ag_mlp* net) {
+    int rc = check_net(net);
+    if (rc) return rc;
+    for (int l = 1; l <= net->nlayers; ++l)
+        AG_REQUIRE(net->sizes[l] % 64 == 0, "the tensor-core layers need widths that are multiples of 64 "
+                                            "(layer %d has %d)", l, net->sizes[l]);
+    return AG_OK;
+}
+
+extern "C" size_t ag_mlp_tc_pack_bytes(const ag_mlp* net) {
+    if (check_net_tc(net)) return 0;
+    size_t c = 0;
+    for (int l = 0; l < net->nlayers; ++l) c += (size_t)net->sizes[l + 1] * 2 * mlp_kp(net->sizes[l]) * 2;
+    return c;
+}
+
+extern "C" int ag_mlp_tc_pack(const ag_mlp* net, const uint16_t* wbf16, uint16_t* wpack, void* stream) {
+    int rc = check_net_tc(net);
+    if (rc) return rc;
+    AG_REQUIRE(wbf16 && wpack && aligned(wpack, 256), "invalid arguments (wpack must be 256-byte aligned)");
+    cudaStream_t s = as_stream(stream);
+    int64_t wo[kMaxLayers], bo[kMaxLayers];
+    offsets(net, wo, bo);
+    size_t off = 0;
+    for (int l = 0; l < net->nlayers; ++l) {
+        const int fi = net->sizes[l], fo = net->sizes[l + 1], kp = mlp_kp(fi);
+        pack_weights_kernel<<<nblk((long)fo * kp, 256), 256, 0, s>>>(
+            reinterpret_cast<const __nv_bfloat16*>(wbf16) + wo[l], fo, fi, kp,
+            reinterpret_cast<__nv_bfloat16*>(wpack) + off);
+        rc = launch_status("pack_weights_kernel");
+        if (rc) return rc;
+        off += (size_t)fo * 2 * kp;
+    }
+    return AG_OK;
+}
+
+extern "C" size_t ag_mlp_tc_workspace_bytes(const ag_mlp* net, int32_t n) {
+    if (check_net_tc(net) || n <= 0) return 0;
+    int kmax = 0;
+    for (int l = 0; l < net->nlayers; ++l) kmax = max(kmax, mlp_kp(net->sizes[l]));
+    const size_t one = ((size_t)n * 2 * kmax * 2 + 255) / 256 * 256;
+    return 2 * one;
+}
+
+template <int BN>
+static int mlp_layer_launch(cudaStream_t s, const __nv_bfloat16* xs, int n, int kp, const __nv_bfloat16* w,
+                            int fo, const float* bias, int gelu_on, float* Z, float* Y, __nv_bfloat16* xnext,
+                            int kp_next, uint32_t* flags) {
+    CUtensorMap mx, mw;
+    int rc = make_map(&mx, xs, n, 2 * kp, TC_BM);
+    if (rc) return rc;
+    rc = make_map(&mw, w, fo, 2 * kp, BN);
+    if (rc) return rc;
+    rc = cuda_status(cudaFuncSetAttribute(mlp_layer_tc_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)MlpTc<BN>::SMEM),
+                     "cudaFuncSetAttribute(mlp_layer_tc_kernel)");
+    if (rc) return rc;
+    int sms = 0;
+    rc = sm_count(&sms);
+    if (rc) return rc;
+    const int mtiles = (n + TC_BM - 1) / TC_BM, ntiles = fo / BN, total = mtiles * ntiles;
+    mlp_layer_tc_kernel<BN><<<total < sms ? total : sms, kMlpThreads, MlpTc<BN>::SMEM, s>>>(
+        mx, mw, n, fo, 2 * kp / TC_BK, mtiles, ntiles, bias, gelu_on, Z, Y, xnext, kp_next, flags);
+    return launch_status("mlp_layer_tc_kernel");
+}
+
+extern "C" int ag_mlp_forward_tc(const ag_mlp* net, const float* params, const uint16_t* wpack, const float* x,
+                                 int32_t n, float* out, float* acts, void* workspace, size_t workspace_bytes,
+                                 uint32_t* flags, void* stream) {
+    int rc = check_net_tc(net);
+    if (rc) return rc;
+    AG_REQUIRE(params && wpack && x && out && flags && n > 0, "invalid arguments");
+    AG_REQUIRE(aligned(out, 16) && (acts == nullptr || aligned(acts, 16)) && aligned(wpack, 256),
+               "out and acts must be 16-byte aligned, wpack 256-byte aligned");
+    const size_t need = ag_mlp_tc_workspace_bytes(net, n);
+    AG_REQUIRE(workspace && workspace_bytes >= need && aligned(workspace, 256),
+               "the tensor-core forward needs %zu bytes of 256-byte aligned workspace", need);
+    cudaStream_t s = as_stream(stream);
+    int64_t wo[kMaxLayers], bo[kMaxLayers];
+    offsets(net, wo, bo);
+    __nv_bfloat16* buf[2] = {reinterpret_cast<__nv_bfloat16*>(workspace),
+                             reinterpret_cast<__nv_bfloat16*>(static_cast<char*>(workspace) + need / 2)};
+    const int fi0 = net->sizes[0], kp0 = mlp_kp(fi0);
+    split_rows_kernel<<<nblk((long)n * kp0, 256), 256, 0, s>>>(x, n, fi0, kp0, buf[0]);
+    rc = launch_status("split_rows_kernel");
+    if (rc) return rc;
+    const __nv_bfloat16* w = reinterpret_cast<const __nv_bfloat16*>(wpack);
+    float* a = acts;
+    for (int l = 0; l < net->nlayers; ++l) {
+        const int fi = net->sizes[l], fo = net->sizes[l + 1], kp = mlp_kp(fi);
+        const bool last = (l == net->nlayers - 1);
+        float* Z = (a && !last) ? a : nullptr;
+        float* Y = last ? out : (a ? a + (int64_t)n * fo : nullptr);
+        __nv_bfloat16* xnext = last ? nullptr : buf[(l + 1) & 1];
+        const int kp_next = last ? 0 : mlp_kp(fo);
+        rc = (fo % 256 == 0)
+                 ? mlp_layer_launch<256>(s, buf[l & 1], n, kp, w, fo, params + bo[l], last ? 0 : 1, Z, Y, xnext,
+                                         kp_next, flags)
+                 : mlp_layer_launch<64>(s, buf[l & 1], n, kp, w, fo, params + bo[l], last ? 0 : 1, Z, Y, xnext,
+                                        kp_next, flags);
+        if (rc) return rc;
+        w += (size_t)fo * 2 * kp;
+        if (a) a += 2 * (int64_t)n * fo;
     }
     return AG_OK;
 }

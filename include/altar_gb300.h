@@ -414,6 +414,22 @@ int ag_adam_step(int64_t count, float* params, const float* grads, float* m, flo
                  float lr, float b1, float b2, float eps, uint16_t* params_bf16, void* stream);
 /* BF16 copy of an FP32 buffer */
 int ag_to_bf16(int64_t count, const float* src, uint16_t* dst, void* stream);
+/*
+ * Network forward on the tcgen05 tensor cores (layer widths after the input must be
+ * multiples of 64).  Each layer is one persistent kernel: the activations as split BF16
+ * rows [x_hi | x_lo] against the packed weights [W | W] (ag_mlp_tc_pack, from the BF16
+ * copy), FP32 accumulation in TMEM, bias and GELU in the epilogue, which writes the next
+ * layer's split input.  acts may be NULL (prediction only); otherwise it receives the FP32
+ * pre-activations and outputs in ag_mlp_forward's layout.  workspace:
+ * ag_mlp_tc_workspace_bytes(net, n) bytes, 256-byte aligned; flags: AG_DEV_ERR_TIMEOUT if
+ * a bounded wait gave up.  No counterpart in the reference.
+ */
+size_t ag_mlp_tc_pack_bytes(const ag_mlp* net);
+int ag_mlp_tc_pack(const ag_mlp* net, const uint16_t* wbf16, uint16_t* wpack, void* stream);
+size_t ag_mlp_tc_workspace_bytes(const ag_mlp* net, int32_t n);
+int ag_mlp_forward_tc(const ag_mlp* net, const float* params, const uint16_t* wpack, const float* x, int32_t n,
+                      float* out, float* acts, void* workspace, size_t workspace_bytes, uint32_t* flags,
+                      void* stream);
 /* llk = norm - 1/2 (q0 - 2 hᵀ c̃ + c̃ᵀ G c̃) with c̃ = scale ⊙ coeff (n x k, k <= 96) */
 int ag_surrogate_llk(int32_t n, int32_t k, const float* coeff, const float* scale, const float* gram,
                      const float* h, double q0, double norm, double* llk, void* stream);

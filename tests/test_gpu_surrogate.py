@@ -325,3 +325,42 @@ def test_trained_network_gain(cuda):
     assert trained[0] < 0.9 * untrained[0]
     assert trained[1] > 0.8 * plain[1]                  # most of plain's acceptance kept
     assert trained[1] > 1.2 * untrained[1]              # without training the screen discards good moves
+
+
+@pytest.mark.parametrize("sizes,n", [(SIZES, 1000), (SIZES, 32768), ((10, 64, 128, 64), 300)])
+def test_mlp_forward_tensor_cores(cuda, sizes, n):
+    """The tcgen05 forward (split-BF16 activations against the BF16 weights, FP32
+    accumulation) against the FP64 oracle with the same BF16-rounded weights, within the
+    SIMT forward's tolerance (1e-4 normwise), with and without the FP32 activations kept;
+    row counts that are not multiples of the 128-row tile included."""
+    sur = Surrogate(sizes, seed=5).init_params()
+    assert sur.tc
+    rng = np.random.default_rng(1)
+    x = rng.uniform(-1, 1, (n, sizes[0]))
+    lib = _native.load()
+    net = ctypes.byref(sur.net)
+    xd = dev(x, torch.float32)
+    out = torch.empty(n, sizes[-1], dtype=torch.float32, device="cuda")
+    acts = torch.empty(lib.ag_mlp_activation_floats(net, n), dtype=torch.float32, device="cuda")
+    ws = torch.empty(lib.ag_mlp_tc_workspace_bytes(net, n), dtype=torch.uint8, device="cuda")
+    flags = torch.zeros(1, dtype=torch.int32, device="cuda")
+    s = stream_handle()
+    flat = sur.params.cpu().numpy().astype(np.float64)
+    P, o = [], 0
+    for fi, fo in zip(sizes[:-1], sizes[1:]):
+        W = _bf16_round(flat[o:o + fo * fi].reshape(fo, fi)); o += fo * fi
+        P.append((W, flat[o:o + fo])); o += fo
+    ref, cache = mlp.forward(P, xd.double().cpu().numpy())
+    for keep in (None, acts):
+        out.zero_()
+        _native.call("ag_mlp_forward_tc", net, ptr(sur.params), ptr(sur.wpack), ptr(xd), n, ptr(out), ptr(keep),
+                     ptr(ws), ws.numel(), ptr(flags), s)
+        torch.cuda.synchronize()
+        assert int(flags.item()) == 0
+        got = out.double().cpu().numpy()
+        assert np.max(np.abs(got - ref)) <= 1e-4 * np.max(np.abs(ref)), np.max(np.abs(got - ref))
+    # the kept activations: layer 0's pre-activation and output as the SIMT forward stores them
+    z0 = acts[:n * sizes[1]].double().cpu().numpy().reshape(n, sizes[1])
+    y0 = acts[n * sizes[1]:2 * n * sizes[1]].double().cpu().numpy().reshape(n, sizes[1])
+    assert np.max(np.abs(z0 - cache[0][1])) <= 1e-4 * np.max(np.abs(cache[0][1]))
+    assert np.max(np.abs(y0 - mlp.gelu(cache[0][1]))) <= 1e-4 * np.max(np.abs(cache[0][1]))
