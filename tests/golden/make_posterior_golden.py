@@ -72,7 +72,7 @@ def cdm_case():
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--seeds", type=int, default=8)
-    ap.add_argument("--cdm-seeds", type=int, default=6)
+    ap.add_argument("--cdm-seeds", type=int, default=12)
     ap.add_argument("--out", default=os.path.join(HERE, "posterior_golden.npz"))
     args = ap.parse_args()
     out = {}
