@@ -211,7 +211,7 @@ class Surrogate:
     def predict(self, theta, lo, hi, out_llk, bufs, mask=None):
         """Surrogate data log-likelihood of device θ rows into out_llk (mask: unused)."""
         n, p = theta.shape
-        x, coeff, acts = bufs
+        x, coeff, acts = bufs[0], bufs[1], bufs[2]
         s = stream_handle()
         b = self.basis
         _native.call("ag_normalize_inputs", ptr(theta), n, p, ptr(lo), ptr(hi), ptr(x), s)

@@ -73,6 +73,8 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--seeds", type=int, default=8)
     ap.add_argument("--cdm-seeds", type=int, default=12)
+    ap.add_argument("--cdm-first-seed", type=int, default=1)
+    ap.add_argument("--skip-mogi", action="store_true")
     ap.add_argument("--out", default=os.path.join(HERE, "posterior_golden.npz"))
     args = ap.parse_args()
     out = {}
@@ -86,7 +88,7 @@ def main():
         return catmip.diag_llk(u, d, np.full(X.size, 2.5e-5))[0], np.zeros(th.shape[0], bool)
 
     rows, stages = [], []
-    for seed in range(1, args.seeds + 1):
+    for seed in range(1, 0 if args.skip_mogi else args.seeds + 1):
         r = catmip.Annealing(mogi_llk, lo, hi, chains=1024, steps=5, seed=seed).run()
         rows.append(summaries_mogi(r["theta"]))
         stages.append(len(r["stages"]))
@@ -103,7 +105,7 @@ def main():
         return cref.llk(2, th, layout, X, Y, los.ravel(), d, w, norm, nthreads=os.cpu_count())
 
     rows, stages = [], []
-    for seed in range(1, args.cdm_seeds + 1):
+    for seed in range(args.cdm_first_seed, args.cdm_first_seed + args.cdm_seeds):
         r = catmip.Annealing(cdm_llk, CDM_LO, CDM_HI, chains=2048, steps=5, seed=seed).run()
         rows.append(summaries_cdm(r["theta"]))
         stages.append(len(r["stages"]))

@@ -85,5 +85,9 @@ def test_cdm_posterior_within_2_mcse(cuda):
     names = ("x", "y", "depth", "opening", "a_min", "a_mid", "a_max")
     labels = [f"mean {p}" for p in names] + [f"sd {p}" for p in names]
     z = _compare("CDM, 576 stations, 2,048 chains", labels, np.array(rows), ref)
+    dev_rows = np.array(rows)
+    print("  per seed (device - oracle, same random streams), in MCSE:")
+    for j, lab in enumerate(labels):
+        print(f"  {lab:>14s} " + " ".join("%+.1f" % v for v in (dev_rows[:, j] - ref[:, j]) / ref[:, j].std(ddof=1)))
     print(f"  stages: device {np.mean(stages):.1f}, oracle {G['cdm_stages'].mean():.1f}")
     assert np.all(np.abs(z) <= 2.0), z
