@@ -194,7 +194,7 @@ def test_cdm_llk_given_residuals(cuda):
     # end to end against the FP64 oracle: bounded by the FP32 forward error
     full, _ = catmip.diag_llk(cdm_los_oracle(theta, X, Y, los), d, var)
     rel = np.abs(llk - full) / np.abs(full)
-    assert np.median(rel) < 1e-4
+    assert np.median(rel) < 1e-6 and rel.max() < 1e-5, (np.median(rel), rel.max())
 
 
 def test_cdm_mask_and_surface_status(cuda):
