@@ -451,9 +451,13 @@ using namespace ag;
 struct CdmVariant { int warps; };
 static constexpr CdmVariant kCdmVariants[] = {{8}, {4}, {4}, {2}, {4}, {4}, {2}, {4}, {4}, {4}, {4}};
 static constexpr int kCdmVariantCount = 11;
-static constexpr int kMogiChains = 16;
+// Mogi launch variants: chains per CTA held in registers (16, 8, 32)
+static constexpr int kMogiChainsOf[] = {16, 8, 32};
+static constexpr int kMogiVariantCount = 3;
 
-extern "C" int32_t ag_forward_variants(int model) { return model == AG_MODEL_CDM ? kCdmVariantCount : 1; }
+extern "C" int32_t ag_forward_variants(int model) {
+    return model == AG_MODEL_CDM ? kCdmVariantCount : model == AG_MODEL_MOGI ? kMogiVariantCount : 0;
+}
 
 // CDM workspace: compacted chain constants, the chain of each slot, the set-up header (slot
 // count and cost histogram), each requested chain's cost bucket
@@ -549,15 +553,23 @@ static int forward_llk(int model, const ag_layout* layout, const double* theta, 
     }
     if (model == AG_MODEL_MOGI) {
         AG_REQUIRE(L.nsources == 1 || L.nsources == 2, "1 or 2 Mogi sources are supported");
-        const int grid = (n + kMogiChains - 1) / kMogiChains;
-        if (L.nsources == 1)
-            mogi_llk_kernel<kMogiChains, 1><<<grid, 256, 0, s>>>(
-                L, theta, n, mask_in, xy, ld, st->weight, st->oid, noffsets, st->m, st->m_padded, norm, llk,
-                residuals, index, count);
-        else
-            mogi_llk_kernel<kMogiChains, 2><<<grid, 256, 0, s>>>(
-                L, theta, n, mask_in, xy, ld, st->weight, st->oid, noffsets, st->m, st->m_padded, norm, llk,
-                residuals, index, count);
+        AG_REQUIRE(L.variant >= 0 && L.variant < kMogiVariantCount, "Mogi variant %d out of range [0, %d)",
+                   L.variant, kMogiVariantCount);
+        const int ch = kMogiChainsOf[L.variant];
+        const int grid = (n + ch - 1) / ch;
+#define AG_MOGI_LAUNCH(CH, NS)                                                                               \
+    mogi_llk_kernel<CH, NS><<<grid, 256, 0, s>>>(L, theta, n, mask_in, xy, ld, st->weight, st->oid, noffsets, \
+                                                 st->m, st->m_padded, norm, llk, residuals, index, count)
+        if (L.nsources == 1) {
+            if (ch == 8) AG_MOGI_LAUNCH(8, 1);
+            else if (ch == 32) AG_MOGI_LAUNCH(32, 1);
+            else AG_MOGI_LAUNCH(16, 1);
+        } else {
+            if (ch == 8) AG_MOGI_LAUNCH(8, 2);
+            else if (ch == 32) AG_MOGI_LAUNCH(32, 2);
+            else AG_MOGI_LAUNCH(16, 2);
+        }
+#undef AG_MOGI_LAUNCH
         return launch_status("mogi_llk_kernel");
     }
     return set_error(AG_ERR_ARG, "unknown model %d", model);

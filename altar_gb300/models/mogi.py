@@ -14,8 +14,10 @@ from .observations import Observations
 
 class Mogi(Bayesian):
     def __init__(self, psets, observations=None, case=None, nu=0.25, log_strength=True, sources=1,
-                 **kwds):
+                 autotune=False, **kwds):
         super().__init__(psets=psets, **kwds)
+        self.autotune = bool(autotune)
+        self.tuning = None
         self.nu = float(nu)
         self.log_strength = bool(log_strength)
         self.sources = int(sources)
@@ -42,6 +44,13 @@ class Mogi(Bayesian):
             return _native.Layout(self.parameters, p["location"].offset, p["depth"].offset,
                                   p["source"].offset, -1, -1, off, int(self.log_strength), 1, 0, nu=self.nu)
         raise NotImplementedError("multi-source layouts are built with Mogi.layout_multi")
+
+    def initializeSample(self, step, attempt=0, redraw=None):
+        super().initializeSample(step, attempt=attempt, redraw=redraw)
+        if self.autotune and redraw is None:
+            from ..autotune import tune
+            self.tuning = tune(self.strategy, step.theta)     # chains per CTA of the Mogi kernel
+        return self
 
     def dataLikelihood(self, step):
         self.strategy.dataLikelihood(model=self, step=step)

@@ -264,6 +264,32 @@ def test_mogi_two_sources_log_strength(cuda):
     assert np.all(err < 1e-5), err.max()
 
 
+@pytest.mark.parametrize("nsources", [1, 2])
+def test_mogi_launch_variants_identical(cuda, nsources):
+    """The Mogi launch variants (8, 16 or 32 chains per CTA) differ only in how many chains a
+    CTA holds: each lane accumulates the same stations in the same order, so residuals and
+    log-likelihoods agree bit for bit; the autotuner picks among them."""
+    lib = _native.load()
+    assert lib.ag_forward_variants(_native.AG_MODEL_MOGI) == 3
+    rng = np.random.default_rng(11)
+    X, Y = rng.uniform(-25e3, 25e3, 1000), rng.uniform(-25e3, 25e3, 1000)
+    los = np.tile([0.38, -0.08, 0.92], (X.size, 1))
+    cols = [rng.uniform(-1e4, 1e4, 77), rng.uniform(-1e4, 1e4, 77), rng.uniform(1e3, 8e3, 77),
+            rng.uniform(5, 7, 77)]
+    theta = np.stack(cols * nsources, 1)
+    d = rng.normal(0, 5e-3, X.size)
+    runs = {}
+    for v in range(3):
+        strat, _ = mogi_strategy(X, Y, los, d, np.full(X.size, 2.5e-5), log_strength=True,
+                                 nparams=4 * nsources, nsources=nsources, stride=4 if nsources > 1 else 0)
+        strat.layout.variant = v
+        runs[v] = _residuals(strat, theta, X.size)
+    llk0, res0 = runs[0]
+    for v, (llk, res) in runs.items():
+        np.testing.assert_array_equal(res, res0, err_msg=f"variant {v}")
+        np.testing.assert_array_equal(llk, llk0, err_msg=f"variant {v}")
+
+
 def test_host_buffer_call_pattern(cuda):
     """The reference's call pattern: host θ in, host data log-likelihood out."""
     rng = np.random.default_rng(8)
