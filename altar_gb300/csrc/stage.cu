@@ -276,24 +276,21 @@ __global__ void __launch_bounds__(1024) cov_median_kernel(const double* __restri
     }
 }
 
-// shifted weight moments of one grid point over one chunk of chains
-__global__ void __launch_bounds__(256) cov_eval_kernel(const double* __restrict__ llk, int n,
-                                                       const CovState* __restrict__ S,
-                                                       double* __restrict__ part) {
-    const int pt = blockIdx.y;
-    if (S->done || pt >= S->npts) return;
-    const double g = S->pts[pt];
-    const double med = S->median;
-    const double mx = g * (S->llk_max - med);
+// shifted weight moments Σe and Σe², e = exp(g (llk − median) − g (llk_max − median)), of one
+// chunk of kEvalChunk chains: 256 threads each sum their chains in index order, then the warps'
+// sums are added in warp order
+__device__ void chunk_moments(const double* __restrict__ llk, int n, double g, double med, double llk_max,
+                              int chunk, double* __restrict__ out) {
+    __shared__ double r1[8], r2[8];
+    const double mx = g * (llk_max - med);
     double s1 = 0.0, s2 = 0.0;
-    const int begin = blockIdx.x * kEvalChunk;
+    const int begin = chunk * kEvalChunk;
     const int end = min(n, begin + kEvalChunk);
     for (int i = begin + threadIdx.x; i < end; i += blockDim.x) {
         const double e = exp(g * (llk[i] - med) - mx);
         s1 += e;
         s2 = fma(e, e, s2);
     }
-    __shared__ double r1[8], r2[8];
     s1 = warp_sum(s1);
     s2 = warp_sum(s2);
     if ((threadIdx.x & 31) == 0) {
@@ -307,9 +304,10 @@ __global__ void __launch_bounds__(256) cov_eval_kernel(const double* __restrict_
             a += r1[w];
             b += r2[w];
         }
-        part[((size_t)pt * gridDim.x + blockIdx.x) * 2 + 0] = a;
-        part[((size_t)pt * gridDim.x + blockIdx.x) * 2 + 1] = b;
+        out[0] = a;
+        out[1] = b;
     }
+    __syncthreads();      // r1 and r2 are reused by the next chunk
 }
 
 // COV of the normalised weights from the shifted moments, with the reference's
@@ -324,59 +322,50 @@ __device__ double cov_from_moments(double s1, double s2, double mx, int n) {
     return c;
 }
 
-__global__ void cov_decide_kernel(int n, int nblk, double target, double tol,
-                                  const double* __restrict__ part, CovState* __restrict__ S) {
-    if (threadIdx.x != 0 || S->done) return;
-    double cov[kGridPoints];
-    for (int pt = 0; pt < S->npts; ++pt) {
-        double a = 0.0, b = 0.0;
-        for (int k = 0; k < nblk; ++k) {
-            a += part[((size_t)pt * nblk + k) * 2 + 0];
-            b += part[((size_t)pt * nblk + k) * 2 + 1];
-        }
-        cov[pt] = cov_from_moments(a, b, S->pts[pt] * (S->llk_max - S->median), n);
-    }
+// One level of the grid search (COV.cc:240-326) given the COVs of this round's points: round 0
+// evaluated the full remaining step, later rounds the kGridPoints points of a level.
+__device__ void grid_step(CovState& S, const double* cov, double target, double tol) {
     const double Nbeta = 10.0;
-    if (S->level == 0) {
+    if (S.level == 0) {
         // skip straight to β = 1 (COV.cc:257-268)
-        S->cov_high = cov[0];
+        S.cov_high = cov[0];
         if (cov[0] < target || fabs(cov[0] - target) < tol) {
-            S->done = 1;
-            S->skip = 1;
-            S->dbeta = S->high;
+            S.done = 1;
+            S.skip = 1;
+            S.dbeta = S.high;
             return;
         }
     } else {
         // scan of one level (COV.cc:287-311)
         bool found = false;
         int nb = 0;
-        for (; nb < S->npts; ++nb) {
+        for (; nb < S.npts; ++nb) {
             if (fabs(cov[nb] - target) < tol) { found = true; break; }
             if (cov[nb] >= target) { if (nb == 0) found = true; break; }
         }
-        const double step = S->step;
+        const double step = S.step;
         // a completed scan leaves the reference's accumulator one step past the last
         // point and steps it back (COV.cc:301), which can differ from that point in the
         // last bit
-        const double guess = (nb < S->npts) ? S->pts[nb] : (S->pts[S->npts - 1] + step) - step;
-        S->high = guess;
-        S->low = guess - step;
-        if (found || S->level >= kGridLevels) {
-            S->done = 1;
-            S->dbeta = guess;
+        const double guess = (nb < S.npts) ? S.pts[nb] : (S.pts[S.npts - 1] + step) - step;
+        S.high = guess;
+        S.low = guess - step;
+        if (found || S.level >= kGridLevels) {
+            S.done = 1;
+            S.dbeta = guess;
             return;
         }
     }
     // next level: points low, low + step, ... accumulated as the reference does
-    S->level += 1;
-    const double step = (S->high - S->low) / Nbeta;
-    S->step = step;
-    double g = S->low;
+    S.level += 1;
+    const double step = (S.high - S.low) / Nbeta;
+    S.step = step;
+    double g = S.low;
     for (int k = 0; k < kGridPoints; ++k) {
-        S->pts[k] = g;
+        S.pts[k] = g;
         g += step;
     }
-    S->npts = kGridPoints;
+    S.npts = kGridPoints;
 }
 
 // Brent's minimiser for δβ (COV.cc:58-219).  The reference minimises f(δβ) = (COV − target)²
@@ -386,94 +375,83 @@ __global__ void cov_decide_kernel(int n, int nblk, double target, double tol,
 // iteration itself is Brent's published method (R. P. Brent, "Algorithms for Minimization
 // without Derivatives", 1973, ch. 5, procedure localmin: parabolic interpolation through the
 // three best points, golden-section steps when the parabola is unacceptable) restated here.
-// One call per evaluation round: the COVs of the points of the previous round come in through
-// the partial moments, the next point goes out through S->pts.
+// One call per evaluation round: the COVs of the points of the previous round come in as
+// cov[], the next point goes out through S.pts.
 __device__ inline double brent_metric(double cov, double target) {
     return (cov >= 1e100) ? 1e100 : (cov - target) * (cov - target);
 }
 
-__global__ void cov_brent_kernel(int n, int nblk, double target, double tol, int maxiter,
-                                 const double* __restrict__ part, CovState* __restrict__ S) {
-    if (threadIdx.x != 0 || S->done) return;
-    double cov[2];
-    for (int pt = 0; pt < S->npts && pt < 2; ++pt) {
-        double a = 0.0, b = 0.0;
-        for (int k = 0; k < nblk; ++k) {
-            a += part[((size_t)pt * nblk + k) * 2 + 0];
-            b += part[((size_t)pt * nblk + k) * 2 + 1];
-        }
-        cov[pt] = cov_from_moments(a, b, S->pts[pt] * (S->llk_max - S->median), n);
-    }
+__device__ void brent_step(CovState& S, const double* cov, double target, double tol, int maxiter) {
     const double golden = 0.3819660112501051;      // (3 − √5) / 2
-    if (S->level == 0) {
+    if (S.level == 0) {
         // full remaining step first: skip straight to β = 1 if it meets the target (COV.cc:103-116)
-        S->cov_high = cov[0];
+        S.cov_high = cov[0];
         if (cov[0] < target || fabs(cov[0] - target) < tol) {
-            S->done = 1;
-            S->skip = 1;
-            S->dbeta = S->high;
+            S.done = 1;
+            S.skip = 1;
+            S.dbeta = S.high;
             return;
         }
         // bracket [0, 1 − β], first point the reference's guess, interior point v = w at the
         // golden section of the bracket; both evaluated in the next round
-        S->level = 1;
-        S->a = 0.0;
-        S->b = S->high;
-        S->x = (5.0e-5 < S->high) ? 5.0e-5 : 0.5 * S->high;
-        S->v = S->w = S->a + golden * (S->b - S->a);
-        S->d = S->e = 0.0;
-        S->iter = 0;
-        S->phase = 0;
-        S->pts[0] = S->x;
-        S->pts[1] = S->v;
-        S->npts = 2;
+        S.level = 1;
+        S.a = 0.0;
+        S.b = S.high;
+        S.x = (5.0e-5 < S.high) ? 5.0e-5 : 0.5 * S.high;
+        S.v = S.w = S.a + golden * (S.b - S.a);
+        S.d = S.e = 0.0;
+        S.iter = 0;
+        S.phase = 0;
+        S.pts[0] = S.x;
+        S.pts[1] = S.v;
+        S.npts = 2;
         return;
     }
-    if (S->phase == 0) {
-        S->fx = brent_metric(cov[0], target);
-        S->fv = S->fw = brent_metric(cov[1], target);
-        S->phase = 1;
+    if (S.phase == 0) {
+        S.fx = brent_metric(cov[0], target);
+        S.fv = S.fw = brent_metric(cov[1], target);
+        S.phase = 1;
     } else {
         // fold the new point u into the bracket and the three best points
-        const double u = S->u, fu = brent_metric(cov[0], target);
-        if (fu <= S->fx) {
-            if (u < S->x) S->b = S->x; else S->a = S->x;
-            S->v = S->w; S->fv = S->fw;
-            S->w = S->x; S->fw = S->fx;
-            S->x = u; S->fx = fu;
+        const double u = S.u, fu = brent_metric(cov[0], target);
+        if (fu <= S.fx) {
+            if (u < S.x) S.b = S.x; else S.a = S.x;
+            S.v = S.w; S.fv = S.fw;
+            S.w = S.x; S.fw = S.fx;
+            S.x = u; S.fx = fu;
         } else {
-            if (u < S->x) S->a = u; else S->b = u;
-            if (fu <= S->fw || S->w == S->x) {
-                S->v = S->w; S->fv = S->fw;
-                S->w = u; S->fw = fu;
-            } else if (fu <= S->fv || S->v == S->x || S->v == S->w) {
-                S->v = u; S->fv = fu;
+            if (u < S.x) S.a = u; else S.b = u;
+            if (fu <= S.fw || S.w == S.x) {
+                S.v = S.w; S.fv = S.fw;
+                S.w = u; S.fw = fu;
+            } else if (fu <= S.fv || S.v == S.x || S.v == S.w) {
+                S.v = u; S.fv = fu;
             }
         }
-        S->iter += 1;
+        S.iter += 1;
         // the reference's convergence test is on the COV of the latest point (COV.cc:182)
-        if (fabs(cov[0] - target) < tol || S->iter >= maxiter) {
-            S->done = 1;
-            S->dbeta = S->x;
+        if (fabs(cov[0] - target) < tol || S.iter >= maxiter) {
+            S.done = 1;
+            S.dbeta = S.x;
             return;
         }
     }
     // next point
-    const double x = S->x, a = S->a, b = S->b;
+    const double x = S.x, a = S.a, b = S.b;
     const double xm = 0.5 * (a + b);
     const double tol1 = 1.4901161193847656e-08 * fabs(x) + 1e-15;   // √ε·|x| plus an absolute floor
     const double tol2 = 2.0 * tol1;
     if (fabs(x - xm) <= tol2 - 0.5 * (b - a)) {                     // bracket down to the tolerance
-        S->done = 1;
-        S->dbeta = x;
+        S.done = 1;
+        S.dbeta = x;
         return;
     }
-    double d = S->d, e = S->e;
+    double d = S.d, e = S.e;
     bool parabolic = false;
     if (fabs(e) > tol1) {
-        double r = (x - S->w) * (S->fx - S->fv);
-        double q = (x - S->v) * (S->fx - S->fw);
-        double pp = (x - S->v) * q - (x - S->w) * r;
+        double r = (x - S.w) * (S.fx - S.fv);
+        double q = (x - S.v) * (S.fx - S.fw);
+        double pp = (x - S.v) * q - (x - S.w) * r;
         q = 2.0 * (q - r);
         if (q > 0.0) pp = -pp; else q = -q;
         const double e_prev = e;
@@ -490,70 +468,132 @@ __global__ void cov_brent_kernel(int n, int nblk, double target, double tol, int
         d = golden * e;
     }
     const double u = (fabs(d) >= tol1) ? x + d : x + ((d >= 0.0) ? tol1 : -tol1);
-    S->d = d;
-    S->e = e;
-    S->u = u;
-    S->pts[0] = u;
-    S->npts = 1;
+    S.d = d;
+    S.e = e;
+    S.u = u;
+    S.pts[0] = u;
+    S.npts = 1;
 }
 
-// final weights at the chosen δβ: sums first, then normalise
-__global__ void __launch_bounds__(256) cov_final_sum_kernel(const double* __restrict__ llk, int n,
-                                                            const CovState* __restrict__ S,
-                                                            double* __restrict__ part) {
-    const double g = S->dbeta, med = S->median;
-    const double mx = g * (S->llk_max - med);
-    double s1 = 0.0, s2 = 0.0;
-    const int begin = blockIdx.x * kEvalChunk;
-    const int end = min(n, begin + kEvalChunk);
-    for (int i = begin + threadIdx.x; i < end; i += blockDim.x) {
-        const double e = exp(g * (llk[i] - med) - mx);
-        s1 += e;
-        s2 = fma(e, e, s2);
-    }
-    __shared__ double r1[8], r2[8];
-    s1 = warp_sum(s1);
-    s2 = warp_sum(s2);
-    if ((threadIdx.x & 31) == 0) {
-        r1[threadIdx.x >> 5] = s1;
-        r2[threadIdx.x >> 5] = s2;
-    }
+// Grid-wide barrier of a cooperative launch (every block of the grid is resident).  The
+// barrier words (arrival count, generation) are cleared by the host before the launch and
+// the count returns to zero at every barrier.  A block that waits more than kBarrierLimit
+// polls raises DEV_ERR_TIMEOUT and returns false; every later barrier then gives up too, so a
+// lost block ends the kernel with the flag set instead of hanging it.
+constexpr uint32_t kBarrierLimit = 1u << 22;
+struct __align__(256) GridBarrier {
+    unsigned count;
+    unsigned gen;
+};
+
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ bool grid_sync(GridBarrier* bar, uint32_t* flags) {
+    __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
-        double a = 0.0, b = 0.0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
-            a += r1[w];
-            b += r2[w];
+        const unsigned gen = ld_acquire_gpu(&bar->gen);
+        __threadfence();
+        int ok = 1;
+        if (atomicAdd(&bar->count, 1u) == gridDim.x - 1) {
+            atomicExch(&bar->count, 0u);
+            __threadfence();
+            atomicAdd(&bar->gen, 1u);
+        } else {
+            uint32_t polls = 0;
+            while (ld_acquire_gpu(&bar->gen) == gen) {
+                if (++polls > kBarrierLimit) {
+                    ok = 0;
+                    raise_flag(flags, DEV_ERR_TIMEOUT);
+                    break;
+                }
+                __nanosleep(64);
+            }
         }
-        part[(size_t)blockIdx.x * 2 + 0] = a;
-        part[(size_t)blockIdx.x * 2 + 1] = b;
+        __threadfence();
+        s_ok = ok;
     }
+    __syncthreads();
+    return s_ok != 0;
 }
 
-__global__ void cov_final_state_kernel(int n, int nblk, const double* __restrict__ part,
-                                       CovState* __restrict__ S, double* __restrict__ beta,
-                                       double* __restrict__ dbeta_cov) {
-    if (threadIdx.x != 0) return;
-    double a = 0.0, b = 0.0;
-    for (int k = 0; k < nblk; ++k) {
-        a += part[(size_t)k * 2 + 0];
-        b += part[(size_t)k * 2 + 1];
+// The whole δβ search of one stage and its weights in one cooperative launch (COV.cc:58-368).
+// Each round, the blocks evaluate the (point, chunk) moments of the round's points, meet at a
+// grid barrier, and then every block adds the partials in chunk order and takes the same
+// decision on its own copy of the search state, so a round needs one barrier.  The partials
+// alternate between two buffers, so a block that starts the next round cannot overwrite
+// partials that a slower block is still adding.  Then the moments at the chosen δβ, one more
+// barrier, and the normalised weights.  Sums and decisions are those of one chunk per CTA and
+// a sequential total over the chunks, whatever the grid size.
+template <bool BRENT>
+__global__ void __launch_bounds__(256) cov_schedule_kernel(const double* __restrict__ llk, int n, double target,
+                                                           double tol, int maxiter, int rounds,
+                                                           CovState* __restrict__ S, double* __restrict__ part,
+                                                           GridBarrier* __restrict__ bar, double* __restrict__ beta,
+                                                           double* __restrict__ dbeta_cov, double* __restrict__ w,
+                                                           uint32_t* __restrict__ flags) {
+    __shared__ CovState sS;
+    __shared__ double s_tot[2 * kGridPoints];
+    if (threadIdx.x == 0) sS = *S;        // median, maximum and the first round's point
+    __syncthreads();
+    const int nblk = (n + kEvalChunk - 1) / kEvalChunk;
+    const size_t pbuf = (size_t)kGridPoints * nblk * 2;
+    const double med = sS.median, lmax = sS.llk_max;
+    for (int round = 0; round < rounds && !sS.done; ++round) {
+        double* pr = part + (size_t)(round & 1) * pbuf;
+        const int npts = sS.npts;
+        for (int it = blockIdx.x; it < npts * nblk; it += gridDim.x) {
+            const int pt = it / nblk, c = it - pt * nblk;
+            chunk_moments(llk, n, sS.pts[pt], med, lmax, c, pr + ((size_t)pt * nblk + c) * 2);
+        }
+        if (!grid_sync(bar, flags)) return;
+        if ((int)threadIdx.x < 2 * npts) {
+            const int pt = threadIdx.x >> 1, m = threadIdx.x & 1;
+            double a = 0.0;
+            for (int k = 0; k < nblk; ++k) a += __ldcg(pr + ((size_t)pt * nblk + k) * 2 + m);
+            s_tot[threadIdx.x] = a;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double cov[kGridPoints];
+            for (int pt = 0; pt < npts; ++pt)
+                cov[pt] = cov_from_moments(s_tot[2 * pt], s_tot[2 * pt + 1], sS.pts[pt] * (lmax - med), n);
+            if (BRENT)
+                brent_step(sS, cov, target, tol, maxiter);
+            else
+                grid_step(sS, cov, target, tol);
+        }
+        __syncthreads();
     }
-    S->s1 = a;
-    S->cov = cov_from_moments(a, b, S->dbeta * (S->llk_max - S->median), n);
-    // β bookkeeping (COV.cc:264, 323)
-    *beta = S->skip ? 1.0 : S->beta0 + S->dbeta;
-    dbeta_cov[0] = S->dbeta;
-    dbeta_cov[1] = S->cov;
-}
-
-__global__ void cov_weights_kernel(const double* __restrict__ llk, int n,
-                                   const CovState* __restrict__ S, double* __restrict__ w) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const double g = S->dbeta, med = S->median;
-    const double mx = g * (S->llk_max - med);
-    w[i] = exp(g * (llk[i] - med) - mx) / S->s1;
+    // moments at the chosen δβ, then the state, β, and the normalised weights
+    double* fp = part + 2 * pbuf;
+    const double g = sS.dbeta;
+    for (int c = blockIdx.x; c < nblk; c += gridDim.x) chunk_moments(llk, n, g, med, lmax, c, fp + 2 * c);
+    if (!grid_sync(bar, flags)) return;
+    if (threadIdx.x == 0) {
+        double a = 0.0, b = 0.0;
+        for (int k = 0; k < nblk; ++k) {
+            a += __ldcg(fp + 2 * k);
+            b += __ldcg(fp + 2 * k + 1);
+        }
+        sS.s1 = a;
+        sS.cov = cov_from_moments(a, b, g * (lmax - med), n);
+        if (blockIdx.x == 0) {
+            *S = sS;
+            // β bookkeeping (COV.cc:264, 323)
+            *beta = sS.skip ? 1.0 : sS.beta0 + sS.dbeta;
+            dbeta_cov[0] = sS.dbeta;
+            dbeta_cov[1] = sS.cov;
+        }
+    }
+    __syncthreads();
+    const double s1 = sS.s1, mx = g * (lmax - med);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        w[i] = exp(g * (llk[i] - med) - mx) / s1;
 }
 
 // ---------------------------------------------------------------------------
@@ -568,11 +608,12 @@ static int sigma_chunk(int p) {
 
 constexpr int kSigmaBlocks = 256;  // at most this many partial sums per entry
 
-// Block b sums the chunks [b·cpb, (b+1)·cpb) in order into part[b][e].
-__global__ void __launch_bounds__(256) sigma_partial_kernel(const double* __restrict__ theta,
-                                                            const double* __restrict__ w, int n,
-                                                            int p, int chunk, int cpb,
-                                                            double* __restrict__ part) {
+// Block b sums the chunks [b·cpb, (b+1)·cpb) in order into part[b][e]; the last block to
+// finish adds the blocks' partials in block order and assembles Σ.
+__global__ void __launch_bounds__(256) sigma_kernel(const double* __restrict__ theta,
+                                                    const double* __restrict__ w, int n, int p, int chunk,
+                                                    int cpb, double* __restrict__ part, double* __restrict__ tot,
+                                                    unsigned* __restrict__ done, double* __restrict__ sigma) {
     extern __shared__ double sm[];      // [chunk][p] θ, then [chunk] w
     double* sth = sm;
     double* sw = sm + (size_t)chunk * p;
@@ -609,29 +650,32 @@ __global__ void __launch_bounds__(256) sigma_partial_kernel(const double* __rest
             part[(size_t)blockIdx.x * nent + e] = acc;
         }
     }
-}
-
-// totals over the chunks, in chunk order
-__global__ void sigma_total_kernel(int nent, int nblk, const double* __restrict__ part, double* __restrict__ tot) {
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= nent) return;
-    double acc = 0.0;
-    for (int k = 0; k < nblk; ++k) acc += part[(size_t)k * nent + e];
-    tot[e] = acc;
-}
-
-// Σ_ab = Σ w θ_a θ_b - θ̄_a θ̄_b with θ̄ = Σ w θ / Σ w (gsl_stats_wmean)
-__global__ void sigma_assemble_kernel(int p, const double* __restrict__ tot, double* __restrict__ sigma) {
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= p * (p + 1) / 2) return;
-    int a = (int)((sqrt(8.0 * e + 1.0) - 1.0) * 0.5);
-    while ((a + 1) * (a + 2) / 2 <= e) ++a;
-    while (a * (a + 1) / 2 > e) --a;
-    const int b = e - a * (a + 1) / 2;
-    const double ma = tot[1 + a] / tot[0], mb = tot[1 + b] / tot[0];
-    const double v = tot[1 + p + e] - ma * mb;
-    sigma[a * p + b] = v;
-    sigma[b * p + a] = v;
+    // the last block to finish (threadfence reduction: the count is cleared before the launch)
+    __shared__ int s_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = (atomicAdd(done, 1u) == gridDim.x - 1);
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    // totals over the blocks, in block order
+    for (int e = threadIdx.x; e < nent; e += blockDim.x) {
+        double acc = 0.0;
+        for (int k = 0; k < (int)gridDim.x; ++k) acc += __ldcg(part + (size_t)k * nent + e);
+        tot[e] = acc;
+    }
+    __syncthreads();
+    // Σ_ab = Σ w θ_a θ_b - θ̄_a θ̄_b with θ̄ = Σ w θ / Σ w (gsl_stats_wmean)
+    for (int e = threadIdx.x; e < p * (p + 1) / 2; e += blockDim.x) {
+        int a = (int)((sqrt(8.0 * e + 1.0) - 1.0) * 0.5);
+        while ((a + 1) * (a + 2) / 2 <= e) ++a;
+        while (a * (a + 1) / 2 > e) --a;
+        const int b = e - a * (a + 1) / 2;
+        const double ma = tot[1 + a] / tot[0], mb = tot[1 + b] / tot[0];
+        const double v = tot[1 + p + e] - ma * mb;
+        sigma[a * p + b] = v;
+        sigma[b * p + a] = v;
+    }
 }
 
 // chol(scaling² Σ), lower triangle row-major (Metropolis.py:103-107).  One CTA,
@@ -686,7 +730,8 @@ __global__ void cholesky_kernel(int p, const double* __restrict__ sigma,
 struct ResampleHdr {
     int total;        // number of copied rows (Σ counts)
     int first_src;    // source row of output row 0
-    int pad[2];
+    unsigned done;    // blocks of counts_rank_kernel finished
+    int pad;
 };
 
 // sequential FP64 partial sums, as itertools.accumulate (COV.py:242-251)
@@ -722,35 +767,11 @@ __global__ void __launch_bounds__(32) cdf_kernel(const double* __restrict__ w, i
     }
 }
 
-// counts[i] = #{j : edges[i] <= r_j < edges[i+1]}; r_j >= edges[n] dropped (gsl_histogram)
-__global__ void counts_kernel(int n, uint64_t seed, const uint32_t* __restrict__ epoch,
-                              const double* __restrict__ edges, int* __restrict__ counts) {
-    int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= n) return;
-    u32x4 r = draw(seed, (uint32_t)j, 0u, STREAM_RESAMPLE, 0u, *epoch);
-    const double x = u01_closed_open(r.x, r.y);
-    if (!(x >= edges[0]) || !(x < edges[n])) return;
-    // largest i with edges[i] <= x
-    int lo = 0, hi = n;          // edges[lo] <= x < edges[hi]
-    while (hi - lo > 1) {
-        int mid = (lo + hi) >> 1;
-        if (x >= edges[mid]) lo = mid; else hi = mid;
-    }
-    atomicAdd(&counts[lo], 1);
-}
-
-__global__ void count_hist_kernel(int n, const int* __restrict__ counts, int* __restrict__ hist) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n && counts[i] > 0) atomicAdd(&hist[counts[i]], 1);
-}
-
 // base[v] = Σ_{v' > v} v'·hist[v'] (reverse exclusive scan) then stable ranks within
-// equal counts: start_i = base[c_i] + c_i · #{k < i : c_k = c_i}
+// equal counts: start_i = base[c_i] + c_i · #{k < i : c_k = c_i}.  One CTA of 1024 threads.
 constexpr int kRankCache = 4096;
-__global__ void __launch_bounds__(1024) rank_kernel(int n, const int* __restrict__ counts,
-                                                    int* __restrict__ hist, int* __restrict__ base,
-                                                    int* __restrict__ seen, int* __restrict__ start,
-                                                    ResampleHdr* __restrict__ hdr) {
+__device__ void rank_counts(int n, const int* __restrict__ counts, int* __restrict__ hist, int* __restrict__ base,
+                            int* __restrict__ seen, int* __restrict__ start, ResampleHdr* __restrict__ hdr) {
     __shared__ int warp_tot[32];
     __shared__ int carry;
     __shared__ int s_seen[kRankCache];
@@ -761,7 +782,7 @@ __global__ void __launch_bounds__(1024) rank_kernel(int n, const int* __restrict
     // values n .. 0 in chunks of blockDim, processed from high to low
     for (int top = n; top >= 0; top -= (int)blockDim.x) {
         const int v = top - (int)threadIdx.x;
-        const int x = (v >= 1) ? v * hist[v] : 0;
+        const int x = (v >= 1) ? v * __ldcg(hist + v) : 0;
         // inclusive scan inside the block in thread order (= decreasing v)
         int s = x;
         for (int o = 1; o < 32; o <<= 1) {
@@ -791,7 +812,7 @@ __global__ void __launch_bounds__(1024) rank_kernel(int n, const int* __restrict
     int first = -1;
     for (int i0 = 0; i0 < n; i0 += 32) {
         const int i = i0 + lane;
-        const int c = (i < n) ? counts[i] : 0;
+        const int c = (i < n) ? __ldcg(counts + i) : 0;
         const unsigned peers = __match_any_sync(0xffffffffu, c);
         const int leader = __ffs(peers) - 1;
         const int rank = __popc(peers & ((1u << lane) - 1u));
@@ -812,6 +833,44 @@ __global__ void __launch_bounds__(1024) rank_kernel(int n, const int* __restrict
     }
     for (int o = 16; o > 0; o >>= 1) first = max(first, __shfl_xor_sync(0xffffffffu, first, o));
     if (lane == 0) hdr->first_src = first;
+}
+
+// counts[i] = #{j : edges[i] <= r_j < edges[i+1]}; r_j >= edges[n] dropped (gsl_histogram).
+// One thread per uniform; the last block to finish (threadfence reduction: the block count is
+// cleared before the launch) forms the histogram of the counts and the ranks.
+__global__ void __launch_bounds__(1024) counts_rank_kernel(int n, uint64_t seed, const uint32_t* __restrict__ epoch,
+                                                           const double* __restrict__ edges, int* __restrict__ counts,
+                                                           int* __restrict__ hist, int* __restrict__ base,
+                                                           int* __restrict__ seen, int* __restrict__ start,
+                                                           ResampleHdr* __restrict__ hdr, unsigned* __restrict__ done) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < n) {
+        u32x4 r = draw(seed, (uint32_t)j, 0u, STREAM_RESAMPLE, 0u, *epoch);
+        const double x = u01_closed_open(r.x, r.y);
+        if (x >= edges[0] && x < edges[n]) {
+            // largest i with edges[i] <= x
+            int lo = 0, hi = n;          // edges[lo] <= x < edges[hi]
+            while (hi - lo > 1) {
+                int mid = (lo + hi) >> 1;
+                if (x >= edges[mid]) lo = mid; else hi = mid;
+            }
+            atomicAdd(&counts[lo], 1);
+        }
+    }
+    __shared__ int s_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = (atomicAdd(done, 1u) == gridDim.x - 1);
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int c = __ldcg(counts + i);
+        if (c > 0) atomicAdd(&hist[c], 1);
+    }
+    __threadfence_block();
+    __syncthreads();
+    rank_counts(n, counts, hist, base, seen, start, hdr);
 }
 
 __global__ void gather_kernel(int n, int p, const double* __restrict__ beta,
@@ -942,12 +1001,77 @@ extern "C" int ag_posterior(const ag_stage_state* st, int32_t n, const double* p
     return launch_status("posterior_kernel");
 }
 
+// COV workspace: schedule state | grid barrier | partial moments (two round buffers of
+// kGridPoints x chunks x 2, then the final chunks x 2)
 static size_t cov_part_offset() { return (sizeof(CovState) + 255) / 256 * 256; }
+static size_t cov_part_doubles(int n) { return (size_t)(2 * kGridPoints + 1) * blocks(n, kEvalChunk) * 2; }
 
 extern "C" size_t ag_cov_workspace_bytes(int32_t n) {
     if (n <= 0) return 0;
-    const size_t nblk = (size_t)blocks(n, kEvalChunk);
-    return cov_part_offset() + nblk * kGridPoints * 2 * sizeof(double);
+    return cov_part_offset() + sizeof(GridBarrier) + cov_part_doubles(n) * sizeof(double);
+}
+
+// blocks of cov_schedule_kernel<BRENT> that fit on the current device at once (the cooperative
+// launch's limit), looked up once per device
+constexpr int kCoopMaxDevices = 64;
+template <bool BRENT>
+static int cov_coresident_blocks(int* out) {
+    static std::mutex mu;
+    static int cache[kCoopMaxDevices] = {};
+    int dev = 0;
+    int rc = cuda_status(cudaGetDevice(&dev), "cudaGetDevice");
+    if (rc) return rc;
+    if (dev < 0 || dev >= kCoopMaxDevices)
+        return set_error(AG_ERR_SIZE, "device %d is beyond the %d devices the COV schedule tracks", dev,
+                         kCoopMaxDevices);
+    std::lock_guard<std::mutex> lock(mu);
+    if (!cache[dev]) {
+        int occ = 0, sms = 0;
+        rc = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, cov_schedule_kernel<BRENT>, 256, 0),
+                         "cudaOccupancyMaxActiveBlocksPerMultiprocessor(cov_schedule_kernel)");
+        if (rc) return rc;
+        rc = cuda_status(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev),
+                         "cudaDeviceGetAttribute(multiprocessor count)");
+        if (rc) return rc;
+        if (occ < 1) return set_error(AG_ERR_CUDA, "cov_schedule_kernel does not fit on an SM");
+        cache[dev] = occ * sms;
+    }
+    *out = cache[dev];
+    return AG_OK;
+}
+
+// median (one CTA), then the whole search and the weights in one cooperative launch; the
+// caller's scratch holds the state, the barrier words and the partials
+template <bool BRENT>
+static int cov_schedule_launch(const ag_stage_state* st, const double* data_llk, int n, double target,
+                               double tol, int maxiter, int rounds, void* scratch, cudaStream_t s) {
+    char* base = static_cast<char*>(scratch);
+    CovState* S = reinterpret_cast<CovState*>(base);
+    GridBarrier* bar = reinterpret_cast<GridBarrier*>(base + cov_part_offset());
+    double* part = reinterpret_cast<double*>(base + cov_part_offset() + sizeof(GridBarrier));
+    int grid = 0;
+    int rc = cov_coresident_blocks<BRENT>(&grid);
+    if (rc) return rc;
+    const int items = kGridPoints * blocks(n, kEvalChunk);
+    if (grid > items) grid = items;
+    rc = cuda_status(cudaMemsetAsync(bar, 0, sizeof(GridBarrier), s), "cudaMemsetAsync(COV barrier)");
+    if (rc) return rc;
+    cov_median_kernel<<<1, 1024, 0, s>>>(data_llk, n, st->beta, S);
+    rc = launch_status("cov_median_kernel");
+    if (rc) return rc;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cuda_status(cudaLaunchKernelEx(&cfg, cov_schedule_kernel<BRENT>, data_llk, n, target, tol, maxiter,
+                                          rounds, S, part, bar, st->beta, st->dbeta_cov, st->w, st->dev_flags),
+                       "cov_schedule_kernel (cooperative launch)");
 }
 
 extern "C" int ag_cov_schedule(const ag_stage_state* st, const double* data_llk, int32_t n,
@@ -959,19 +1083,9 @@ extern "C" int ag_cov_schedule(const ag_stage_state* st, const double* data_llk,
     const size_t need = ag_cov_workspace_bytes(n);
     AG_REQUIRE(workspace && workspace_bytes >= need && aligned(workspace, 256),
                "ag_cov_schedule needs %zu bytes of 256-byte aligned workspace", need);
-    cudaStream_t s = as_stream(stream);
-    CovState* S = reinterpret_cast<CovState*>(workspace);
-    double* part = reinterpret_cast<double*>(static_cast<char*>(workspace) + cov_part_offset());
-    const int nblk = blocks(n, kEvalChunk);
-    cov_median_kernel<<<1, 1024, 0, s>>>(data_llk, n, st->beta, S);
-    for (int round = 0; round <= kGridLevels; ++round) {
-        cov_eval_kernel<<<dim3(nblk, kGridPoints), 256, 0, s>>>(data_llk, n, S, part);
-        cov_decide_kernel<<<1, 32, 0, s>>>(n, nblk, target, tol, part, S);
-    }
-    cov_final_sum_kernel<<<nblk, 256, 0, s>>>(data_llk, n, S, part);
-    cov_final_state_kernel<<<1, 32, 0, s>>>(n, nblk, part, S, st->beta, st->dbeta_cov);
-    cov_weights_kernel<<<blocks(n, 256), 256, 0, s>>>(data_llk, n, S, st->w);
-    return launch_status("cov schedule kernels");
+    // round 0 evaluates the full remaining step, rounds 1..kGridLevels one level each
+    return cov_schedule_launch<false>(st, data_llk, n, target, tol, 0, kGridLevels + 1, workspace,
+                                      as_stream(stream));
 }
 
 extern "C" int ag_cov_schedule_brent(const ag_stage_state* st, const double* data_llk, int32_t n,
@@ -983,21 +1097,10 @@ extern "C" int ag_cov_schedule_brent(const ag_stage_state* st, const double* dat
     const size_t need = ag_cov_workspace_bytes(n);
     AG_REQUIRE(workspace && workspace_bytes >= need && aligned(workspace, 256),
                "ag_cov_schedule_brent needs %zu bytes of 256-byte aligned workspace", need);
-    cudaStream_t s = as_stream(stream);
-    CovState* S = reinterpret_cast<CovState*>(workspace);
-    double* part = reinterpret_cast<double*>(static_cast<char*>(workspace) + cov_part_offset());
-    const int nblk = blocks(n, kEvalChunk);
     const int iters = maxiter < kBrentMaxIter ? maxiter : kBrentMaxIter;
-    cov_median_kernel<<<1, 1024, 0, s>>>(data_llk, n, st->beta, S);
     // round 0: the full step; round 1: the guess and the interior point; then one point per iteration
-    for (int round = 0; round < iters + 2; ++round) {
-        cov_eval_kernel<<<dim3(nblk, 2), 256, 0, s>>>(data_llk, n, S, part);
-        cov_brent_kernel<<<1, 32, 0, s>>>(n, nblk, target, tol, iters, part, S);
-    }
-    cov_final_sum_kernel<<<nblk, 256, 0, s>>>(data_llk, n, S, part);
-    cov_final_state_kernel<<<1, 32, 0, s>>>(n, nblk, part, S, st->beta, st->dbeta_cov);
-    cov_weights_kernel<<<blocks(n, 256), 256, 0, s>>>(data_llk, n, S, st->w);
-    return launch_status("cov schedule kernels (Brent)");
+    return cov_schedule_launch<true>(st, data_llk, n, target, tol, iters, iters + 2, workspace,
+                                     as_stream(stream));
 }
 
 static void sigma_grid(int n, int p, int* chunk, int* nblk, int* cpb) {
@@ -1012,7 +1115,7 @@ extern "C" size_t ag_sigma_workspace_bytes(int32_t n, int32_t p) {
     int chunk, nblk, cpb;
     sigma_grid(n, p, &chunk, &nblk, &cpb);
     const size_t nent = 1 + p + (size_t)p * (p + 1) / 2;
-    return ((size_t)nblk + 1) * nent * sizeof(double);
+    return ((size_t)nblk + 1) * nent * sizeof(double) + 256;    // partials, totals, the block count
 }
 
 extern "C" int ag_weighted_cov(const ag_stage_state* st, const double* theta, int32_t n, int32_t p,
@@ -1028,17 +1131,17 @@ extern "C" int ag_weighted_cov(const ag_stage_state* st, const double* theta, in
     const int nent = 1 + p + p * (p + 1) / 2;
     const size_t smem = (size_t)chunk * (p + 1) * sizeof(double);
     if (smem > 48 * 1024) {
-        rc = cuda_status(cudaFuncSetAttribute(sigma_partial_kernel,
-                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                         "cudaFuncSetAttribute(sigma_partial_kernel)");
+        rc = cuda_status(cudaFuncSetAttribute(sigma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                         "cudaFuncSetAttribute(sigma_kernel)");
         if (rc) return rc;
     }
     double* part = reinterpret_cast<double*>(workspace);
     double* tot = part + (size_t)nblk * nent;
-    sigma_partial_kernel<<<nblk, 256, smem, s>>>(theta, st->w, n, p, chunk, cpb, part);
-    sigma_total_kernel<<<blocks(nent, 256), 256, 0, s>>>(nent, nblk, part, tot);
-    sigma_assemble_kernel<<<blocks(p * (p + 1) / 2, 256), 256, 0, s>>>(p, tot, st->sigma);
-    return launch_status("weighted covariance kernels");
+    unsigned* done = reinterpret_cast<unsigned*>(tot + nent);
+    rc = cuda_status(cudaMemsetAsync(done, 0, sizeof(unsigned), s), "cudaMemsetAsync(Σ block count)");
+    if (rc) return rc;
+    sigma_kernel<<<nblk, 256, smem, s>>>(theta, st->w, n, p, chunk, cpb, part, tot, done, st->sigma);
+    return launch_status("sigma_kernel");
 }
 
 extern "C" int ag_cholesky_scaled(const ag_stage_state* st, int32_t p, void* stream) {
@@ -1049,7 +1152,8 @@ extern "C" int ag_cholesky_scaled(const ag_stage_state* st, int32_t p, void* str
     return launch_status("cholesky_kernel");
 }
 
-// workspace layout: hdr | edges[n+1] | counts[n] (if not given) | hist[n+1] | base[n+1] | seen[n+1] | start[n]
+// workspace layout: hdr (with the block count of counts_rank_kernel) | edges[n+1] |
+// counts[n] (if not given) | hist[n+1] | base[n+1] | seen[n+1] | start[n]
 static size_t align256(size_t b) { return (b + 255) / 256 * 256; }
 extern "C" size_t ag_resample_workspace_bytes(int32_t n) {
     if (n <= 0) return 0;
@@ -1091,10 +1195,11 @@ extern "C" int ag_resample(const ag_stage_state* st, int32_t n, int32_t p, uint6
     if (rc) return rc;
     rc = cuda_status(cudaMemsetAsync(seen, 0, (size_t)(n + 1) * sizeof(int), s), "memset seen");
     if (rc) return rc;
+    rc = cuda_status(cudaMemsetAsync(&hdr->done, 0, sizeof(unsigned), s), "memset block count");
+    if (rc) return rc;
     cdf_kernel<<<1, 32, 0, s>>>(st->w, n, edges);
-    counts_kernel<<<blocks(n, 256), 256, 0, s>>>(n, seed, st->epoch, edges, cnt);
-    count_hist_kernel<<<blocks(n, 256), 256, 0, s>>>(n, cnt, hist);
-    rank_kernel<<<1, 1024, 0, s>>>(n, cnt, hist, base, seen, start, hdr);
+    counts_rank_kernel<<<blocks(n, 1024), 1024, 0, s>>>(n, seed, st->epoch, edges, cnt, hist, base, seen, start,
+                                                         hdr, &hdr->done);
     gather_kernel<<<blocks(n, 128), 128, 0, s>>>(n, p, st->beta, cnt, start, hdr, theta_in, prior_in,
                                                  data_in, theta_out, prior_out, data_out, post_out);
     return launch_status("resample kernels");
@@ -1115,8 +1220,8 @@ extern "C" int ag_adapt_scaling(const ag_stage_state* st, double aw, double rw, 
 // fixed memory budget, embedders that must not change their device footprint
 // after start-up, and loops that must not enter the allocator at all because
 // cudaMalloc and cudaFree may synchronise the device.  This entry point
-// needs no caller workspace: its scratch (the schedule state and the
-// per-block partial moments) lives in a file-scope device array of fixed
+// needs no caller workspace: its scratch (the schedule state, the grid
+// barrier words and the partial moments) lives in a file-scope device array of fixed
 // size, reserved when this file's module is loaded on a device and held by
 // every device that loads it until the process exits.  Under CUDA's default
 // lazy module loading the module is loaded by the first use of any kernel or
@@ -1137,7 +1242,9 @@ namespace {
 constexpr int32_t kNoAllocMaxChains = 1 << 18;
 constexpr size_t kNoAllocState = (sizeof(CovState) + 255) / 256 * 256;
 constexpr size_t kNoAllocBytes =
-    kNoAllocState + (size_t)((kNoAllocMaxChains + kEvalChunk - 1) / kEvalChunk) * kGridPoints * 2 * sizeof(double);
+    kNoAllocState + sizeof(GridBarrier) +
+    (size_t)(2 * kGridPoints + 1) * ((kNoAllocMaxChains + kEvalChunk - 1) / kEvalChunk) * 2 * sizeof(double);
+static_assert(kNoAllocState == (sizeof(CovState) + 255) / 256 * 256, "no-alloc layout follows the workspace layout");
 constexpr int kNoAllocMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_cov_scratch[kNoAllocBytes];
@@ -1184,16 +1291,5 @@ extern "C" int ag_cov_schedule_noalloc(const ag_stage_state* st, const double* d
     // the state block starts from zero on every call; the partials are written before they are read
     rc = cuda_status(cudaMemsetAsync(scratch, 0, kNoAllocState, s), "cudaMemsetAsync(scratch state)");
     if (rc) return rc;
-    CovState* S = reinterpret_cast<CovState*>(scratch);
-    double* part = reinterpret_cast<double*>(static_cast<char*>(scratch) + kNoAllocState);
-    const int nblk = blocks(n, kEvalChunk);
-    cov_median_kernel<<<1, 1024, 0, s>>>(data_llk, n, st->beta, S);
-    for (int round = 0; round <= kGridLevels; ++round) {
-        cov_eval_kernel<<<dim3(nblk, kGridPoints), 256, 0, s>>>(data_llk, n, S, part);
-        cov_decide_kernel<<<1, 32, 0, s>>>(n, nblk, target, tol, part, S);
-    }
-    cov_final_sum_kernel<<<nblk, 256, 0, s>>>(data_llk, n, S, part);
-    cov_final_state_kernel<<<1, 32, 0, s>>>(n, nblk, part, S, st->beta, st->dbeta_cov);
-    cov_weights_kernel<<<blocks(n, 256), 256, 0, s>>>(data_llk, n, S, st->w);
-    return launch_status("cov schedule kernels (no-alloc)");
+    return cov_schedule_launch<false>(st, data_llk, n, target, tol, 0, kGridLevels + 1, scratch, s);
 }

@@ -818,7 +818,9 @@ def run_ours(args):
         c0 = rank * N if shards is not None else 0
         th_all = step.theta[c0:c0 + N].clone()           # this GPU's block
         out = torch.empty(n, dtype=torch.float64, device="cuda")
+        torch.cuda.nvtx.range_push("roofline")            # lets a profiler select these launches
         model.strategy.forward(th_all, out)
+        torch.cuda.nvtx.range_pop()
         fev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(3)]
         for a, b in fev:
             flush.zero_()
@@ -907,9 +909,10 @@ def run_ours(args):
                                     "(MEASURED_PEAKS.json has no FP32 figure)"},
         "e2e": {"value": world * N * S / t_e2e, "unit": "chain-steps/s", "h2d_bytes_per_step": io_bytes,
                 "d2h_bytes_per_step": io_bytes},
-        # per stage (one CUDA graph): 28 COV schedule + 3 Σ + 5 resampling + cholesky + adapt, and
-        # per Metropolis step propose, CDM cost classes, CDM set-up, CDM likelihood, accept
-        "gpu_launches": (38 + 5 * S) * args.steps,
+        # per stage (one CUDA graph): COV median + cooperative COV schedule, Σ, Cholesky, CDF,
+        # counts and ranks, gather, adapt; per Metropolis step propose, CDM cost classes, CDM set-up,
+        # CDM likelihood, accept
+        "gpu_launches": (8 + 5 * S) * args.steps,
         "cpu_baseline": {"value": cpu_rate, "unit": "chain-steps/s", "cores": cores, "kind": "port",
                          "sample": f"{args.cpu_chains} chains x {X.size} stations, likelihood only, "
                                    f"{cpu_dt:.1f} s (FP64 C restatement of models/cdm/cdm/libcdm.py)"},

@@ -5,8 +5,9 @@
  * comment says otherwise; the library allocates nothing and keeps no global
  * mutable state apart from a per-thread error string, with one exception:
  * ag_cov_schedule_noalloc keeps its scratch in a fixed device array inside the
- * library (about 45 KB per device) and caches that array's address per
- * device.  Every call is
+ * library (about 95 KB per device) and caches that array's address per
+ * device; the COV schedule entry points cache the co-resident block count of
+ * their cooperative kernel per device.  Every call is
  * asynchronous on the given stream (a cudaStream_t passed as void*, NULL =
  * legacy default stream) and returns AG_OK or an error code; the message of
  * the last error of the calling thread is available from ag_last_error().
@@ -240,12 +241,13 @@ int ag_cov_schedule_brent(const ag_stage_state* st, const double* data_llk, int3
  * after start-up, or a loop that must not enter the allocator because cudaMalloc
  * and cudaFree may synchronise the device).  Same inputs and
  * results as ag_cov_schedule without the workspace: the scratch is a fixed
- * device array inside the library (about 45 KB, held by every device that
+ * device array inside the library (about 95 KB, held by every device that
  * loads the library until exit).  Supports at most
  * ag_cov_schedule_noalloc_max_chains() chains (262,144); more returns
  * AG_ERR_SIZE.  All calls share that array: calls that overlap on the GPU
  * race, so issue them in order on one stream.  The first call on a device
- * looks up the array's address and should come before any stream capture.
+ * looks up the array's address (and the schedule kernel's co-resident block
+ * count) and should come before any stream capture.
  * The array is reserved when the library's stage module is loaded on a device:
  * under CUDA's default lazy module loading that happens at the first call into
  * any of the stage entry points (this one, ag_cov_schedule, ag_resample, ...),
