@@ -3,8 +3,9 @@
 Runs ``oracle.catmip.Annealing`` -- the FP64 restatement of the reference's
 annealing loop (altar/altar/bayesian/Annealer.py:79-135 with COV.py:66-251 and
 Metropolis.py:63-281) that draws from the same Philox streams as the device --
-on two problems for seeds 1..K and stores, per seed, the summaries of the final
-population.  The spread of a summary over the seeds is the Monte Carlo standard
+on two problems for seeds 1..K (8 Mogi, 24 CDM) and stores, per seed, the summaries
+of the final population.  Seeds can be generated in batches (--cdm-first-seed,
+--cdm-seeds, --skip-mogi) and their rows concatenated in seed order.  The spread of a summary over the seeds is the Monte Carlo standard
 error of one run (it includes the correlation the resampling introduces).
 
   * ``mogi_*``: the Mogi workload (1,024 LOS points on a 32x32 grid over ±15 km,
@@ -72,7 +73,7 @@ def cdm_case():
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--seeds", type=int, default=8)
-    ap.add_argument("--cdm-seeds", type=int, default=12)
+    ap.add_argument("--cdm-seeds", type=int, default=24)
     ap.add_argument("--cdm-first-seed", type=int, default=1)
     ap.add_argument("--skip-mogi", action="store_true")
     ap.add_argument("--out", default=os.path.join(HERE, "posterior_golden.npz"))
