@@ -88,7 +88,7 @@ AG_STATION_TILE = 128
 
 class StationSet(ctypes.Structure):
     _fields_ = [("xy", c_void_p), ("losd", c_void_p), ("weight", c_void_p), ("oid", c_void_p),
-                ("m", c_int32), ("m_padded", c_int32)]
+                ("m", c_int32), ("m_padded", c_int32), ("tile_box", c_void_p)]
 
 
 class Layout(ctypes.Structure):
@@ -133,7 +133,8 @@ _SIGNATURES = {
     "ag_forward_variants": (c_int32, [c_int]),
     "ag_forward_llk": (c_int, [c_int, P, P, c_int32, P, c_double, P, P, P, P, P, c_size_t, P]),
     "ag_cdm_check": (c_int, [P, P, c_int32, P, P]),
-    "ag_cdm_work": (c_int, [P, P, c_int32, P, P, P]),
+    "ag_cdm_work": (c_int, [P, P, c_int32, P, P, P, P]),
+    "ag_station_boxes": (c_int, [P, c_int32, c_int32, P, P]),
     "ag_forward_llk_subset": (c_int, [c_int, P, P, c_int32, P, c_double, P, P, P, P, P, P, c_size_t, P]),
     "ag_linear_kpad": (c_int32, [c_int32]),
     "ag_linear_prepare": (c_int, [P, c_int32, c_int32, P, P]),

@@ -8,10 +8,11 @@
 // libcdm.py:310-372 (angular-dislocation pair of one side, artefact-free
 // configurations I and II), libcdm.py:375-430 (AngDisDisp terms).
 //
-// A rectangle far from the free surface compared with its size is evaluated
-// instead as the integral of point tensile dislocations over its area
-// (Gauss-Legendre product rule, QuadC below): the same field without the
-// cancellation between its four sides.
+// A rectangle far from the stations compared with its size (far from the free
+// surface, or far from a tile of stations) is evaluated instead as the integral of
+// point tensile dislocations over its area (Gauss-Legendre product rule, RectQ
+// below): the same field without the cancellation between its four sides, and
+// with a few nodes where the stations are far.
 #pragma once
 #include <math.h>
 #include <stdint.h>
@@ -236,39 +237,62 @@ AG_CDM_FN bool cdm_corners(const double* th, const Layout& L, Vec3 V[3][4]) {
 //
 // The rectangle's field is the integral of that kernel over the rectangle, taken with an
 // n1 × n2 Gauss-Legendre product rule.  The integrand is analytic in each coordinate; its
-// singularities lie where the station-to-point distance vanishes, at least D (the depth of
-// the rectangle's shallowest corner) from every point of the rectangle, so the error of
-// an n-point rule along a side of half-length h falls like ρ^(-2n), ρ = D/h + sqrt((D/h)² + 1)
-// (the Bernstein ellipse through the nearest singularity).  Each direction gets the
-// smallest n with ρ^(-2n) <= kQuadTol; the rectangle is integrated when n1 n2 <= kQuadBudget
-// (its four sides cost about as much as 20 nodes) and evaluated by its sides otherwise (a
-// rectangle close to the surface, where its sides do not cancel much).  The nodes are
-// summed in FP32 without cancellation: for a rectangle whose distance from the stations is
-// many times its size, the FP32 sum of its four sides loses the factor distance/size in
-// accuracy, the quadrature does not.
+// singularities lie where the station-to-point distance vanishes, at least D from every
+// point of the rectangle for the stations in question, so the error of an n-point rule
+// along a side of half-length h falls like ρ^(-2n), ρ = D/h + sqrt((D/h)² + 1) (the
+// Bernstein ellipse through the nearest singularity).  Each direction gets the smallest n
+// with ρ^(-2n) <= kQuadTol, found by comparing δ² = (D/h)² with the thresholds
+// kQuadDelta2 (no transcendental function, so the kernel, the work count and the host
+// build decide alike).  Two distances are used:
+//   * per chain, D = the depth of the rectangle's shallowest corner (a lower bound for every
+//     station): a rectangle with n1 n2 <= kQuadBudget is integrated everywhere ("far"
+//     rectangle; its four sides cost about as much as 20 nodes), the others are evaluated
+//     by their sides;
+//   * per station tile (AG_STATION_TILE consecutive stations), D² = depth² + gap², gap the
+//     horizontal distance between the tile's bounding box and the rectangle's corners': far
+//     rectangles take the tile's (smaller) node counts, and a rectangle evaluated by its
+//     sides is integrated over the tiles where n1 n2 <= kQuadBudget nodes cost less than
+//     its sides.  Stations far from the source then take a few nodes instead of many.
+// The nodes are summed in FP32 without cancellation: for a rectangle whose distance from
+// the stations is many times its size, the FP32 sum of its four sides loses the factor
+// distance/size in accuracy, the quadrature does not.
 constexpr double kQuadTol = 1e-7;
 constexpr int kQuadBudget = 32;
-constexpr int kQuadMaxNodes = 46;
 
-struct __align__(16) QuadC {
-    float4 h0;                    // strike direction (a, b) = (cos, sin), sin δ, q offset Q0
-    float4 h1;                    // -k sin²δ, node count (integer bits), 0, 0
-    float4 node[kQuadMaxNodes];   // x, y (strike frame, relative to the source centre), depth, weight
-};
-static_assert(sizeof(QuadC) <= 4 * sizeof(SideC), "a rectangle's quadrature block overlays its four sides");
-static_assert(kQuadBudget <= kQuadMaxNodes, "quadrature node budget");
+// δ_n² = ((ρ_n - 1/ρ_n)/2)², ρ_n = kQuadTol^(-1/(2n)): n nodes per direction suffice for
+// δ² >= δ_n² (n = 1 ... kGaussMax; rounded up to FP32)
+AG_GL_TABLE float kQuadDelta2[kGaussMax] = {
+    2.499999750e+06f, 7.900695190e+02f, 5.336203003e+01f, 1.356297970e+01f, 5.789669037e+00f, 3.186530590e+00f,
+    2.025000095e+00f, 1.408073664e+00f, 1.040413141e+00f, 8.028496504e-01f, 6.399435997e-01f, 5.230506659e-01f,
+    4.361335039e-01f, 3.696263731e-01f, 3.175248802e-01f, 2.758984566e-01f};
 
-// smallest n with ρ^(-2n) <= kQuadTol, ρ = δ + sqrt(δ² + 1), δ = distance / half-length
-AG_CDM_FN int quad_points(double delta) {
-    const double rho = delta + sqrt(delta * delta + 1.0);
-    const double n = ceil(log(1.0 / kQuadTol) / (2.0 * log(rho)));
-    return (n < 1.0) ? 1 : (n > (double)kGaussMax ? kGaussMax + 1 : (int)n);
+// smallest n in 1 ... kGaussMax with δ² >= δ_n², kGaussMax + 1 if none: the number of
+// thresholds above δ² (they decrease with n), by binary search
+template <class F>
+AG_CDM_FN int quad_n(F delta2) {
+    int k = 0;
+    for (int step = 8; step > 0; step >>= 1)
+        if (k + step <= kGaussMax && delta2 < (F)kQuadDelta2[k + step - 1]) k += step;
+    return k + 1;
 }
 
+// A rectangle's quadrature in parametric form; the nodes of an n1 × n2 rule are generated
+// from it where they are used (rect_node)
+struct __align__(16) RectQ {
+    float4 h0;    // strike direction (a, b) = (cos, sin), sin δ, q offset Q0
+    float4 h1;    // -k sin²δ, 1/h1², 1/h2², D² (D: depth of the shallowest corner)
+    float4 c;     // centre in the strike frame (relative to the source centre), its depth, weight scale
+    float4 e1;    // half edge P2 - P1 in the strike frame (x, y, depth); FLOP per station of the sides
+    float4 e2;    // half edge P4 - P1 in the strike frame (x, y, depth); chain node counts n1 + 256 n2
+    float4 box;   // the corners' horizontal bounding box relative to the source centre: x0, x1, y0, y1
+};
+
 // Per-chain plan shared by the set-up kernel and the work count: bits 0-11 sides evaluated
-// as angular-dislocation pairs, 12-23 which of them are near-vertical, 24-26 rectangles
-// integrated by quadrature (their node counts in nq).  Rectangles that take part follow
-// libcdm.py:226-242 (a zero semi-axis leaves only the rectangle spanned by the other two).
+// as angular-dislocation pairs (where the tile does not integrate their rectangle), 12-23
+// which of them are near-vertical, 24-26 far rectangles integrated everywhere (their node
+// counts in nq), 27-29 rectangles that take part (a RectQ each).  Rectangles that take part
+// follow libcdm.py:226-242 (a zero semi-axis leaves only the rectangle spanned by the other
+// two).
 template <class Layout>
 AG_CDM_FN uint32_t cdm_plan(const double* th, const Layout& L, const Vec3 V[3][4], int nq[3][2]) {
     const double ax = th[L.axes_idx], ay = th[L.axes_idx + 1], az = th[L.axes_idx + 2];
@@ -293,11 +317,11 @@ AG_CDM_FN uint32_t cdm_plan(const double* th, const Layout& L, const Vec3 V[3][4
         double D = -V[r][0].z;
         for (int e = 1; e < 4; ++e) D = fmin(D, -V[r][e].z);
         if (h1 > 0.0 && h2 > 0.0 && D > 0.0) {
-            const int n1 = quad_points(D / h1), n2 = quad_points(D / h2);
+            const int n1 = quad_n((D * D) / (h1 * h1)), n2 = quad_n((D * D) / (h2 * h2));
             if (n1 <= kGaussMax && n2 <= kGaussMax && n1 * n2 <= kQuadBudget) {
                 nq[r][0] = n1;
                 nq[r][1] = n2;
-                mask |= 1u << (24 + r);
+                mask |= (1u << (24 + r)) | (1u << (27 + r));
                 continue;
             }
         }
@@ -307,13 +331,45 @@ AG_CDM_FN uint32_t cdm_plan(const double* th, const Layout& L, const Vec3 V[3][4
             if (act) mask |= 1u << (r * 4 + e);
             if (act && steep) mask |= 1u << (kSides + r * 4 + e);
         }
+        if (mask >> (4 * r) & 0xFu) mask |= 1u << (27 + r);
     }
     return mask;
 }
 
-// Quadrature constants of rectangle P1..P4 (P2 - P1 and P4 - P1 its edges) for n1 × n2 nodes
-AG_CDM_FN void fill_quad(QuadC& Q, const Vec3 P[4], double opening, double nu, double x0, double y0, int n1,
-                         int n2) {
+// float rounded down / up (a box that contains the exact one)
+AG_CDM_FN float f32_down(double v) {
+#ifdef __CUDA_ARCH__
+    return __double2float_rd(v);
+#else
+    float f = (float)v;
+    if ((double)f > v) f = nextafterf(f, -INFINITY);
+    return f;
+#endif
+}
+AG_CDM_FN float f32_up(double v) {
+#ifdef __CUDA_ARCH__
+    return __double2float_ru(v);
+#else
+    float f = (float)v;
+    if ((double)f < v) f = nextafterf(f, INFINITY);
+    return f;
+#endif
+}
+
+// FP32 work per station (FMA = 2), counted from the pair and quadrature code below and
+// checked against a counting evaluation in the CPU tests
+constexpr int kFlopSide = 251;          // one angular-dislocation pair
+constexpr int kFlopSteepExtra = 78;     // near-vertical pair: remainders of the cot β terms
+constexpr int kFlopQuadRect = 19;       // quadrature rectangle: strike frame, q, back to EFCS
+constexpr int kFlopQuadNode = 48;       // one point tensile dislocation, weighted sum
+constexpr int kFlopStation = 31;        // coordinates, LOS projection, residual, float-float misfit
+constexpr int kSfuSide = 13, kSfuSteepExtra = 3, kSfuQuadNode = 2;
+
+// Parametric quadrature of rectangle P1..P4 (P2 - P1 and P4 - P1 its edges); side_flop is
+// the FP32 work per station of its sides (0 for a far rectangle), n1, n2 its node counts
+// as a far rectangle (0 otherwise)
+AG_CDM_FN void fill_rect(RectQ& R, const Vec3 P[4], double opening, double nu, double x0, double y0,
+                         int side_flop, int n1, int n2) {
     const double PI = 3.14159265358979323846;
     const Vec3 e1 = v_sub(P[1], P[0]), e2 = v_sub(P[3], P[0]);
     Vec3 nrm = v_cross(e1, e2);
@@ -329,39 +385,55 @@ AG_CDM_FN void fill_quad(QuadC& Q, const Vec3 P[4], double opening, double nu, d
         b = nrm.x / sd;
     }
     const Vec3 c = v_add(P[0], v_scale(v_add(e1, e2), 0.5));
-    const double yc = -b * (c.x - x0) + a * (c.y - y0);
-    Q.h0 = make_float4((float)a, (float)b, (float)sd, (float)(yc * sd + (-c.z) * cd));
-    Q.h1 = make_float4((float)(-(1.0 - 2.0 * nu) * sd * sd), __int_as_float(n1 * n2), 0.f, 0.f);
-    const double scale = 0.25 * area * opening / (2.0 * PI);
-    int k = 0;
-    for (int i = 0; i < n1; ++i) {
-        const double s = kGaussX[gauss_offset(n1) + i], ws = kGaussW[gauss_offset(n1) + i];
-        for (int j = 0; j < n2; ++j) {
-            const double t = kGaussX[gauss_offset(n2) + j], wt = kGaussW[gauss_offset(n2) + j];
-            const Vec3 xi = v_add(P[0], v_add(v_scale(e1, 0.5 * (1.0 + s)), v_scale(e2, 0.5 * (1.0 + t))));
-            const double dx = xi.x - x0, dy = xi.y - y0;
-            Q.node[k++] = make_float4((float)(a * dx + b * dy), (float)(-b * dx + a * dy), (float)(-xi.z),
-                                      (float)(ws * wt * scale));
-        }
+    const double cx = c.x - x0, cy = c.y - y0;
+    const double yc = -b * cx + a * cy;
+    const double h1 = 0.5 * sqrt(v_dot(e1, e1)), h2 = 0.5 * sqrt(v_dot(e2, e2));
+    double D = -P[0].z, bx0 = P[0].x, bx1 = P[0].x, by0 = P[0].y, by1 = P[0].y;
+    for (int k = 1; k < 4; ++k) {
+        D = fmin(D, -P[k].z);
+        bx0 = fmin(bx0, P[k].x); bx1 = fmax(bx1, P[k].x);
+        by0 = fmin(by0, P[k].y); by1 = fmax(by1, P[k].y);
     }
-    for (; k < kQuadMaxNodes; ++k) Q.node[k] = make_float4(0.f, 0.f, 1.f, 0.f);
+    R.h0 = make_float4((float)a, (float)b, (float)sd, (float)(yc * sd + (-c.z) * cd));
+    R.h1 = make_float4((float)(-(1.0 - 2.0 * nu) * sd * sd), h1 > 0.0 ? (float)(1.0 / (h1 * h1)) : 0.f,
+                       h2 > 0.0 ? (float)(1.0 / (h2 * h2)) : 0.f, f32_down(D * D));
+    R.c = make_float4((float)(a * cx + b * cy), (float)yc, (float)(-c.z),
+                      (float)(0.25 * area * opening / (2.0 * PI)));
+    const Vec3 E1 = v_scale(e1, 0.5), E2 = v_scale(e2, 0.5);
+    R.e1 = make_float4((float)(a * E1.x + b * E1.y), (float)(-b * E1.x + a * E1.y), (float)(-E1.z), (float)side_flop);
+    R.e2 = make_float4((float)(a * E2.x + b * E2.y), (float)(-b * E2.x + a * E2.y), (float)(-E2.z),
+                       __int_as_float(n1 + 256 * n2));
+    R.box = make_float4(f32_down(bx0 - x0), f32_up(bx1 - x0), f32_down(by0 - y0), f32_up(by1 - y0));
 }
 
-// Constants of a chain whose corners V lie below the surface, following the plan: the
-// active sides of the rectangles evaluated by their sides, the nodes of the others (a
-// QuadC in place of the rectangle's four SideC).  Returns the plan's mask.
+// FP32 work per station of the sides of rectangle r in the plan
+AG_CDM_FN void rect_side_work(uint32_t mask, int r, int& flop, int& sfu) {
+    flop = 0;
+    sfu = 0;
+    for (int e = 0; e < 4; ++e) {
+        const int k = 4 * r + e;
+        if (!(mask >> k & 1u)) continue;
+        const bool st = (mask >> (kSides + k)) & 1u;
+        flop += kFlopSide + (st ? kFlopSteepExtra : 0);
+        sfu += kSfuSide + (st ? kSfuSteepExtra : 0);
+    }
+}
+
+// Constants of a chain whose corners V lie below the surface, following the plan: a RectQ
+// for every rectangle that takes part, and the SideC of the active sides of the rectangles
+// that are not far.  Returns the plan's mask.
 template <class Layout>
 AG_CDM_FN uint32_t cdm_sides(const double* th, const Layout& L, const Vec3 V[3][4], double x0, double y0,
-                             SideC* side) {
+                             SideC* side, RectQ* rect) {
     int nq[3][2];
     const uint32_t mask = cdm_plan(th, L, V, nq);
     const double opening = th[L.strength_idx];
     for (int r = 0; r < 3; ++r) {
-        if (mask >> (24 + r) & 1u) {
-            fill_quad(*reinterpret_cast<QuadC*>(&side[r * 4]), V[r], opening, L.nu, x0, y0, nq[r][0], nq[r][1]);
-            continue;
-        }
-        if (!(mask >> (4 * r) & 0xFu)) continue;
+        if (!(mask >> (27 + r) & 1u)) continue;
+        int sf, su;
+        rect_side_work(mask, r, sf, su);
+        fill_rect(rect[r], V[r], opening, L.nu, x0, y0, sf, nq[r][0], nq[r][1]);
+        if (mask >> (24 + r) & 1u) continue;
         Vec3 nrm = v_cross(v_sub(V[r][1], V[r][0]), v_sub(V[r][3], V[r][0]));
         nrm = v_scale(nrm, 1.0 / sqrt(v_dot(nrm, nrm)));
         const Vec3 b = v_scale(nrm, opening);
@@ -373,26 +445,73 @@ AG_CDM_FN uint32_t cdm_sides(const double* th, const Layout& L, const Vec3 V[3][
     return mask;
 }
 
-// FP32 work per station of a chain with this plan (FMA = 2): the counts of the pair and
-// quadrature code below, checked against a counting evaluation in the CPU tests
-constexpr int kFlopSide = 251;          // one angular-dislocation pair
-constexpr int kFlopSteepExtra = 78;     // near-vertical pair: remainders of the cot β terms
-constexpr int kFlopQuadRect = 19;       // quadrature rectangle: strike frame, q, back to EFCS
-constexpr int kFlopQuadNode = 48;       // one point tensile dislocation, weighted sum
-constexpr int kFlopStation = 31;        // coordinates, LOS projection, residual, float-float misfit
-constexpr int kSfuSide = 13, kSfuSteepExtra = 3, kSfuQuadNode = 2;
-AG_CDM_FN void cdm_work(uint32_t mask, const int nq[3][2], uint32_t& flop, uint32_t& sfu) {
-    uint32_t f = kFlopStation, u = 0;
-    for (int k = 0; k < kSides; ++k) {
-        if (!(mask >> k & 1u)) continue;
-        const bool st = (mask >> (kSides + k)) & 1u;
-        f += kFlopSide + (st ? kFlopSteepExtra : 0);
-        u += kSfuSide + (st ? kSfuSteepExtra : 0);
-    }
+// The plan and the RectQ of every rectangle that takes part (no side constants): what the
+// cost classes and the work count need
+template <class Layout>
+AG_CDM_FN uint32_t cdm_rects(const double* th, const Layout& L, const Vec3 V[3][4], double x0, double y0,
+                             RectQ* rect) {
+    int nq[3][2];
+    const uint32_t mask = cdm_plan(th, L, V, nq);
     for (int r = 0; r < 3; ++r) {
-        if (!(mask >> (24 + r) & 1u)) continue;
-        f += kFlopQuadRect + kFlopQuadNode * nq[r][0] * nq[r][1];
-        u += kSfuQuadNode * nq[r][0] * nq[r][1];
+        if (!(mask >> (27 + r) & 1u)) continue;
+        int sf, su;
+        rect_side_work(mask, r, sf, su);
+        fill_rect(rect[r], V[r], th[L.strength_idx], L.nu, x0, y0, sf, nq[r][0], nq[r][1]);
+    }
+    return mask;
+}
+
+// Node counts of rectangle R over a station tile whose bounding box, relative to the source
+// centre, is [bx0, bx1] × [by0, by1]: δ² = (D² + gap²)/h² per direction.  A far rectangle
+// keeps at most its chain node counts; a rectangle evaluated by its sides is integrated over
+// the tile when its nodes fit the budget and cost less than its sides.  Returns whether the
+// tile integrates it.
+AG_CDM_FN bool tile_quad(const RectQ& R, bool far, float bx0, float bx1, float by0, float by1, int& n1, int& n2) {
+    const float gx = fmaxf(0.0f, fmaxf(__fsub_rn(R.box.x, bx1), __fsub_rn(bx0, R.box.y)));
+    const float gy = fmaxf(0.0f, fmaxf(__fsub_rn(R.box.z, by1), __fsub_rn(by0, R.box.w)));
+    const float D2 = __fadd_rn(R.h1.w, __fadd_rn(__fmul_rn(gx, gx), __fmul_rn(gy, gy)));
+    n1 = quad_n(__fmul_rn(D2, R.h1.y));
+    n2 = quad_n(__fmul_rn(D2, R.h1.z));
+    if (far) {
+        const int nc = __float_as_int(R.e2.w);
+        n1 = n1 < (nc & 255) ? n1 : (nc & 255);
+        n2 = n2 < (nc >> 8) ? n2 : (nc >> 8);
+        return true;
+    }
+    return n1 <= kGaussMax && n2 <= kGaussMax && n1 * n2 <= kQuadBudget &&
+           kFlopQuadRect + kFlopQuadNode * n1 * n2 < (int)R.e1.w;
+}
+
+// Node k = (i, j) of the n1 × n2 rule on R (k < n1 n2 <= kQuadBudget): position in the
+// strike frame, depth, weight, from the FP32 rules gx, gw (kGaussXf, kGaussWf or a copy).
+// i = floor((k + 1/2)/n2) is exact in FP32 for k < 32 (the fraction stays 1/(2 n2) away from
+// an integer, far above the rounding of the approximate reciprocal).
+AG_CDM_FN float4 rect_node(const RectQ& R, int n1, int n2, int k, const float* gx, const float* gw) {
+    const int i = (int)(__fmul_rn(__fadd_rn((float)k, 0.5f), __fdividef(1.0f, (float)n2)));
+    const int j = k - i * n2;
+    const float s = gx[gauss_offset(n1) + i], t = gx[gauss_offset(n2) + j];
+    const float w = __fmul_rn(gw[gauss_offset(n1) + i], gw[gauss_offset(n2) + j]);
+    return make_float4(fmaf(t, R.e2.x, fmaf(s, R.e1.x, R.c.x)), fmaf(t, R.e2.y, fmaf(s, R.e1.y, R.c.y)),
+                       fmaf(t, R.e2.z, fmaf(s, R.e1.z, R.c.z)), __fmul_rn(w, R.c.w));
+}
+
+// FP32 work per station of a chain over one tile (its plan's sides, and the nodes of the
+// rectangles the tile integrates)
+AG_CDM_FN void tile_work(const RectQ* rect, uint32_t mask, float bx0, float bx1, float by0, float by1,
+                         uint32_t& flop, uint32_t& sfu) {
+    uint32_t f = kFlopStation, u = 0;
+    for (int r = 0; r < 3; ++r) {
+        if (!(mask >> (27 + r) & 1u)) continue;
+        int n1, n2;
+        if (tile_quad(rect[r], (mask >> (24 + r)) & 1u, bx0, bx1, by0, by1, n1, n2)) {
+            f += kFlopQuadRect + kFlopQuadNode * n1 * n2;
+            u += kSfuQuadNode * n1 * n2;
+        } else {
+            int sf, su;
+            rect_side_work(mask, r, sf, su);
+            f += sf;
+            u += su;
+        }
     }
     flop = f;
     sfu = u;
@@ -733,25 +852,24 @@ AG_DEVICE_INLINE void side_pair(const K& k, V Xr, V Yr, V& ue, V& un, V& uv, boo
         side_pair_t<false>(k, Xr, Yr, ue, un, uv);
 }
 
-// One rectangle by its quadrature nodes (QuadC; the point tensile dislocation above).
+// One rectangle by nn quadrature nodes (from rect_node; the point tensile dislocation above).
 // Per station: the strike-frame coordinates and q once, then per node
 //   R² = x² + y² + d², A = 1/(R(R+d)²), E = 1/(R³(R+d)²), B = (3R+d) E/(R+d), T = 3q²/R⁵,
 //   ux = x [T - k s² (1/R³ - (A - y² B))],  uy = y [T - k s² (A - x² B)],
 //   uz = d T - k s² (1/(R(R+d)) - x²(2R+d) E),
 // weighted and summed in FP32 (the nodes' terms vary smoothly: no cancellation).
 template <class V>
-AG_DEVICE_INLINE void rect_quad(const QuadC& Q, V Xr, V Yr, V& ue, V& un, V& uv) {
+AG_DEVICE_INLINE void rect_quad(const RectQ& Q, const float4* node, int nn, V Xr, V Yr, V& ue, V& un, V& uv) {
     const V a = V(Q.h0.x), b = V(Q.h0.y);
     const V xs = vfma(a, Xr, vmul(b, Yr));
     const V ys = vfma(a, Yr, vneg(vmul(b, Xr)));
     const V q = vfma(ys, V(Q.h0.z), V(-Q.h0.w));
     const V q3 = vmul(vmul(q, q), V(3.0f));
     const V nks2 = V(Q.h1.x);
-    const int nn = __float_as_int(Q.h1.y);
     V sx(0.0f), sy(0.0f), sz(0.0f);
 #pragma unroll 2
     for (int k = 0; k < nn; ++k) {
-        const float4 nd = Q.node[k];
+        const float4 nd = node[k];
         const V x = vsub(xs, V(nd.x)), y = vsub(ys, V(nd.y)), d = V(nd.z), w = V(nd.w);
         const V R2 = vfma(x, x, vfma(y, y, vmul(d, d)));
         const V iR = vrsqrt(R2);

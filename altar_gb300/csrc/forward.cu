@@ -17,14 +17,17 @@
 // cancellation never happens in floating point.
 //
 // Work decomposition: cdm_setup_kernel computes each chain's per-side
-// constants in FP64 and packs the chains that have work (not masked, not
-// above the free surface) into consecutive slots; the likelihood kernel runs
-// one warp per slot, lanes over stations; a CTA holds WARPS chains whose
-// constants live in shared memory and are read with broadcast vector loads;
-// station tiles stream through a ring of shared-memory buffers filled by 1-D
-// bulk copies (cp.async.bulk + mbarrier) and shared by the CTA's warps.  Each
-// lane accumulates w·r² in float-float; the warp's sum is reduced in FP64 in
-// a fixed order.
+// constants and per-rectangle quadrature parameters in FP64 and packs the
+// chains that have work (not masked, not above the free surface) into
+// consecutive slots; the likelihood kernel runs one warp per slot, lanes over
+// stations; a CTA holds WARPS chains whose constants live in shared memory and
+// are read with broadcast vector loads; station tiles stream through a ring of
+// shared-memory buffers filled by 1-D bulk copies (cp.async.bulk + mbarrier)
+// and shared by the CTA's warps.  For each tile a warp decides, from the
+// tile's bounding box, which rectangles it integrates by quadrature and with
+// how many nodes (generated into shared memory), and evaluates the sides of the
+// others.  Each lane accumulates w·r² in float-float; the warp's sum is reduced
+// in FP64 in a fixed order.
 #include <math.h>
 #include <stdint.h>
 
@@ -48,6 +51,7 @@ struct __align__(16) ChainC {
     float off[kMaxOffsets];     // per-dataset offsets θ[offset_idx + k]
     float pad2[8];
     SideC side[kSides];
+    RectQ rect[3];              // every rectangle that takes part, parametric quadrature
 };
 static_assert(sizeof(ChainC) % 16 == 0, "ChainC must be a whole number of float4");
 
@@ -73,12 +77,31 @@ __device__ __forceinline__ int cost_bucket(uint32_t flop) {
     return b < kCostBuckets - 1 ? b : kCostBuckets - 1;
 }
 
+// Per-station work of a chain averaged over every stride-th station tile (tile boxes
+// relative to the source centre as the likelihood kernel forms them)
+__device__ float sampled_tile_work(const RectQ* rect, uint32_t mask, const float4* __restrict__ tile_box,
+                                   int ntiles, int stride, float x0h, float x0l, float y0h, float y0l) {
+    float f = 0.f;
+    int cnt = 0;
+    for (int t = stride / 2; t < ntiles; t += stride) {
+        const float4 tb = __ldg(tile_box + t);
+        uint32_t fl, su;
+        tile_work(rect, mask, __fsub_rn(__fsub_rn(tb.x, x0h), x0l), __fsub_rn(__fsub_rn(tb.y, x0h), x0l),
+                  __fsub_rn(__fsub_rn(tb.z, y0h), y0l), __fsub_rn(__fsub_rn(tb.w, y0h), y0l), fl, su);
+        f += (float)fl;
+        ++cnt;
+    }
+    return cnt ? f / (float)cnt : (float)kFlopStation;
+}
+
 // One thread per requested chain (all n, or the first *count_in of index_in): -1 for a masked
-// chain, -2 (and the status bit) for one above the free surface, else its cost bucket
+// chain, -2 (and the status bit) for one above the free surface, else its cost bucket (the
+// work of its plan averaged over a sample of the station tiles)
 __global__ void cdm_cost_kernel(ag_layout L, const double* __restrict__ theta, int n,
                                 const uint32_t* __restrict__ mask_in, uint32_t* __restrict__ chain_status,
                                 const int32_t* __restrict__ index_in, const int32_t* __restrict__ count_in,
-                                int8_t* __restrict__ key, SetupHdr* __restrict__ hdr) {
+                                const float4* __restrict__ tile_box, int ntiles, int8_t* __restrict__ key,
+                                SetupHdr* __restrict__ hdr) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
     int i = t;
@@ -97,10 +120,14 @@ __global__ void cdm_cost_kernel(ag_layout L, const double* __restrict__ theta, i
         key[t] = -2;
         return;
     }
-    int nq[3][2];
-    uint32_t flop, sfu;
-    cdm_work(cdm_plan(th, L, V, nq), nq, flop, sfu);
-    const int b = cost_bucket(flop);
+    const double x0 = th[L.x_idx], y0 = th[L.x_idx + 1];
+    float x0h, x0l, y0h, y0l;
+    split_hilo(x0, x0h, x0l);
+    split_hilo(y0, y0h, y0l);
+    RectQ rect[3];
+    const uint32_t mask = cdm_rects(th, L, V, x0, y0, rect);
+    const int stride = ntiles > 16 ? ntiles / 16 : 1;
+    const int b = cost_bucket((uint32_t)sampled_tile_work(rect, mask, tile_box, ntiles, stride, x0h, x0l, y0h, y0l));
     key[t] = (int8_t)b;
     atomicAdd(&hdr->hist[b], 1);
 }
@@ -144,7 +171,7 @@ __global__ void cdm_setup_kernel(ag_layout L, const double* __restrict__ theta, 
     split_hilo(y0, C.hdr.z, C.hdr.w);
     for (int k = 0; k < kMaxOffsets; ++k)
         C.off[k] = (k < noffsets) ? (float)th[L.offset_idx + k] : 0.f;
-    const uint32_t mask = cdm_sides(th, L, V, x0, y0, C.side);
+    const uint32_t mask = cdm_sides(th, L, V, x0, y0, C.side, C.rect);
     // a chain with no active side still needs a llk: keep bit 31 as "evaluate"
     C.side_mask = mask | 0x80000000u;
 }
@@ -157,50 +184,87 @@ __global__ void cdm_check_kernel(ag_layout L, const double* __restrict__ theta, 
     if (cdm_corners(theta + (size_t)i * L.nparams, L, V)) chain_status[i] |= CHAIN_ABOVE_SURFACE;
 }
 
-// FP32 operations per station the likelihood kernel executes for each chain (its plan:
-// sides and quadrature nodes); 0 for chains above the free surface, which it skips
+// FP32 operations the likelihood kernel executes for each chain over the m stations (its
+// plan per station tile: sides and quadrature nodes); 0 for chains above the free surface,
+// which it skips
 __global__ void cdm_work_kernel(ag_layout L, const double* __restrict__ theta, int n,
-                                uint32_t* __restrict__ flop, uint32_t* __restrict__ sfu) {
+                                const float4* __restrict__ tile_box, int m, double* __restrict__ flop,
+                                double* __restrict__ sfu) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double* th = theta + (size_t)i * L.nparams;
     Vec3 V[3][4];
-    uint32_t f = 0u, u = 0u;
+    double f = 0.0, u = 0.0;
     if (!cdm_corners(th, L, V)) {
-        int nq[3][2];
-        cdm_work(cdm_plan(th, L, V, nq), nq, f, u);
+        const double x0 = th[L.x_idx], y0 = th[L.x_idx + 1];
+        float x0h, x0l, y0h, y0l;
+        split_hilo(x0, x0h, x0l);
+        split_hilo(y0, y0h, y0l);
+        RectQ rect[3];
+        const uint32_t mask = cdm_rects(th, L, V, x0, y0, rect);
+        const int ntiles = (m + kTile - 1) / kTile;
+        for (int t = 0; t < ntiles; ++t) {
+            const float4 tb = __ldg(tile_box + t);
+            uint32_t fl, su;
+            tile_work(rect, mask, __fsub_rn(__fsub_rn(tb.x, x0h), x0l), __fsub_rn(__fsub_rn(tb.y, x0h), x0l),
+                      __fsub_rn(__fsub_rn(tb.z, y0h), y0l), __fsub_rn(__fsub_rn(tb.w, y0h), y0l), fl, su);
+            const int cnt = min(kTile, m - t * kTile);
+            f += (double)fl * cnt;
+            u += (double)su * cnt;
+        }
     }
     flop[i] = f;
     if (sfu) sfu[i] = u;
 }
 
+// Bounding box of each tile of AG_STATION_TILE stations (coordinates hi + lo), rounded
+// outwards to FP32; padding stations (index >= m) are left out.  One warp per tile.
+__global__ void station_boxes_kernel(const float4* __restrict__ xy, int m, int ntiles, float4* __restrict__ box) {
+    const int t = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (t >= ntiles) return;
+    double x0 = INFINITY, x1 = -INFINITY, y0 = INFINITY, y1 = -INFINITY;
+    for (int j = t * kTile + lane; j < min(m, (t + 1) * kTile); j += 32) {
+        const float4 a = xy[j];
+        const double x = (double)a.x + (double)a.y, y = (double)a.z + (double)a.w;
+        x0 = fmin(x0, x); x1 = fmax(x1, x);
+        y0 = fmin(y0, y); y1 = fmax(y1, y);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        x0 = fmin(x0, __shfl_xor_sync(0xffffffffu, x0, o));
+        x1 = fmax(x1, __shfl_xor_sync(0xffffffffu, x1, o));
+        y0 = fmin(y0, __shfl_xor_sync(0xffffffffu, y0, o));
+        y1 = fmax(y1, __shfl_xor_sync(0xffffffffu, y1, o));
+    }
+    if (lane == 0) box[t] = make_float4(f32_down(x0), f32_up(x1), f32_down(y0), f32_up(y1));
+}
+
 // ---------------------------------------------------------------------------
 // CDM likelihood.  One warp per compacted chain slot, lanes over stations.
-// Station tiles stream through a ring of kStages shared-memory buffers filled
+// Station tiles stream through a ring of STAGES shared-memory buffers filled
 // by 1-D bulk copies: each warp waits on the buffer's full barrier, works
 // through the tile and counts itself done; the warp that finishes a tile last
-// refills that buffer with the tile kStages ahead.  No CTA-wide barrier is
-// taken per tile, so warps drift apart by up to kStages - 1 tiles instead of
+// refills that buffer with the tile STAGES ahead.  No CTA-wide barrier is
+// taken per tile, so warps drift apart by up to STAGES - 1 tiles instead of
 // waiting for the slowest one at every tile.
-constexpr int kStages = 4;
-
-template <int WARPS, int MINB, int SPL>
+template <int WARPS, int MINB, int SPL, int STAGES>
 __global__ void __launch_bounds__(WARPS * 32, MINB)
 cdm_llk_kernel(const ChainC* __restrict__ chains, const int32_t* __restrict__ slot_chain,
                const int32_t* __restrict__ nslots_ptr, int n, const float4* __restrict__ xy,
                const float4* __restrict__ losd, const float* __restrict__ wt,
-               const int32_t* __restrict__ oid, int m, int m_padded, double norm,
-               double* __restrict__ llk, float* __restrict__ resid, uint32_t* __restrict__ flags) {
+               const int32_t* __restrict__ oid, const float4* __restrict__ tile_box, int m, int m_padded,
+               double norm, double* __restrict__ llk, float* __restrict__ resid, uint32_t* __restrict__ flags) {
     const int nslots = min(n, *nslots_ptr);
     if ((int)(blockIdx.x * WARPS) >= nslots) return;       // whole CTA past the active chains
     __shared__ ChainC s_chain[WARPS];
-    __shared__ float4 s_xy[kStages][kTile];
-    __shared__ float4 s_ld[kStages][kTile];
-    __shared__ __align__(16) float s_w[kStages][kTile];
-    __shared__ __align__(16) int32_t s_oid[kStages][kTile];
-    __shared__ __align__(8) uint64_t full[kStages];
-    __shared__ int s_done[kStages];
+    __shared__ float4 s_xy[STAGES][kTile];
+    __shared__ float4 s_ld[STAGES][kTile];
+    __shared__ __align__(16) float s_w[STAGES][kTile];
+    __shared__ __align__(16) int32_t s_oid[STAGES][kTile];
+    __shared__ __align__(8) uint64_t full[STAGES];
+    __shared__ int s_done[STAGES];
     __shared__ int s_issued;
+    __shared__ float4 s_node[WARPS][kQuadBudget];     // each warp's nodes of the rectangle in hand
+    __shared__ float s_gx[136], s_gw[136];             // Gauss-Legendre rules (FP32)
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int slot = blockIdx.x * WARPS + warp;
@@ -210,6 +274,10 @@ cdm_llk_kernel(const ChainC* __restrict__ chains, const int32_t* __restrict__ sl
     const bool with_oid = (oid != nullptr);
     const uint32_t tile_bytes = kTile * (16u + 16u + 4u) + (with_oid ? kTile * 4u : 0u);
 
+    for (int k = threadIdx.x; k < 136; k += blockDim.x) {
+        s_gx[k] = kGaussXf[k];
+        s_gw[k] = kGaussWf[k];
+    }
     // this warp's chain constants
     if (active) {
         const float4* src = reinterpret_cast<const float4*>(chains + slot);
@@ -226,12 +294,12 @@ cdm_llk_kernel(const ChainC* __restrict__ chains, const int32_t* __restrict__ sl
         if (with_oid) bulk_g2s(&s_oid[buf][0], oid + base, kTile * 4u, &full[buf]);
     };
     if (threadIdx.x == 0) {
-        for (int b = 0; b < kStages; ++b) {
+        for (int b = 0; b < STAGES; ++b) {
             mbar_init(&full[b], 1);
             s_done[b] = 0;
         }
         fence_mbar_init();
-        const int first = ntiles < kStages ? ntiles : kStages;
+        const int first = ntiles < STAGES ? ntiles : STAGES;
         for (int t = 0; t < first; ++t) issue(t, t);
         s_issued = first;
     }
@@ -242,14 +310,38 @@ cdm_llk_kernel(const ChainC* __restrict__ chains, const int32_t* __restrict__ sl
     ff acc{0.f, 0.f};
     bool failed = false;
     for (int t = 0; t < ntiles; ++t) {
-        const int buf = t % kStages;
-        const uint32_t phase = (uint32_t)(t / kStages) & 1u;
+        const int buf = t % STAGES;
+        const uint32_t phase = (uint32_t)(t / STAGES) & 1u;
         const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(&full[buf], phase, kWaitLimit));
         if (!ok) {
             failed = true;
             break;
         }
         if (smask) {
+            // this tile's plan: the rectangles it integrates (node counts packed 5 + 5 bits per
+            // rectangle) and the sides of the others
+            const float4 tb = __ldg(tile_box + t);
+            const float bx0 = __fsub_rn(__fsub_rn(tb.x, x0h), x0l), bx1 = __fsub_rn(__fsub_rn(tb.y, x0h), x0l);
+            const float by0 = __fsub_rn(__fsub_rn(tb.z, y0h), y0l), by1 = __fsub_rn(__fsub_rn(tb.w, y0h), y0l);
+            uint32_t sides = smask & 0x0FFFu, qrect = 0u, qpack = 0u;
+#pragma unroll
+            for (int r = 0; r < 3; ++r) {
+                int n1, n2;
+                if ((smask >> (27 + r) & 1u) &&
+                    tile_quad(C.rect[r], (smask >> (24 + r)) & 1u, bx0, bx1, by0, by1, n1, n2)) {
+                    qrect |= 1u << r;
+                    qpack |= (uint32_t)(n1 | (n2 << 5)) << (10 * r);
+                    sides &= ~(0xFu << (4 * r));
+                }
+            }
+            // one rectangle's nodes into this warp's buffer (every lane reads all of them)
+            auto load_nodes = [&](int r) {
+                const int n1 = (qpack >> (10 * r)) & 31, n2 = (qpack >> (10 * r + 5)) & 31;
+                __syncwarp();
+                if (lane < n1 * n2) s_node[warp][lane] = rect_node(C.rect[r], n1, n2, lane, s_gx, s_gw);
+                __syncwarp();
+                return n1 * n2;
+            };
             // u projected on the LOS, minus data and offset; accumulate w r² and store r
             auto finish = [&](float e_, float n_, float v_, int j) {
                 const float4 B = s_ld[buf][j];
@@ -274,19 +366,20 @@ cdm_llk_kernel(const ChainC* __restrict__ chains, const int32_t* __restrict__ sl
                         Yr.v[q] = (A.z - y0h) + (A.w - y0l);
                     }
                     SV<SPL> ue(0.f), un(0.f), uv(0.f);
-                    uint32_t msk = smask & 0x0FFFu;
+                    uint32_t msk = sides;
 #pragma unroll 1
                     while (msk) {
                         const int sidx = __ffs(msk) - 1;
                         msk &= msk - 1;
                         side_pair<SV<SPL>>(ScalarSide(C.side[sidx]), Xr, Yr, ue, un, uv, (smask >> (kSides + sidx)) & 1u);
                     }
-                    uint32_t qm = (smask >> 24) & 7u;
+                    uint32_t qm = qrect;
 #pragma unroll 1
                     while (qm) {
                         const int r = __ffs(qm) - 1;
                         qm &= qm - 1;
-                        rect_quad<SV<SPL>>(*reinterpret_cast<const QuadC*>(&C.side[4 * r]), Xr, Yr, ue, un, uv);
+                        const int nn = load_nodes(r);
+                        rect_quad<SV<SPL>>(C.rect[r], s_node[warp], nn, Xr, Yr, ue, un, uv);
                     }
 #pragma unroll
                     for (int q = 0; q < SPL; ++q) finish(ue.v[q], un.v[q], uv.v[q], j0 + 32 * q);
@@ -297,19 +390,20 @@ cdm_llk_kernel(const ChainC* __restrict__ chains, const int32_t* __restrict__ sl
                     const float Xr = (A.x - x0h) + (A.y - x0l);
                     const float Yr = (A.z - y0h) + (A.w - y0l);
                     float ue = 0.f, un = 0.f, uv = 0.f;
-                    uint32_t msk = smask & 0x0FFFu;
+                    uint32_t msk = sides;
 #pragma unroll 1
                     while (msk) {
                         const int sidx = __ffs(msk) - 1;
                         msk &= msk - 1;
                         side_pair<float>(ScalarSide(C.side[sidx]), Xr, Yr, ue, un, uv, (smask >> (kSides + sidx)) & 1u);
                     }
-                    uint32_t qm = (smask >> 24) & 7u;
+                    uint32_t qm = qrect;
 #pragma unroll 1
                     while (qm) {
                         const int r = __ffs(qm) - 1;
                         qm &= qm - 1;
-                        rect_quad<float>(*reinterpret_cast<const QuadC*>(&C.side[4 * r]), Xr, Yr, ue, un, uv);
+                        const int nn = load_nodes(r);
+                        rect_quad<float>(C.rect[r], s_node[warp], nn, Xr, Yr, ue, un, uv);
                     }
                     finish(ue, un, uv, j);
                 }
@@ -322,9 +416,9 @@ cdm_llk_kernel(const ChainC* __restrict__ chains, const int32_t* __restrict__ sl
             if (atomicAdd(&s_done[buf], 1) == WARPS - 1) {
                 __threadfence_block();
                 s_done[buf] = 0;
-                if (t + kStages < ntiles) {
+                if (t + STAGES < ntiles) {
                     fence_proxy_async_smem();
-                    issue(t + kStages, buf);
+                    issue(t + STAGES, buf);
                     atomicAdd(&s_issued, 1);
                 }
             }
@@ -335,8 +429,8 @@ cdm_llk_kernel(const ChainC* __restrict__ chains, const int32_t* __restrict__ sl
         if (threadIdx.x == 0) {
             raise_flag(flags, DEV_ERR_TIMEOUT);
             const int last = s_issued;
-            for (int t = (last > kStages ? last - kStages : 0); t < last; ++t)
-                mbar_wait_bounded(&full[t % kStages], (uint32_t)(t / kStages) & 1u, kWaitLimit);
+            for (int t = (last > STAGES ? last - STAGES : 0); t < last; ++t)
+                mbar_wait_bounded(&full[t % STAGES], (uint32_t)(t / STAGES) & 1u, kWaitLimit);
         }
         return;
     }
@@ -449,8 +543,8 @@ using namespace ag;
 // CDM launch variants: warps (= chains) per CTA and resident CTAs per SM the
 // register allocation targets; chosen per problem by the autotuner
 struct CdmVariant { int warps; };
-static constexpr CdmVariant kCdmVariants[] = {{8}, {4}, {4}, {2}, {4}, {4}, {2}, {4}, {4}, {4}, {4}};
-static constexpr int kCdmVariantCount = 11;
+static constexpr CdmVariant kCdmVariants[] = {{8}, {4}, {4}, {2}, {4}, {4}, {2}, {4}, {4}, {4}, {4}, {1}, {1}, {1}, {2}};
+static constexpr int kCdmVariantCount = 15;
 // Mogi launch variants: chains per CTA held in registers (16, 8, 32)
 static constexpr int kMogiChainsOf[] = {16, 8, 32};
 static constexpr int kMogiVariantCount = 3;
@@ -512,6 +606,10 @@ static int forward_llk(int model, const ag_layout* layout, const double* theta, 
         const size_t need = ag_forward_workspace_bytes(model, n);
         AG_REQUIRE(workspace != nullptr && workspace_bytes >= need && aligned(workspace, 256),
                    "CDM needs %zu bytes of 256-byte aligned workspace", need);
+        AG_REQUIRE(st->tile_box != nullptr && aligned(st->tile_box, 16),
+                   "the CDM needs the stations' tile boxes (ag_station_boxes), 16-byte aligned");
+        const float4* tile_box = reinterpret_cast<const float4*>(st->tile_box);
+        const int ntiles = st->m_padded / AG_STATION_TILE;
         ChainC* chains = reinterpret_cast<ChainC*>(workspace);
         int32_t* slot_chain = reinterpret_cast<int32_t*>(static_cast<char*>(workspace) +
                                                          al256((size_t)n * sizeof(ChainC)));
@@ -521,7 +619,8 @@ static int forward_llk(int model, const ag_layout* layout, const double* theta, 
         int32_t* nslots = &hdr->nslots;
         rc = cuda_status(cudaMemsetAsync(hdr, 0, sizeof(SetupHdr), s), "cudaMemsetAsync(set-up header)");
         if (rc) return rc;
-        cdm_cost_kernel<<<(n + 127) / 128, 128, 0, s>>>(L, theta, n, mask_in, chain_status, index, count, key, hdr);
+        cdm_cost_kernel<<<(n + 127) / 128, 128, 0, s>>>(L, theta, n, mask_in, chain_status, index, count, tile_box,
+                                                        ntiles, key, hdr);
         rc = launch_status("cdm_cost_kernel");
         if (rc) return rc;
         cdm_setup_kernel<<<(n + 127) / 128, 128, 0, s>>>(L, theta, n, key, chains, noffsets, index, count,
@@ -532,21 +631,28 @@ static int forward_llk(int model, const ag_layout* layout, const double* theta, 
         AG_REQUIRE(v >= 0 && v < kCdmVariantCount, "CDM variant %d out of range [0, %d)", v, kCdmVariantCount);
         const int warps = kCdmVariants[v].warps;
         const int grid = (n + warps - 1) / warps;
-#define AG_CDM_LAUNCH(W, B, SPL)                                                                    \
-    cdm_llk_kernel<W, B, SPL><<<grid, W * 32, 0, s>>>(chains, slot_chain, nslots, n, xy, ld, st->weight, \
-                                                      st->oid, st->m, st->m_padded, norm, llk, residuals, nullptr)
+#define AG_CDM_LAUNCH(W, B, SPL, ST)                                                                    \
+    cdm_llk_kernel<W, B, SPL, ST><<<grid, W * 32, 0, s>>>(chains, slot_chain, nslots, n, xy, ld, st->weight, \
+                                                          st->oid, tile_box, st->m, st->m_padded, norm, llk,     \
+                                                          residuals, nullptr)
+        // warps per CTA, CTAs per SM, stations per lane, ring depth; a CTA of one warp has its
+        // own ring, so its chain never waits for another chain's tiles
         switch (v) {
-            case 0: AG_CDM_LAUNCH(8, 2, 1); break;
-            case 1: AG_CDM_LAUNCH(4, 4, 1); break;
-            case 2: AG_CDM_LAUNCH(4, 5, 1); break;
-            case 3: AG_CDM_LAUNCH(2, 8, 1); break;
-            case 4: AG_CDM_LAUNCH(4, 3, 2); break;
-            case 5: AG_CDM_LAUNCH(4, 4, 2); break;
-            case 6: AG_CDM_LAUNCH(2, 6, 2); break;
-            case 7: AG_CDM_LAUNCH(4, 2, 4); break;
-            case 8: AG_CDM_LAUNCH(4, 3, 4); break;
-            case 9: AG_CDM_LAUNCH(4, 4, 4); break;
-            default: AG_CDM_LAUNCH(4, 5, 4); break;
+            case 0: AG_CDM_LAUNCH(8, 2, 1, 4); break;
+            case 1: AG_CDM_LAUNCH(4, 4, 1, 4); break;
+            case 2: AG_CDM_LAUNCH(4, 5, 1, 4); break;
+            case 3: AG_CDM_LAUNCH(2, 8, 1, 4); break;
+            case 4: AG_CDM_LAUNCH(4, 3, 2, 4); break;
+            case 5: AG_CDM_LAUNCH(4, 4, 2, 4); break;
+            case 6: AG_CDM_LAUNCH(2, 6, 2, 4); break;
+            case 7: AG_CDM_LAUNCH(4, 2, 4, 4); break;
+            case 8: AG_CDM_LAUNCH(4, 3, 4, 4); break;
+            case 9: AG_CDM_LAUNCH(4, 4, 4, 4); break;
+            case 10: AG_CDM_LAUNCH(4, 5, 4, 4); break;
+            case 11: AG_CDM_LAUNCH(1, 12, 4, 2); break;
+            case 12: AG_CDM_LAUNCH(1, 12, 4, 3); break;
+            case 13: AG_CDM_LAUNCH(1, 10, 4, 3); break;
+            default: AG_CDM_LAUNCH(2, 6, 4, 3); break;
         }
 #undef AG_CDM_LAUNCH
         return launch_status("cdm_llk_kernel");
@@ -593,15 +699,30 @@ extern "C" int ag_forward_llk_subset(int model, const ag_layout* layout, const d
                        residuals, workspace, workspace_bytes, stream);
 }
 
-extern "C" int ag_cdm_work(const ag_layout* layout, const double* theta, int32_t n, uint32_t* flop_per_station,
-                           uint32_t* sfu_per_station, void* stream) {
-    AG_REQUIRE(layout && theta && flop_per_station && n > 0, "invalid arguments");
+extern "C" int ag_cdm_work(const ag_layout* layout, const double* theta, int32_t n, const ag_station_set* st,
+                           double* flop, double* sfu, void* stream) {
+    AG_REQUIRE(layout && theta && flop && n > 0, "invalid arguments");
+    int rc = check_stations(st);
+    if (rc) return rc;
+    AG_REQUIRE(st->tile_box != nullptr && aligned(st->tile_box, 16),
+               "the CDM needs the stations' tile boxes (ag_station_boxes), 16-byte aligned");
     const ag_layout L = *layout;
     AG_REQUIRE(L.nparams > 0 && L.axes_idx >= 0 && L.axes_idx + 2 < L.nparams && L.omega_idx >= 0 &&
                    L.omega_idx + 2 < L.nparams,
                "invalid CDM layout");
-    cdm_work_kernel<<<(n + 127) / 128, 128, 0, as_stream(stream)>>>(L, theta, n, flop_per_station, sfu_per_station);
+    cdm_work_kernel<<<(n + 127) / 128, 128, 0, as_stream(stream)>>>(
+        L, theta, n, reinterpret_cast<const float4*>(st->tile_box), st->m, flop, sfu);
     return launch_status("cdm_work_kernel");
+}
+
+extern "C" int ag_station_boxes(const float* xy, int32_t m, int32_t m_padded, float* tile_box, void* stream) {
+    AG_REQUIRE(xy && tile_box && m > 0 && m_padded >= m && m_padded % AG_STATION_TILE == 0,
+               "invalid arguments (m=%d, m_padded=%d must be a multiple of %d)", m, m_padded, AG_STATION_TILE);
+    AG_REQUIRE(aligned(xy, 16) && aligned(tile_box, 16), "xy and tile_box must be 16-byte aligned");
+    const int ntiles = m_padded / AG_STATION_TILE;
+    station_boxes_kernel<<<(ntiles + 7) / 8, 256, 0, as_stream(stream)>>>(
+        reinterpret_cast<const float4*>(xy), m, ntiles, reinterpret_cast<float4*>(tile_box));
+    return launch_status("station_boxes_kernel");
 }
 
 extern "C" int ag_cdm_check(const ag_layout* layout, const double* theta, int32_t n,

@@ -75,10 +75,14 @@ class Stations:
             self.oid = torch.from_numpy(o).to(DEVICE)
         else:
             self.oid = None
+        # bounding box of each tile of stations (the CDM picks its quadrature per tile)
+        self.tile_box = torch.empty(mp // tile, 4, dtype=torch.float32, device=DEVICE)
+        _native.call("ag_station_boxes", ctypes.c_void_p(self.xy.data_ptr()), m, mp,
+                     ctypes.c_void_p(self.tile_box.data_ptr()), stream_handle())
         self._struct = _native.StationSet(self.xy.data_ptr(), self.losd.data_ptr(),
                                           self.weight.data_ptr(),
                                           self.oid.data_ptr() if self.oid is not None else None,
-                                          m, mp)
+                                          m, mp, self.tile_box.data_ptr())
 
     @property
     def struct(self):

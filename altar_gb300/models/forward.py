@@ -90,13 +90,14 @@ class CUDA:
         return out
 
     def work(self, theta, stream=None):
-        """CDM: FP32 operations (FMA = 2) and special-function operations per station that the
-        likelihood kernel executes for each row of device θ (0 above the free surface)."""
+        """CDM: FP32 operations (FMA = 2) and special-function operations that the likelihood
+        kernel executes for each row of device θ over the m stations, tile by tile (0 above the
+        free surface)."""
         n = theta.shape[0]
-        flop = torch.empty(n, dtype=torch.int32, device=theta.device)
-        sfu = torch.empty(n, dtype=torch.int32, device=theta.device)
-        _native.call("ag_cdm_work", ctypes.byref(self.layout), ptr(theta), n, ptr(flop), ptr(sfu),
-                     stream_handle(stream))
+        flop = torch.empty(n, dtype=torch.float64, device=theta.device)
+        sfu = torch.empty(n, dtype=torch.float64, device=theta.device)
+        _native.call("ag_cdm_work", ctypes.byref(self.layout), ptr(theta), n, self.stations.struct, ptr(flop),
+                     ptr(sfu), stream_handle(stream))
         return flop, sfu
 
     def dataLikelihood(self, model, step):

@@ -37,11 +37,12 @@ LOS = (0.38, -0.08, 0.92)
 PRIORS = [(-1e4, 1e4), (-1e4, 1e4), (1e3, 1e4), (-50.0, 50.0), (100.0, 3000.0), (100.0, 3000.0),
           (100.0, 3000.0), (-90.0, 90.0), (-90.0, 90.0), (-90.0, 90.0)]
 # parameter order: x0, y0, depth, opening, ax, ay, az, ωx, ωy, ωz
-# FP32 work of the fused CDM kernel: per (chain, station) pair it is the chain's plan, summed
-# by the library (ag_cdm_work): 251 FLOP (FMA = 2) and 13 special-function operations per
-# rectangle side evaluated as an angular-dislocation pair (78 FLOP and 3 more for a
-# near-vertical side), 19 + 48 per node for a rectangle integrated by quadrature, + 31 per
-# station; the constants are counted from the source by tests/cdm_host/cdm_host.cpp
+# FP32 work of the fused CDM kernel: per (chain, station) pair it is the plan of the chain over
+# the station's tile, summed by the library (ag_cdm_work): 251 FLOP (FMA = 2) and 13
+# special-function operations per rectangle side evaluated as an angular-dislocation pair (78
+# FLOP and 3 more for a near-vertical side), 19 + 48 per node for a rectangle integrated by
+# quadrature, + 31 per station; the constants are counted from the source by
+# tests/cdm_host/cdm_host.cpp
 L2_FLUSH_BYTES = 256 << 20
 
 
@@ -832,7 +833,7 @@ def run_ours(args):
         pairs = n * X.size
         flop_chain, sfu_chain = model.strategy.work(th_all, stream=stream)
         torch.cuda.synchronize()
-        flop_launch = float(flop_chain.double().sum().item()) * X.size
+        flop_launch = float(flop_chain.sum().item())         # per chain: summed over the stations
         evaluated_pairs = int((flop_chain > 0).sum().item()) * X.size
         achieved = flop_launch / t_fwd / 1e12
         pk = peaks()
@@ -902,7 +903,8 @@ def run_ours(args):
                      "frac": achieved / fp32_peak, "traffic": profile_traffic,
                      "kernel": "cdm_setup_kernel + cdm_llk_kernel",
                      "flop_per_launch": flop_launch, "flop_per_pair": flop_launch / max(1, evaluated_pairs),
-                     "flop_source": "per-chain plan summed by ag_cdm_work (sides and quadrature nodes)",
+                     "flop_source": "plan of each chain over each station tile, summed by ag_cdm_work "
+                                    "(sides and quadrature nodes)",
                      "pairs_per_launch": pairs, "evaluated_pairs_per_launch": evaluated_pairs,
                      "ms_per_launch": t_fwd * 1e3, "sms": sms,
                      "peak_source": "nominal FP32 FMA rate at the measured max SM clock "

@@ -65,7 +65,19 @@ typedef struct ag_station_set {
     const int32_t* oid;    /* [m_padded]: dataset id, selects θ[offset_idx + oid]; NULL = none */
     int32_t m;             /* number of observations */
     int32_t m_padded;      /* multiple of AG_STATION_TILE */
+    const float* tile_box; /* [m_padded / AG_STATION_TILE][4]: x min, x max, y min, y max of each tile's
+                              observations, rounded outwards (ag_station_boxes); needed by the CDM,
+                              which picks its quadrature per tile; NULL for Mogi */
 } ag_station_set;
+
+/*
+ * Fills tile_box from xy: the bounding box of each tile of AG_STATION_TILE
+ * consecutive observations (padding left out), rounded outwards to FP32.  No
+ * counterpart in the reference.  Observations ordered so that consecutive ones
+ * lie close together (rows of a grid, a space-filling order) give small boxes
+ * and let the CDM integrate more of its rectangles with few nodes.
+ */
+int ag_station_boxes(const float* xy, int32_t m, int32_t m_padded, float* tile_box, void* stream);
 
 /*
  * Parameter layout of a sample row.  Replaces libcudacdm.layout
@@ -135,14 +147,14 @@ int ag_forward_llk_subset(int model, const ag_layout* layout, const double* thet
                           float* residuals, void* workspace, size_t workspace_bytes, void* stream);
 
 /*
- * Work of the CDM likelihood kernel per station for each chain: the FP32
- * operations (FMA = 2) and special-function operations its plan executes
- * (rectangles evaluated by their sides or, far from the free surface, by
+ * Work of the CDM likelihood kernel for each chain over the stations' m
+ * observations: the FP32 operations (FMA = 2) and special-function operations
+ * its plan executes, tile by tile (rectangles evaluated by their sides or by
  * quadrature nodes); 0 for chains above the free surface.  For roofline
- * accounting; sfu_per_station may be NULL.  No counterpart in the reference.
+ * accounting; sfu may be NULL.  No counterpart in the reference.
  */
-int ag_cdm_work(const ag_layout* layout, const double* theta, int32_t n, uint32_t* flop_per_station,
-                uint32_t* sfu_per_station, void* stream);
+int ag_cdm_work(const ag_layout* layout, const double* theta, int32_t n, const ag_station_set* stations,
+                double* flop, double* sfu, void* stream);
 
 /*
  * CDM geometry check only: chain_status[i] |= AG_CHAIN_ABOVE_SURFACE where a

@@ -42,8 +42,8 @@ def host(tmp_path_factory):
     lib.cdm_host_side_counts.argtypes = [P(ctypes.c_long)] * 4
     lib.cdm_host_quad_counts.argtypes = [P(ctypes.c_long)] * 4
     lib.cdm_host_work_constants.argtypes = [P(ctypes.c_int)]
-    lib.cdm_host_plan.argtypes = [P(ctypes.c_double), ctypes.c_double, P(ctypes.c_uint32), P(ctypes.c_int),
-                                  P(ctypes.c_uint32), P(ctypes.c_uint32)]
+    lib.cdm_host_plan.argtypes = [P(ctypes.c_double), ctypes.c_double, P(ctypes.c_float), ctypes.c_int,
+                                  P(ctypes.c_uint32), P(ctypes.c_int), P(ctypes.c_double), P(ctypes.c_double)]
     return lib
 
 
@@ -75,18 +75,57 @@ def test_flop_counts_match_library_constants(host):
     assert k["station"] == 31
 
 
-def _plan(host, th):
-    m, f, u = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32()
+def _plan(host, th, box=None, m=1):
+    """Plan of one source and the work over m stations in tiles with the given boxes (default:
+    one station at the source centre, the tile closest to every rectangle)."""
+    mask, f, u = ctypes.c_uint32(), ctypes.c_double(), ctypes.c_double()
     nq = (ctypes.c_int * 6)()
     t = np.ascontiguousarray(th, dtype=np.float64)
-    assert host.cdm_host_plan(_dp(t), 0.25, ctypes.byref(m), nq, ctypes.byref(f), ctypes.byref(u)) == 0
-    return m.value, np.array(list(nq)).reshape(3, 2), f.value
+    if box is None:
+        box = np.array([[th[0], th[0], th[1], th[1]]], dtype=np.float32)
+    box = np.ascontiguousarray(box, dtype=np.float32)
+    assert host.cdm_host_plan(_dp(t), 0.25, box.ctypes.data_as(P(ctypes.c_float)), m, ctypes.byref(mask), nq,
+                              ctypes.byref(f), ctypes.byref(u)) == 0
+    return mask.value, np.array(list(nq)).reshape(3, 2), f.value
+
+
+def _thresholds():
+    import re
+    text = open(os.path.join(HERE, "..", "altar_gb300", "csrc", "cdm_side.cuh")).read()
+    body = re.search(r"kQuadDelta2\[kGaussMax\] = \{([^}]*)\}", text).group(1)
+    return np.array([float(v.strip().rstrip("f")) for v in body.replace("\n", " ").split(",") if v.strip()],
+                    dtype=np.float32)
+
+
+def _nodes(delta2):
+    """Smallest n with δ² >= δ_n² (17 if none), as the library's threshold search."""
+    T = _thresholds().astype(np.float64)
+    for n in range(1, 17):
+        if delta2 >= T[n - 1]:
+            return n
+    return 17
+
+
+def test_quadrature_thresholds():
+    """δ_n² is the smallest δ² at which n nodes per direction meet ρ^(-2n) <= 1e-7
+    (ρ = δ + sqrt(δ² + 1)), rounded up to FP32: n - 1 nodes do not meet it there."""
+    T = _thresholds().astype(np.float64)
+    for n in range(1, 17):
+        d = np.sqrt(T[n - 1])
+        rho = d + np.sqrt(d * d + 1)
+        assert rho ** (-2 * n) <= 1e-7 * (1 + 1e-6)
+        if n > 1:
+            assert rho ** (-2 * (n - 1)) > 1e-7
+        rho_n = 1e-7 ** (-1.0 / (2 * n))
+        exact = ((rho_n - 1 / rho_n) / 2) ** 2
+        assert exact <= T[n - 1] <= exact * (1 + 2 ** -22)
 
 
 def test_plan_quadrature_far_rectangles(host):
-    """A rectangle is integrated with n1 x n2 nodes, n_i the smallest n with
-    ρ_i^(-2n) <= 1e-7 (ρ = δ + sqrt(δ² + 1), δ = depth of the shallowest corner / half
-    side), when n1 n2 <= 32; otherwise its sides are evaluated."""
+    """A rectangle is integrated everywhere ("far") with n1 x n2 nodes, n_i the smallest n
+    with ρ_i^(-2n) <= 1e-7 (ρ = δ + sqrt(δ² + 1), δ = depth of the shallowest corner / half
+    side), when n1 n2 <= 32; otherwise its sides are evaluated (over the tiles where they
+    cost less than the quadrature: here a tile at the source, the same as the chain plan)."""
     from oracle import cdm as ocdm
     k = _constants(host)
     nquad = 0
@@ -98,7 +137,7 @@ def test_plan_quadrature_far_rectangles(host):
             h1 = np.linalg.norm(V[r][1] - V[r][0]) / 2
             h2 = np.linalg.norm(V[r][3] - V[r][0]) / 2
             D = -V[r][:, 2].max()
-            n = [int(np.ceil(np.log(1e7) / (2 * np.log(d + np.sqrt(d * d + 1))))) for d in (D / h1, D / h2)]
+            n = [_nodes((D * D) / (h * h)) for h in (h1, h2)]
             quad = max(n) <= 16 and n[0] * n[1] <= 32
             assert bool(mask >> (24 + r) & 1) == quad
             sides = (mask >> (4 * r)) & 0xF

@@ -100,8 +100,10 @@ def test_cdm_prior_sources_workload_grid(cuda):
 
 
 def test_cdm_work_count_matches_host_plan(cuda):
-    """ag_cdm_work (the roofline's FLOP count) follows the same per-chain plan as the set-up
-    kernel: against the host build of that plan, and 0 for a source above the surface."""
+    """ag_cdm_work (the roofline's FLOP count) follows the likelihood kernel's plan tile by
+    tile: against the host build of that plan over the same tile boxes (ag_station_boxes),
+    and 0 for a source above the surface.  On the workload's grid the far tiles integrate
+    most rectangles with a few nodes, below the work of the chain plan alone."""
     import ctypes
     import shutil
     import subprocess
@@ -115,20 +117,33 @@ def test_cdm_work_count_matches_host_plan(cuda):
                     os.path.join(here, "cdm_host", "cdm_host.cpp"), "-o", so], check=True)
     host = ctypes.CDLL(so)
     P = ctypes.POINTER
+    host.cdm_host_plan.argtypes = [P(ctypes.c_double), ctypes.c_double, P(ctypes.c_float), ctypes.c_int,
+                                   P(ctypes.c_uint32), P(ctypes.c_int), P(ctypes.c_double), P(ctypes.c_double)]
     theta = cdm_prior_rows(200, seed=31)
     theta = np.concatenate([theta, [[0, 0, 200.0, 1.0, 2000, 2000, 2000, 0, 0, 0]]])
-    X = np.linspace(-1e3, 1e3, 8)
-    strat, _ = cdm_strategy(X, X, np.tile(LOS, (X.size, 1)), np.zeros(X.size), np.ones(X.size))
+    g = np.linspace(-20e3, 20e3, 200)
+    X, Y = [a.ravel() for a in np.meshgrid(g, g)]
+    strat, _ = cdm_strategy(X, Y, np.tile(LOS, (X.size, 1)), np.zeros(X.size), np.ones(X.size))
     flop, sfu = strat.work(dev(theta))
     flop = flop.cpu().numpy()
+    box = np.ascontiguousarray(strat.stations.tile_box.cpu().numpy())
     assert flop[-1] == 0
+    chain_only = []
     for k, th in enumerate(theta[:-1]):
-        m, f, u = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32()
+        mask, f, u = ctypes.c_uint32(), ctypes.c_double(), ctypes.c_double()
         nq = (ctypes.c_int * 6)()
         t = np.ascontiguousarray(th)
-        assert host.cdm_host_plan(t.ctypes.data_as(P(ctypes.c_double)), ctypes.c_double(0.25), ctypes.byref(m),
-                                  nq, ctypes.byref(f), ctypes.byref(u)) == 0
+        assert host.cdm_host_plan(t.ctypes.data_as(P(ctypes.c_double)), 0.25, box.ctypes.data_as(P(ctypes.c_float)),
+                                  X.size, ctypes.byref(mask), nq, ctypes.byref(f), ctypes.byref(u)) == 0
         assert flop[k] == f.value, k
+        # the chain plan alone: every tile as close as the source centre
+        b0 = np.array([[th[0], th[0], th[1], th[1]]], dtype=np.float32)
+        assert host.cdm_host_plan(t.ctypes.data_as(P(ctypes.c_double)), 0.25, b0.ctypes.data_as(P(ctypes.c_float)),
+                                  1, ctypes.byref(mask), nq, ctypes.byref(f), ctypes.byref(u)) == 0
+        chain_only.append(f.value * X.size)
+    ratio = np.sum(chain_only) / np.sum(flop[:-1])
+    print(f"\nwork of the chain plan / work of the tile plan on the 40,000-station grid: {ratio:.2f}")
+    assert ratio > 1.2
 
 
 def test_cdm_launch_variants_identical(cuda):
