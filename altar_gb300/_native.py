@@ -88,7 +88,7 @@ AG_STATION_TILE = 128
 
 class StationSet(ctypes.Structure):
     _fields_ = [("xy", c_void_p), ("losd", c_void_p), ("weight", c_void_p), ("oid", c_void_p),
-                ("m", c_int32), ("m_padded", c_int32), ("tile_box", c_void_p)]
+                ("m", c_int32), ("m_padded", c_int32), ("tile_box", c_void_p), ("order", c_void_p)]
 
 
 class Layout(ctypes.Structure):

@@ -487,7 +487,7 @@ class DelayedAcceptance(Metropolis):
         res = torch.zeros(n, strat.stations.m_padded, dtype=torch.float32, device=DEVICE)
         out = torch.empty(n, dtype=torch.float64, device=DEVICE)
         strat.forward(theta, out, residuals=res)
-        return res + strat.stations.losd[:, 3]
+        return res + strat.stations.data_rows
 
     def _set_bounds(self, step):
         th = step.theta
@@ -506,7 +506,7 @@ class DelayedAcceptance(Metropolis):
         th = step.theta.index_select(0, rows).contiguous()
         self._set_bounds(step)
         fields = self._fields(strat, th)
-        sur.fit_basis(fields, strat.stations.weight, strat.stations.losd[:, 3], strat.norm)
+        sur.fit_basis(fields, strat.stations.weight_rows, strat.stations.data_rows, strat.norm)
         p = step.parameters
         x = torch.empty(th.shape[0], p, dtype=torch.float32, device=DEVICE)
         _native.call("ag_normalize_inputs", ptr(th), th.shape[0], p, ptr(self._bounds[0]), ptr(self._bounds[1]),
@@ -527,7 +527,7 @@ class DelayedAcceptance(Metropolis):
         tmp = torch.empty(th.shape[0], dtype=torch.float64, device=DEVICE)
         sur.predict(th, self._bounds[0], self._bounds[1], tmp, bufs)
         approx = sur.reconstruct(bufs[1])
-        w = strat.stations.weight
+        w = strat.stations.weight_rows
         err2 = ((approx - exact) ** 2 * w).sum(1) / strat.stations.m
         return float(torch.sqrt(err2.mean()))
 

@@ -251,8 +251,9 @@ __global__ void __launch_bounds__(WARPS * 32, MINB)
 cdm_llk_kernel(const ChainC* __restrict__ chains, const int32_t* __restrict__ slot_chain,
                const int32_t* __restrict__ nslots_ptr, int n, const float4* __restrict__ xy,
                const float4* __restrict__ losd, const float* __restrict__ wt,
-               const int32_t* __restrict__ oid, const float4* __restrict__ tile_box, int m, int m_padded,
-               double norm, double* __restrict__ llk, float* __restrict__ resid, uint32_t* __restrict__ flags) {
+               const int32_t* __restrict__ oid, const float4* __restrict__ tile_box,
+               const int32_t* __restrict__ order, int m, int m_padded, double norm, double* __restrict__ llk,
+               float* __restrict__ resid, uint32_t* __restrict__ flags) {
     const int nslots = min(n, *nslots_ptr);
     if ((int)(blockIdx.x * WARPS) >= nslots) return;       // whole CTA past the active chains
     __shared__ ChainC s_chain[WARPS];
@@ -260,6 +261,7 @@ cdm_llk_kernel(const ChainC* __restrict__ chains, const int32_t* __restrict__ sl
     __shared__ float4 s_ld[STAGES][kTile];
     __shared__ __align__(16) float s_w[STAGES][kTile];
     __shared__ __align__(16) int32_t s_oid[STAGES][kTile];
+    __shared__ float4 s_box[STAGES];                  // each tile's bounding box, with the tile
     __shared__ __align__(8) uint64_t full[STAGES];
     __shared__ int s_done[STAGES];
     __shared__ int s_issued;
@@ -272,7 +274,7 @@ cdm_llk_kernel(const ChainC* __restrict__ chains, const int32_t* __restrict__ sl
     const int chain = active ? slot_chain[slot] : n;
     const int ntiles = m_padded / kTile;
     const bool with_oid = (oid != nullptr);
-    const uint32_t tile_bytes = kTile * (16u + 16u + 4u) + (with_oid ? kTile * 4u : 0u);
+    const uint32_t tile_bytes = kTile * (16u + 16u + 4u) + (with_oid ? kTile * 4u : 0u) + 16u;
 
     for (int k = threadIdx.x; k < 136; k += blockDim.x) {
         s_gx[k] = kGaussXf[k];
@@ -292,6 +294,7 @@ cdm_llk_kernel(const ChainC* __restrict__ chains, const int32_t* __restrict__ sl
         bulk_g2s(&s_ld[buf][0], losd + base, kTile * 16u, &full[buf]);
         bulk_g2s(&s_w[buf][0], wt + base, kTile * 4u, &full[buf]);
         if (with_oid) bulk_g2s(&s_oid[buf][0], oid + base, kTile * 4u, &full[buf]);
+        bulk_g2s(&s_box[buf], tile_box + t, 16u, &full[buf]);
     };
     if (threadIdx.x == 0) {
         for (int b = 0; b < STAGES; ++b) {
@@ -320,7 +323,7 @@ cdm_llk_kernel(const ChainC* __restrict__ chains, const int32_t* __restrict__ sl
         if (smask) {
             // this tile's plan: the rectangles it integrates (node counts packed 5 + 5 bits per
             // rectangle) and the sides of the others
-            const float4 tb = __ldg(tile_box + t);
+            const float4 tb = s_box[buf];
             const float bx0 = __fsub_rn(__fsub_rn(tb.x, x0h), x0l), bx1 = __fsub_rn(__fsub_rn(tb.y, x0h), x0l);
             const float by0 = __fsub_rn(__fsub_rn(tb.z, y0h), y0l), by1 = __fsub_rn(__fsub_rn(tb.w, y0h), y0l);
             uint32_t sides = smask & 0x0FFFu, qrect = 0u, qpack = 0u;
@@ -352,7 +355,7 @@ cdm_llk_kernel(const ChainC* __restrict__ chains, const int32_t* __restrict__ sl
                 if (w != 0.f) ff_add_wsq(acc, r, w);
                 if (resid) {
                     const int col = t * kTile + j;
-                    resid[(size_t)chain * m_padded + col] = (col < m) ? r : 0.f;
+                    resid[(size_t)chain * m_padded + (order ? __ldg(order + col) : col)] = (col < m) ? r : 0.f;
                 }
             };
             if constexpr (SPL > 1) {
@@ -450,9 +453,9 @@ __global__ void __launch_bounds__(256, 2)
 mogi_llk_kernel(ag_layout L, const double* __restrict__ theta, int n,
                 const uint32_t* __restrict__ mask_in, const float4* __restrict__ xy,
                 const float4* __restrict__ losd, const float* __restrict__ wt,
-                const int32_t* __restrict__ oid, int noffsets, int m, int m_padded, double norm,
-                double* __restrict__ llk, float* __restrict__ resid, const int32_t* __restrict__ index,
-                const int32_t* __restrict__ count) {
+                const int32_t* __restrict__ oid, const int32_t* __restrict__ order, int noffsets, int m,
+                int m_padded, double norm, double* __restrict__ llk, float* __restrict__ resid,
+                const int32_t* __restrict__ index, const int32_t* __restrict__ count) {
     if (index && (int)(blockIdx.x * CH) >= *count) return;
     __shared__ MogiSrc s_src[CH][NSRC];
     __shared__ int s_chain[CH];
@@ -516,7 +519,8 @@ mogi_llk_kernel(ag_layout L, const double* __restrict__ theta, int n,
             float r = u - B.w;
             if (oid) r -= s_off[c][o];
             if (w != 0.f) ff_add_wsq(acc[c], r, w);
-            if (resid && s_chain[c] < n) resid[(size_t)s_chain[c] * m_padded + j] = (j < m) ? r : 0.f;
+            if (resid && s_chain[c] < n)
+                resid[(size_t)s_chain[c] * m_padded + (order ? __ldg(order + j) : j)] = (j < m) ? r : 0.f;
         }
     }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -571,8 +575,8 @@ static int check_stations(const ag_station_set* st) {
                "m=%d m_padded=%d: m_padded must be a multiple of %d and >= m", st->m,
                st->m_padded, AG_STATION_TILE);
     AG_REQUIRE(aligned(st->xy, 16) && aligned(st->losd, 16) && aligned(st->weight, 16) &&
-                   (st->oid == nullptr || aligned(st->oid, 16)),
-               "station arrays must be 16-byte aligned");
+                   (st->oid == nullptr || aligned(st->oid, 16)) && (st->order == nullptr || aligned(st->order, 4)),
+               "station arrays must be 16-byte aligned (order 4-byte)");
     return AG_OK;
 }
 
@@ -633,8 +637,8 @@ static int forward_llk(int model, const ag_layout* layout, const double* theta, 
         const int grid = (n + warps - 1) / warps;
 #define AG_CDM_LAUNCH(W, B, SPL, ST)                                                                    \
     cdm_llk_kernel<W, B, SPL, ST><<<grid, W * 32, 0, s>>>(chains, slot_chain, nslots, n, xy, ld, st->weight, \
-                                                          st->oid, tile_box, st->m, st->m_padded, norm, llk,     \
-                                                          residuals, nullptr)
+                                                          st->oid, tile_box, st->order, st->m, st->m_padded,     \
+                                                          norm, llk, residuals, nullptr)
         // warps per CTA, CTAs per SM, stations per lane, ring depth; a CTA of one warp has its
         // own ring, so its chain never waits for another chain's tiles
         switch (v) {
@@ -664,8 +668,8 @@ static int forward_llk(int model, const ag_layout* layout, const double* theta, 
         const int ch = kMogiChainsOf[L.variant];
         const int grid = (n + ch - 1) / ch;
 #define AG_MOGI_LAUNCH(CH, NS)                                                                               \
-    mogi_llk_kernel<CH, NS><<<grid, 256, 0, s>>>(L, theta, n, mask_in, xy, ld, st->weight, st->oid, noffsets, \
-                                                 st->m, st->m_padded, norm, llk, residuals, index, count)
+    mogi_llk_kernel<CH, NS><<<grid, 256, 0, s>>>(L, theta, n, mask_in, xy, ld, st->weight, st->oid, st->order, \
+                                                 noffsets, st->m, st->m_padded, norm, llk, residuals, index, count)
         if (L.nsources == 1) {
             if (ch == 8) AG_MOGI_LAUNCH(8, 1);
             else if (ch == 32) AG_MOGI_LAUNCH(32, 1);

@@ -38,7 +38,11 @@ class CUDA:
         obs = model.obs
         dense = getattr(obs, "dense", False)
         weight = np.zeros(obs.observations) if dense else 1.0 / obs.variance
-        self.stations = Stations(obs.x, obs.y, obs.los, obs.d, weight, obs.oid)
+        # the CDM stores its stations along a Hilbert curve (compact tiles, fewer quadrature
+        # nodes); residual rows keep the caller's order.  Dense Cd whitens residual rows in
+        # place, which wants them written in order: no reordering there.
+        reorder = self.kind == _native.AG_MODEL_CDM and not dense
+        self.stations = Stations(obs.x, obs.y, obs.los, obs.d, weight, obs.oid, reorder=reorder)
         self.layout = model.layout()
         self.norm = obs.normalization()
         if dense:

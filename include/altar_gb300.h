@@ -68,6 +68,10 @@ typedef struct ag_station_set {
     const float* tile_box; /* [m_padded / AG_STATION_TILE][4]: x min, x max, y min, y max of each tile's
                               observations, rounded outwards (ag_station_boxes); needed by the CDM,
                               which picks its quadrature per tile; NULL for Mogi */
+    const int32_t* order;  /* [m_padded]: column of stored observation j in the caller's order, for the
+                              residual rows (a permutation with order[j] = j for j >= m); NULL = the
+                              stored order.  Storing the observations along a space-filling curve
+                              makes the CDM's tiles compact: fewer quadrature nodes per station */
 } ag_station_set;
 
 /*
