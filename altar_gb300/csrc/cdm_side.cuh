@@ -361,7 +361,7 @@ AG_CDM_FN float f32_up(double v) {
 constexpr int kFlopSide = 251;          // one angular-dislocation pair
 constexpr int kFlopSteepExtra = 78;     // near-vertical pair: remainders of the cot β terms
 constexpr int kFlopQuadRect = 19;       // quadrature rectangle: strike frame, q, back to EFCS
-constexpr int kFlopQuadNode = 48;       // one point tensile dislocation, weighted sum
+constexpr int kFlopQuadNode = 45;       // one point tensile dislocation, weighted sum
 constexpr int kFlopStation = 31;        // coordinates, LOS projection, residual, float-float misfit
 constexpr int kSfuSide = 13, kSfuSteepExtra = 3, kSfuQuadNode = 2;
 
@@ -853,10 +853,11 @@ AG_DEVICE_INLINE void side_pair(const K& k, V Xr, V Yr, V& ue, V& un, V& uv, boo
 }
 
 // One rectangle by nn quadrature nodes (from rect_node; the point tensile dislocation above).
-// Per station: the strike-frame coordinates and q once, then per node
-//   R² = x² + y² + d², A = 1/(R(R+d)²), E = 1/(R³(R+d)²), B = (3R+d) E/(R+d), T = 3q²/R⁵,
+// Per station: the strike-frame coordinates and q once, then per node, with s = 1/(R(R+d)),
+//   R² = x² + y² + d², A = s/(R+d) = 1/(R(R+d)²), E = A/R² = 1/(R³(R+d)²),
+//   B = (3R+d) E/(R+d), T = 3q²/R⁵,
 //   ux = x [T - k s² (1/R³ - (A - y² B))],  uy = y [T - k s² (A - x² B)],
-//   uz = d T - k s² (1/(R(R+d)) - x²(2R+d) E),
+//   uz = d T - k s² (s - x²(2R+d) E),
 // weighted and summed in FP32 (the nodes' terms vary smoothly: no cancellation).
 template <class V>
 AG_DEVICE_INLINE void rect_quad(const RectQ& Q, const float4* node, int nn, V Xr, V Yr, V& ue, V& un, V& uv) {
@@ -871,22 +872,23 @@ AG_DEVICE_INLINE void rect_quad(const RectQ& Q, const float4* node, int nn, V Xr
     for (int k = 0; k < nn; ++k) {
         const float4 nd = node[k];
         const V x = vsub(xs, V(nd.x)), y = vsub(ys, V(nd.y)), d = V(nd.z), w = V(nd.w);
-        const V R2 = vfma(x, x, vfma(y, y, vmul(d, d)));
+        const V x2 = vmul(x, x), y2 = vmul(y, y);
+        const V R2 = vfma(d, d, vadd(x2, y2));
         const V iR = vrsqrt(R2);
         const V R = vmul(R2, iR);
         const V iRd = frcp(vadd(R, d));
-        const V iR2 = vmul(iR, iR), iR3 = vmul(iR2, iR);
+        const V s = vmul(iR, iRd);
+        const V A = vmul(s, iRd);
+        const V iR2 = vmul(iR, iR);
+        const V E = vmul(A, iR2);
+        const V iR3 = vmul(iR2, iR);
         const V T = vmul(q3, vmul(iR3, iR2));
-        const V iRd2 = vmul(iRd, iRd);
-        const V A = vmul(iR, iRd2);
-        const V E = vmul(iR3, iRd2);
         const V B = vmul(vmul(vfma(V(3.0f), R, d), E), iRd);
-        const V x2 = vmul(x, x), y2 = vmul(y, y);
         const V G1 = vfma(vneg(x2), B, A);
         const V G2 = vfma(vneg(y2), B, A);
         const V ux = vmul(x, vfma(nks2, vsub(iR3, G2), T));
         const V uy = vmul(y, vfma(nks2, G1, T));
-        const V I5 = vfma(vneg(vmul(x2, vfma(V(2.0f), R, d))), E, vmul(iR, iRd));
+        const V I5 = vfma(vneg(vmul(x2, vfma(V(2.0f), R, d))), E, s);
         const V uz = vfma(nks2, I5, vmul(d, T));
         sx = vfma(w, ux, sx);
         sy = vfma(w, uy, sy);

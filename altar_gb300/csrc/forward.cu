@@ -265,7 +265,10 @@ cdm_llk_kernel(const ChainC* __restrict__ chains, const int32_t* __restrict__ sl
     __shared__ __align__(8) uint64_t full[STAGES];
     __shared__ int s_done[STAGES];
     __shared__ int s_issued;
-    __shared__ float4 s_node[WARPS][kQuadBudget];     // each warp's nodes of the rectangle in hand
+    // each warp's quadrature nodes: one buffer per rectangle (one shared by the three where
+    // shared memory is short), regenerated only when a tile needs other node counts
+    constexpr int kNodeBufs = WARPS <= 4 ? 3 : 1;
+    __shared__ float4 s_node[WARPS][kNodeBufs][kQuadBudget];
     __shared__ float s_gx[136], s_gw[136];             // Gauss-Legendre rules (FP32)
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -312,6 +315,7 @@ cdm_llk_kernel(const ChainC* __restrict__ chains, const int32_t* __restrict__ sl
     const float x0h = C.hdr.x, x0l = C.hdr.y, y0h = C.hdr.z, y0l = C.hdr.w;
     ff acc{0.f, 0.f};
     bool failed = false;
+    uint64_t node_keys = ~0ull;       // 12 bits per buffer: rectangle, n1, n2 of the nodes it holds
     for (int t = 0; t < ntiles; ++t) {
         const int buf = t % STAGES;
         const uint32_t phase = (uint32_t)(t / STAGES) & 1u;
@@ -337,13 +341,19 @@ cdm_llk_kernel(const ChainC* __restrict__ chains, const int32_t* __restrict__ sl
                     sides &= ~(0xFu << (4 * r));
                 }
             }
-            // one rectangle's nodes into this warp's buffer (every lane reads all of them)
-            auto load_nodes = [&](int r) {
+            // one rectangle's nodes in this warp's buffer (every lane reads all of them); the
+            // buffer is refilled only when it holds other nodes
+            auto load_nodes = [&](int r) -> const float4* {
                 const int n1 = (qpack >> (10 * r)) & 31, n2 = (qpack >> (10 * r + 5)) & 31;
-                __syncwarp();
-                if (lane < n1 * n2) s_node[warp][lane] = rect_node(C.rect[r], n1, n2, lane, s_gx, s_gw);
-                __syncwarp();
-                return n1 * n2;
+                const int b = kNodeBufs == 3 ? r : 0;
+                const uint64_t key = (uint64_t)(r | (n1 << 2) | (n2 << 7));
+                if (((node_keys >> (12 * b)) & 0xFFFull) != key) {
+                    __syncwarp();
+                    if (lane < n1 * n2) s_node[warp][b][lane] = rect_node(C.rect[r], n1, n2, lane, s_gx, s_gw);
+                    __syncwarp();
+                    node_keys = (node_keys & ~(0xFFFull << (12 * b))) | (key << (12 * b));
+                }
+                return s_node[warp][b];
             };
             // u projected on the LOS, minus data and offset; accumulate w r² and store r
             auto finish = [&](float e_, float n_, float v_, int j) {
@@ -381,8 +391,9 @@ cdm_llk_kernel(const ChainC* __restrict__ chains, const int32_t* __restrict__ sl
                     while (qm) {
                         const int r = __ffs(qm) - 1;
                         qm &= qm - 1;
-                        const int nn = load_nodes(r);
-                        rect_quad<SV<SPL>>(C.rect[r], s_node[warp], nn, Xr, Yr, ue, un, uv);
+                        const float4* nodes = load_nodes(r);
+                        rect_quad<SV<SPL>>(C.rect[r], nodes, ((qpack >> (10 * r)) & 31) * ((qpack >> (10 * r + 5)) & 31),
+                                           Xr, Yr, ue, un, uv);
                     }
 #pragma unroll
                     for (int q = 0; q < SPL; ++q) finish(ue.v[q], un.v[q], uv.v[q], j0 + 32 * q);
@@ -405,8 +416,9 @@ cdm_llk_kernel(const ChainC* __restrict__ chains, const int32_t* __restrict__ sl
                     while (qm) {
                         const int r = __ffs(qm) - 1;
                         qm &= qm - 1;
-                        const int nn = load_nodes(r);
-                        rect_quad<float>(C.rect[r], s_node[warp], nn, Xr, Yr, ue, un, uv);
+                        const float4* nodes = load_nodes(r);
+                        rect_quad<float>(C.rect[r], nodes, ((qpack >> (10 * r)) & 31) * ((qpack >> (10 * r + 5)) & 31),
+                                         Xr, Yr, ue, un, uv);
                     }
                     finish(ue, un, uv, j);
                 }
