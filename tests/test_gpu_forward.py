@@ -146,6 +146,39 @@ def test_cdm_work_count_matches_host_plan(cuda):
     assert ratio > 1.2
 
 
+def test_cdm_station_order_and_tile_boxes(cuda):
+    """The CDM stores its stations along a Hilbert curve: every tile box
+    (ag_station_boxes) contains its stations, and the residual rows come back in the
+    caller's order, equal (to the quadrature tolerance and FP32 rounding) to those of the
+    same stations stored in the caller's order, whose tiles are row segments."""
+    from altar_gb300.device import Stations
+    rng = np.random.default_rng(17)
+    X, Y = rng.uniform(-2e4, 2e4, 3000), rng.uniform(-2e4, 2e4, 3000)
+    los = np.tile(LOS, (X.size, 1))
+    theta = cdm_prior_rows(40, seed=19)
+    d = rng.normal(0, 3e-3, X.size)
+    strat, _ = cdm_strategy(X, Y, los, d, np.full(X.size, 9e-6))
+    st = strat.stations
+    assert st.order is not None
+    order = st.order.cpu().numpy()
+    assert sorted(order) == list(range(st.m_padded)) and np.all(order[X.size:] == np.arange(X.size, st.m_padded))
+    box = st.tile_box.cpu().numpy().astype(np.float64)
+    xs, ys = X[order[:X.size]], Y[order[:X.size]]
+    for t in range(box.shape[0]):
+        sl = slice(128 * t, min(X.size, 128 * (t + 1)))
+        assert box[t, 0] <= xs[sl].min() and xs[sl].max() <= box[t, 1], t
+        assert box[t, 2] <= ys[sl].min() and ys[sl].max() <= box[t, 3], t
+    llk, res = _residuals(strat, theta, X.size)
+    # the same stations stored in the caller's order
+    strat.stations = Stations(X, Y, los, d, np.full(X.size, 1 / 9e-6), reorder=False)
+    llk0, res0 = _residuals(strat, theta, X.size)
+    err = np.max(np.abs(res - res0), 1) / np.max(np.abs(res0 + d), 1)
+    assert err.max() < 2e-6, err.max()
+    np.testing.assert_allclose(llk, llk0, rtol=1e-6)
+    ref = cdm_los_oracle(theta[:8], X, Y, los)
+    assert np.max(np.abs(res[:8] + d - ref)) <= TOL_CDM * np.max(np.abs(ref))
+
+
 def test_cdm_launch_variants_identical(cuda):
     """Every launch variant (warps per CTA, register budget, one, two or four stations per
     lane) computes the same residuals and log-likelihoods bit for bit: the rounding of every
