@@ -44,6 +44,9 @@ PRIORS = [(-1e4, 1e4), (-1e4, 1e4), (1e3, 1e4), (-50.0, 50.0), (100.0, 3000.0), 
 # quadrature, + 31 per station; the constants are counted from the source by
 # tests/cdm_host/cdm_host.cpp
 L2_FLUSH_BYTES = 256 << 20
+# a run whose final best data log-likelihood is this far below the best run's has settled in a
+# secondary mode of the likelihood (the modes of the workload differ by hundreds to thousands)
+TRAP_LLK = 50.0
 
 
 def problem(seed=2024, on_device=True):
@@ -272,6 +275,9 @@ def anneal(kind, X, Y, los, d, N, rank, args, seed=1234, max_stages=None):
            "likelihoods_evaluated": evaluated / max(1, steps),
            "mean": th.mean(0).tolist(), "sd": th.std(0).tolist(),
            "invariants": invariants(th),
+           # best data log-likelihood of the final population (a run that settled in a
+           # secondary mode of the likelihood ends far below the others)
+           "llk_max": float(worker.step.data.max().item()),
            "acceptance": [r["accepted"] / max(1, r["accepted"] + r["rejected"] + r["unlikely"]) for r in reps],
            "betas": [r["beta"] for r in reps],
            "stage_s": np.diff([t0] + [r["time"] for r in reps]).tolist()}
@@ -629,12 +635,17 @@ def run_sweep(args, X, Y, los, d, N, rank):
     """Time to β = 1 at equal posterior.  Plain Metropolis with each of --sweep-steps steps
     per stage and the coarse-model delayed-acceptance sampler (stage 1 the exact CDM on every
     32nd/16th/8th station, two rounds of 10 stage-1 moves and an exact correction per stage)
-    run over --seeds.  The reference posterior is the longest plain walk.  For each sampler
-    and each mode-independent summary (the means of centroid, depth, opening and sorted
-    semi-axes), z = (seed mean - reference seed mean) / sqrt(s²/K + s_ref²/K), s the spread
-    of the summary over a sampler's K seeds (one run's Monte Carlo standard error).  A sampler
-    reaches the posterior when every |z| <= 2; the speed-up is the time of the cheapest plain
-    walk that reaches it over the delayed-acceptance time."""
+    run over --seeds.  The reference posterior is the longest plain walk.  A run whose final
+    population's best log-likelihood lies more than TRAP_LLK below the best of all runs has
+    settled in a secondary mode of the likelihood (an annealing trait of CATMIP, a few per
+    cent of the runs); such runs are counted per sampler and left out of the summaries.  For
+    each sampler and each mode-independent summary (the means of centroid, depth, opening
+    and sorted semi-axes), z = (seed mean - reference seed mean) / sqrt(s²/K + s_ref²/K) over
+    the runs in the main mode, s the spread of the summary over a sampler's K such runs (one
+    run's Monte Carlo standard error).  A sampler reaches the posterior when every |z| <= 2
+    and it settles in the main mode no more often than the reference; the speed-up is the
+    time of the cheapest plain walk that reaches it over the delayed-acceptance time (mean
+    over all runs, trapped ones included)."""
     import torch
     seeds = args.seeds
     anneal("plain", X, Y, los, d, N, rank, args, seed=1, max_stages=3)        # one-time costs
@@ -649,27 +660,35 @@ def run_sweep(args, X, Y, los, d, N, rank):
     runs["da"] = [anneal("da", X, Y, los, d, N, rank, args, seed=sd) for sd in seeds]
     torch.cuda.synchronize()
     names = runs["da"][0]["invariants"]["names"]
+    best = max(r["llk_max"] for rs in runs.values() for r in rs)
+    main = {key: [r for r in rs if r["llk_max"] >= best - TRAP_LLK] for key, rs in runs.items()}
     stats = {}
-    for key, rs in runs.items():
+    for key, rs in main.items():
         m = np.array([r["invariants"]["mean"] for r in rs])
-        stats[key] = (m.mean(0), m.std(0, ddof=1) if len(rs) > 1 else np.zeros(m.shape[1]),
-                      float(np.mean([r["time_s"] for r in rs])), float(np.mean([r["stages"] for r in rs])))
+        stats[key] = (m.mean(0), m.std(0, ddof=1) if len(rs) > 1 else np.zeros(m.shape[1]), len(rs))
     ref_key = f"plain{max(args.sweep_steps)}"
-    mref, sref, _, _ = stats[ref_key]
-    K = len(seeds)
+    mref, sref, kref = stats[ref_key]
     out = {}
-    for key, (m, sdev, t, st) in stats.items():
-        z = (m - mref) / np.sqrt((sdev ** 2 + sref ** 2) / K + 1e-300)
-        out[key] = {"time_s": t, "stages": st, "z": z.tolist(),
-                    "reaches": bool(key == ref_key or np.all(np.abs(z) <= 2.0)),
-                    "times_s": [r["time_s"] for r in runs[key]]}
+    for key, (m, sdev, k) in stats.items():
+        z = (m - mref) / np.sqrt(sdev ** 2 / max(k, 1) + sref ** 2 / max(kref, 1) + 1e-300)
+        trapped = len(runs[key]) - k
+        out[key] = {"time_s": float(np.mean([r["time_s"] for r in runs[key]])),
+                    "stages": float(np.mean([r["stages"] for r in runs[key]])), "z": z.tolist(),
+                    "trapped_runs": trapped,
+                    "reaches": bool(key == ref_key or (k >= 2 and np.all(np.abs(z) <= 2.0)
+                                                       and trapped <= len(runs[ref_key]) - kref)),
+                    "times_s": [r["time_s"] for r in runs[key]],
+                    "llk_max": [r["llk_max"] for r in runs[key]],
+                    "summary_means": [r["invariants"]["mean"] for r in runs[key]]}
     plain_ok = [k for k in out if k.startswith("plain") and out[k]["reaches"]]
     cheapest = min(plain_ok, key=lambda k: out[k]["time_s"])
     line = {"metric": "CDM time-to-beta=1 at equal posterior", "unit": "s", "higher_is_better": False,
             "value": out["da"]["time_s"], "n_gpus": 1, "data": "synthetic",
             "config": {"workload": "cdm-40k-obs", "chains": N, "stations": X.size, "seeds": seeds,
                        "plain_steps_per_stage": args.sweep_steps, "reference": ref_key,
-                       "summaries": names, "criterion": "every |z| <= 2 against the reference's seed mean"},
+                       "summaries": names, "trap_llk": TRAP_LLK,
+                       "criterion": "every |z| <= 2 against the reference's seed mean over the runs in the main "
+                                    "mode, and no more runs in a secondary mode than the reference"},
             "samplers": out, "cheapest_plain_at_equal_posterior": cheapest,
             "da_reaches_equal_posterior": out["da"]["reaches"],
             "speedup_da_vs_plain_at_equal_posterior": out[cheapest]["time_s"] / out["da"]["time_s"],
