@@ -136,6 +136,7 @@ _SIGNATURES = {
     "ag_cdm_work": (c_int, [P, P, c_int32, P, P, P, P]),
     "ag_station_boxes": (c_int, [P, c_int32, c_int32, P, P]),
     "ag_forward_llk_subset": (c_int, [c_int, P, P, c_int32, P, c_double, P, P, P, P, P, P, c_size_t, P]),
+    "ag_forward_llk_floor": (c_int, [c_int, P, P, c_int32, P, c_double, P, P, P, P, P, c_size_t, P]),
     "ag_linear_kpad": (c_int32, [c_int32]),
     "ag_linear_prepare": (c_int, [P, c_int32, c_int32, P, P]),
     "ag_linear_workspace_bytes": (c_size_t, [c_int32, c_int32, c_int32]),
@@ -165,6 +166,7 @@ _SIGNATURES = {
     "ag_prior_sample": (c_int, [c_int32, c_int32, P, P, c_uint64, c_uint32, P, P, P]),
     "ag_prior_llk": (c_int, [P, c_int32, c_int32, P, P, P, P, P]),
     "ag_propose": (c_int, [P, P, c_int32, c_int32, P, P, c_uint64, c_uint32, P, P, P, P]),
+    "ag_accept_floor": (c_int, [P, c_int32, c_uint64, c_uint32, P, P, P, P, P]),
     "ag_accept": (c_int, [P, c_int32, c_int32, c_uint64, c_uint32, P, P, P, P, P, P, P, P, P]),
     "ag_cov_workspace_bytes": (c_size_t, [c_int32]),
     "ag_cov_schedule": (c_int, [P, P, c_int32, c_double, c_double, P, c_size_t, P]),

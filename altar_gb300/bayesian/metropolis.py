@@ -6,6 +6,13 @@ reject samples outside the model's support (and, for the CDM, above the free
 surface), evaluate the likelihoods of every candidate, accept where
 log u <= post' - post.  Each step is three launches: propose (+verify +prior),
 the fused forward model, accept.
+
+early_reject: before the forward model, the log-likelihood below which each proposal is
+certainly rejected (the accept test's own uniform, ag_accept_floor); a forward model that
+supports it stops evaluating such a candidate part way (Solonen et al. 2012, "Efficient
+MCMC for climate model parameter estimation: parallel adaptive chains and early
+rejection", Bayesian Analysis 7(3)).  The accept decisions, hence the chains, are the
+same as with full evaluations; only work for rejected candidates is saved.
 """
 import torch
 
@@ -14,13 +21,15 @@ from ..device import DEVICE, ptr, stream_handle
 
 
 class Metropolis:
-    def __init__(self, scaling=0.1, acceptanceWeight=8.0, rejectionWeight=1.0):
+    def __init__(self, scaling=0.1, acceptanceWeight=8.0, rejectionWeight=1.0, early_reject=True):
         self.scaling = float(scaling)
         self.acceptanceWeight = float(acceptanceWeight)
         self.rejectionWeight = float(rejectionWeight)
+        self.early_reject = bool(early_reject)
         self.steps = 1
         self.seed = 0
         self._buf = None
+        self._floor = None
 
     def initialize(self, application):
         self.steps = application.job.steps
@@ -82,6 +91,9 @@ class Metropolis:
         cand, cprior, cdata, mask = self._buffers(n, p)
         st = step.state.struct
         s = stream_handle()
+        early = self.early_reject and getattr(model.strategy, "supports_floor", False)
+        if early and (self._floor is None or self._floor.shape[0] != n):
+            self._floor = torch.empty(n, dtype=torch.float64, device=DEVICE)
         for k in range(self.steps):
             d.notify(event=d.chainAdvanceStart, controller=annealer)
             d.notify(event=d.verifyStart, controller=annealer)
@@ -89,7 +101,12 @@ class Metropolis:
                          self.seed, k, ptr(cand), ptr(mask), ptr(cprior), s)
             d.notify(event=d.verifyFinish, controller=annealer)
             d.notify(event=d.dataStart, controller=annealer)
-            model.strategy.forward(cand, cdata, mask=mask, status=mask)
+            if early:
+                _native.call("ag_accept_floor", st, n, self.seed, k, ptr(mask), ptr(cprior), ptr(step.posterior),
+                             ptr(self._floor), s)
+                model.strategy.forward(cand, cdata, mask=mask, status=mask, floor=self._floor)
+            else:
+                model.strategy.forward(cand, cdata, mask=mask, status=mask)
             d.notify(event=d.dataFinish, controller=annealer)
             d.notify(event=d.acceptStart, controller=annealer)
             _native.call("ag_accept", st, n, p, self.seed, k, ptr(mask), ptr(cand), ptr(cprior),

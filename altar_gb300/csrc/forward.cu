@@ -252,8 +252,9 @@ cdm_llk_kernel(const ChainC* __restrict__ chains, const int32_t* __restrict__ sl
                const int32_t* __restrict__ nslots_ptr, int n, const float4* __restrict__ xy,
                const float4* __restrict__ losd, const float* __restrict__ wt,
                const int32_t* __restrict__ oid, const float4* __restrict__ tile_box,
-               const int32_t* __restrict__ order, int m, int m_padded, double norm, double* __restrict__ llk,
-               float* __restrict__ resid, uint32_t* __restrict__ flags) {
+               const int32_t* __restrict__ order, int m, int m_padded, double norm,
+               const double* __restrict__ llk_floor, double* __restrict__ llk, float* __restrict__ resid,
+               uint32_t* __restrict__ flags) {
     const int nslots = min(n, *nslots_ptr);
     if ((int)(blockIdx.x * WARPS) >= nslots) return;       // whole CTA past the active chains
     __shared__ ChainC s_chain[WARPS];
@@ -316,6 +317,12 @@ cdm_llk_kernel(const ChainC* __restrict__ chains, const int32_t* __restrict__ sl
     ff acc{0.f, 0.f};
     bool failed = false;
     uint64_t node_keys = ~0ull;       // 12 bits per buffer: rectangle, n1, n2 of the nodes it holds
+    // early rejection: the misfit only grows with the stations, so once the partial
+    // log-likelihood is below the chain's floor the proposal is certainly rejected and its
+    // remaining stations are skipped (the llk is then reported as -inf)
+    const double floor_llk = (llk_floor && active && !resid) ? llk_floor[chain] : -INFINITY;
+    bool stopped = false;
+    int t_stop = ntiles;
     for (int t = 0; t < ntiles; ++t) {
         const int buf = t % STAGES;
         const uint32_t phase = (uint32_t)(t / STAGES) & 1u;
@@ -324,7 +331,7 @@ cdm_llk_kernel(const ChainC* __restrict__ chains, const int32_t* __restrict__ sl
             failed = true;
             break;
         }
-        if (smask) {
+        if (smask && !stopped) {
             // this tile's plan: the rectangles it integrates (node counts packed 5 + 5 bits per
             // rectangle) and the sides of the others
             const float4 tb = s_box[buf];
@@ -423,6 +430,7 @@ cdm_llk_kernel(const ChainC* __restrict__ chains, const int32_t* __restrict__ sl
                     finish(ue, un, uv, j);
                 }
             }
+            if (floor_llk > -INFINITY && norm - 0.5 * warp_sum(ff_to_double(acc)) < floor_llk) stopped = true;
         }
         // done with this buffer: the last warp of the CTA to get here refills it
         __syncwarp();
@@ -438,6 +446,23 @@ cdm_llk_kernel(const ChainC* __restrict__ chains, const int32_t* __restrict__ sl
                 }
             }
         }
+        // a CTA of one stopped warp leaves the ring; CTAs of several warps keep counting tiles
+        // (the stopped warp's share of each tile's completion) without computing
+        if (WARPS == 1 && stopped) {
+            t_stop = t;
+            break;
+        }
+    }
+    if (WARPS == 1 && stopped && !failed) {
+        // wait (bounded) for the copies already issued into this CTA's ring before it exits
+        if (lane == 0) {
+            const int last = s_issued;
+            for (int t = t_stop + 1; t < last; ++t)
+                mbar_wait_bounded(&full[t % STAGES], (uint32_t)(t / STAGES) & 1u, kWaitLimit);
+        }
+        __syncwarp();
+        if (lane == 0) llk[chain] = -INFINITY;
+        return;
     }
     if (__syncthreads_or(failed)) {
         // a wait gave up: drain the copies still in flight (bounded) before the CTA exits
@@ -450,7 +475,7 @@ cdm_llk_kernel(const ChainC* __restrict__ chains, const int32_t* __restrict__ sl
         return;
     }
     const double sum = warp_sum(ff_to_double(acc));
-    if (lane == 0 && active) llk[chain] = norm - 0.5 * sum;
+    if (lane == 0 && active) llk[chain] = stopped ? -INFINITY : norm - 0.5 * sum;
 }
 
 // ---------------------------------------------------------------------------
@@ -594,7 +619,7 @@ static int check_stations(const ag_station_set* st) {
 
 static int forward_llk(int model, const ag_layout* layout, const double* theta, int32_t n,
                        const ag_station_set* st, double norm, const uint32_t* mask_in,
-                       const int32_t* index, const int32_t* count, double* llk,
+                       const int32_t* index, const int32_t* count, const double* llk_floor, double* llk,
                        uint32_t* chain_status, float* residuals, void* workspace,
                        size_t workspace_bytes, void* stream) {
     AG_REQUIRE(layout != nullptr && theta != nullptr && llk != nullptr, "null argument");
@@ -650,7 +675,7 @@ static int forward_llk(int model, const ag_layout* layout, const double* theta, 
 #define AG_CDM_LAUNCH(W, B, SPL, ST)                                                                    \
     cdm_llk_kernel<W, B, SPL, ST><<<grid, W * 32, 0, s>>>(chains, slot_chain, nslots, n, xy, ld, st->weight, \
                                                           st->oid, tile_box, st->order, st->m, st->m_padded,     \
-                                                          norm, llk, residuals, nullptr)
+                                                          norm, llk_floor, llk, residuals, nullptr)
         // warps per CTA, CTAs per SM, stations per lane, ring depth; a CTA of one warp has its
         // own ring, so its chain never waits for another chain's tiles
         switch (v) {
@@ -701,8 +726,17 @@ extern "C" int ag_forward_llk(int model, const ag_layout* layout, const double* 
                               const ag_station_set* st, double norm, const uint32_t* mask_in,
                               double* llk, uint32_t* chain_status, float* residuals,
                               void* workspace, size_t workspace_bytes, void* stream) {
-    return forward_llk(model, layout, theta, n, st, norm, mask_in, nullptr, nullptr, llk, chain_status,
+    return forward_llk(model, layout, theta, n, st, norm, mask_in, nullptr, nullptr, nullptr, llk, chain_status,
                        residuals, workspace, workspace_bytes, stream);
+}
+
+extern "C" int ag_forward_llk_floor(int model, const ag_layout* layout, const double* theta, int32_t n,
+                                    const ag_station_set* st, double norm, const uint32_t* mask_in,
+                                    const double* llk_floor, double* llk, uint32_t* chain_status,
+                                    void* workspace, size_t workspace_bytes, void* stream) {
+    AG_REQUIRE(llk_floor != nullptr, "llk_floor must not be NULL (ag_forward_llk evaluates without one)");
+    return forward_llk(model, layout, theta, n, st, norm, mask_in, nullptr, nullptr, llk_floor, llk, chain_status,
+                       nullptr, workspace, workspace_bytes, stream);
 }
 
 extern "C" int ag_forward_llk_subset(int model, const ag_layout* layout, const double* theta,
@@ -711,7 +745,7 @@ extern "C" int ag_forward_llk_subset(int model, const ag_layout* layout, const d
                                      uint32_t* chain_status, float* residuals, void* workspace,
                                      size_t workspace_bytes, void* stream) {
     AG_REQUIRE(index != nullptr && count != nullptr, "index and count must not be NULL");
-    return forward_llk(model, layout, theta, n, st, norm, nullptr, index, count, llk, chain_status,
+    return forward_llk(model, layout, theta, n, st, norm, nullptr, index, count, nullptr, llk, chain_status,
                        residuals, workspace, workspace_bytes, stream);
 }
 

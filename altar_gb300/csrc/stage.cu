@@ -172,6 +172,30 @@ __global__ void accept_kernel(int n, int p, const double* __restrict__ beta, uin
         atomicAdd(&counters[threadIdx.x], (unsigned long long)s_cnt[threadIdx.x]);
 }
 
+// The data log-likelihood below which each proposal is certainly rejected (early rejection,
+// Solonen et al. 2012, Bayesian Analysis 7(3)).  accept_kernel rejects when
+// log u > cprior + β cdata − post; with the same uniform u, every cdata below
+// (post + log u − cprior)/β is rejected.  The floor is lowered by a relative 1e-9 so that a
+// likelihood evaluation stopped below it is rejected whatever the rounding of the test;
+// chains outside the support, and β = 0, get -inf (never stopped).
+__global__ void accept_floor_kernel(int n, const double* __restrict__ beta, uint64_t seed, uint32_t step,
+                                    const uint32_t* __restrict__ epoch, const uint32_t* __restrict__ mask,
+                                    const double* __restrict__ cprior, const double* __restrict__ post,
+                                    double* __restrict__ floor, int chain0) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double b = *beta;
+    double f = -INFINITY;
+    if (!mask[i] && b > 0.0) {
+        u32x4 r = draw(seed, (uint32_t)(chain0 + i), 0u, STREAM_ACCEPT, step, *epoch);
+        const double u = u01_open_closed(r.x, r.y);
+        f = (post[i] + log(u) - cprior[i]) / b;
+        f -= (fabs(f) + 1.0) * 1e-9;
+        if (!(f == f)) f = -INFINITY;
+    }
+    floor[i] = f;
+}
+
 __global__ void posterior_kernel(int n, const double* __restrict__ beta,
                                  const double* __restrict__ prior, const double* __restrict__ data,
                                  double* __restrict__ post) {
@@ -990,6 +1014,17 @@ extern "C" int ag_accept(const ag_stage_state* st, int32_t n, int32_t p, uint64_
         n, p, st->beta, seed, step, st->epoch, mask, cand, cprior, cdata, theta, prior, data, post,
         st->counters, st->chain0);
     return launch_status("accept_kernel");
+}
+
+extern "C" int ag_accept_floor(const ag_stage_state* st, int32_t n, uint64_t seed, uint32_t step,
+                               const uint32_t* mask, const double* cprior, const double* post, double* llk_floor,
+                               void* stream) {
+    int rc = check_state(st);
+    if (rc) return rc;
+    AG_REQUIRE(n > 0 && mask && cprior && post && llk_floor, "invalid arguments");
+    accept_floor_kernel<<<blocks(n, 256), 256, 0, as_stream(stream)>>>(n, st->beta, seed, step, st->epoch, mask,
+                                                                        cprior, post, llk_floor, st->chain0);
+    return launch_status("accept_floor_kernel");
 }
 
 extern "C" int ag_posterior(const ag_stage_state* st, int32_t n, const double* prior,

@@ -75,14 +75,25 @@ class CUDA:
                 self._resid = torch.zeros(n, self.stations.m_padded, dtype=torch.float32, device=DEVICE)
         return self
 
-    def forward(self, theta, out, mask=None, status=None, residuals=None, stream=None):
-        """Data log-likelihood of the rows of device θ into device ``out``."""
+    @property
+    def supports_floor(self):
+        """Early rejection: the CDM with diagonal Cd stops a chain's evaluation below its floor."""
+        return self.kind == _native.AG_MODEL_CDM and self._whiten is None
+
+    def forward(self, theta, out, mask=None, status=None, residuals=None, stream=None, floor=None):
+        """Data log-likelihood of the rows of device θ into device ``out``.  floor (device, one
+        value per row, from ag_accept_floor): rows found below it may stop early with -inf."""
         n = theta.shape[0]
         self.reserve(n)
         s = stream_handle(stream)
         resid = residuals
         if self._whiten is not None and resid is None:
             resid = self._resid[:n]
+        if floor is not None and resid is None and self.supports_floor:
+            _native.call("ag_forward_llk_floor", self.kind, ctypes.byref(self.layout), ptr(theta), n,
+                         self.stations.struct, self.norm, ptr(mask), ptr(floor), ptr(out), ptr(status),
+                         ptr(self._ws), self._ws_bytes, s)
+            return out
         _native.call("ag_forward_llk", self.kind, ctypes.byref(self.layout), ptr(theta), n,
                      self.stations.struct, self.norm, ptr(mask), ptr(out), ptr(status),
                      ptr(resid), ptr(self._ws), self._ws_bytes, s)

@@ -931,9 +931,9 @@ def run_ours(args):
         "e2e": {"value": world * N * S / t_e2e, "unit": "chain-steps/s", "h2d_bytes_per_step": io_bytes,
                 "d2h_bytes_per_step": io_bytes},
         # per stage (one CUDA graph): COV median + cooperative COV schedule, Σ, Cholesky, CDF,
-        # counts and ranks, gather, adapt; per Metropolis step propose, CDM cost classes, CDM set-up,
-        # CDM likelihood, accept
-        "gpu_launches": (8 + 5 * S) * args.steps,
+        # counts and ranks, gather, adapt; per Metropolis step propose, acceptance floor, CDM cost
+        # classes, CDM set-up, CDM likelihood, accept
+        "gpu_launches": (8 + 6 * S) * args.steps,
         "cpu_baseline": {"value": cpu_rate, "unit": "chain-steps/s", "cores": cores, "kind": "port",
                          "sample": f"{args.cpu_chains} chains x {X.size} stations, likelihood only, "
                                    f"{cpu_dt:.1f} s (FP64 C restatement of models/cdm/cdm/libcdm.py)"},

@@ -140,6 +140,19 @@ int ag_forward_llk(int model, const ag_layout* layout, const double* theta, int3
                    void* workspace, size_t workspace_bytes, void* stream);
 
 /*
+ * ag_forward_llk with early rejection (no counterpart in the reference): a chain whose
+ * log-likelihood is found below llk_floor[i] (ag_accept_floor) part way through the
+ * stations stops there and gets llk = -inf; every other chain's llk is exactly what
+ * ag_forward_llk computes.  The Metropolis chains are then the same as without it, with
+ * less work for the proposals that are rejected.  CDM: applied per tile of stations;
+ * Mogi: the floor is ignored.  No residual rows.
+ */
+int ag_forward_llk_floor(int model, const ag_layout* layout, const double* theta, int32_t n,
+                         const ag_station_set* stations, double norm, const uint32_t* mask_in,
+                         const double* llk_floor, double* llk, uint32_t* chain_status,
+                         void* workspace, size_t workspace_bytes, void* stream);
+
+/*
  * ag_forward_llk restricted to the chains index[0 .. *count) (device-side
  * count, e.g. the survivors of a delayed-acceptance screen); llk, chain_status
  * and residual rows of the other chains are left untouched.  No counterpart in
@@ -222,6 +235,18 @@ int ag_propose(const ag_stage_state* st, const double* theta, int32_t n, int32_t
 int ag_accept(const ag_stage_state* st, int32_t n, int32_t p, uint64_t seed, uint32_t step,
               const uint32_t* mask, const double* cand, const double* cprior, const double* cdata,
               double* theta, double* prior, double* data, double* post, void* stream);
+
+/*
+ * Early rejection (no counterpart in the reference, which evaluates every candidate in
+ * full, Metropolis.py:186): llk_floor[i] = the data log-likelihood below which step
+ * `step`'s proposal of chain i is certainly rejected by ag_accept with the same seed, step
+ * and stage state, (post + log u − cprior)/β with the accept test's own uniform u, lowered
+ * by a relative 1e-9; -inf for masked chains or β = 0.  Pass it to ag_forward_llk_floor
+ * between ag_propose and ag_accept.
+ */
+int ag_accept_floor(const ag_stage_state* st, int32_t n, uint64_t seed, uint32_t step,
+                    const uint32_t* mask, const double* cprior, const double* post, double* llk_floor,
+                    void* stream);
 
 /*
  * Bytes of workspace ag_cov_schedule needs for n chains.

@@ -146,6 +146,62 @@ def test_cdm_annealing_runs(cuda):
     assert np.all(np.isfinite(th)) and np.all(np.isfinite(app.controller.worker.step.data.cpu().numpy()))
 
 
+def test_early_rejection_keeps_the_chains(cuda):
+    """Early rejection (the CDM evaluation of a candidate stops once its partial
+    log-likelihood is below the accept test's floor) changes no accept decision: a CDM run
+    with it and one without end with the same θ, log-likelihoods and acceptance counts, bit
+    for bit, over the whole run to β = 1 (the work saved is reported)."""
+    from altar_gb300.bayesian import Metropolis
+    g = np.linspace(-20e3, 20e3, 40)
+    X, Y = [a.ravel() for a in np.meshgrid(g, g)]
+    los = np.tile(LOS, (X.size, 1))
+    truth = cdm_prior_rows(1, seed=21)
+    d = cdm_los_oracle(truth, X, Y, los)[0] + np.random.default_rng(2).normal(0, 3e-3, X.size)
+    psets = {"location": Contiguous(2, Uniform((-1e4, 1e4))), "depth": Contiguous(1, Uniform((1e3, 1e4))),
+             "opening": Contiguous(1, Uniform((-50, 50))), "a": Contiguous(3, Uniform((100, 3000))),
+             "omega": Contiguous(3, Uniform((-90, 90)))}
+    out = {}
+    for early in (False, True):
+        model = CDM(psets, observations=Observations(X, Y, los, d, 9e-6))
+        app = Application(model, job=Job(chains=1024, steps=5), rng=RNG(7),
+                          controller=Annealer(sampler=Metropolis(early_reject=early)))
+        app.run()
+        w = app.controller.worker
+        assert w.step.beta == 1.0
+        out[early] = ([t.cpu().numpy() for t in (w.step.theta, w.step.prior, w.step.data, w.step.posterior)],
+                      [(r["accepted"], r["rejected"], r["unlikely"]) for r in w.reports])
+    for a, b in zip(out[False][0], out[True][0]):
+        np.testing.assert_array_equal(a, b)
+    assert out[False][1] == out[True][1]
+
+
+def test_forward_floor_semantics(cuda):
+    """ag_forward_llk_floor: a chain whose log-likelihood is below its floor may stop with
+    -inf; every other chain gets exactly ag_forward_llk's value."""
+    from gpu_helpers import cdm_strategy, dev
+    g = np.linspace(-20e3, 20e3, 60)
+    X, Y = [a.ravel() for a in np.meshgrid(g, g)]
+    los = np.tile(LOS, (X.size, 1))
+    theta = cdm_prior_rows(64, seed=23)
+    d = np.random.default_rng(5).normal(0, 3e-3, X.size)
+    strat, _ = cdm_strategy(X, Y, los, d, np.full(X.size, 9e-6))
+    th = dev(theta)
+    full = torch.empty(64, dtype=torch.float64, device="cuda")
+    strat.forward(th, full)
+    f = full.cpu().numpy()
+    floor = np.full(64, -np.inf)
+    floor[::4] = f[::4] + 1.0               # certainly below: may stop
+    floor[1::4] = f[1::4] - 1.0             # above its floor: must be exact
+    floor[2::4] = np.inf                    # stops at the first tile
+    got = torch.empty(64, dtype=torch.float64, device="cuda")
+    strat.forward(th, got, floor=dev(floor))
+    g_ = got.cpu().numpy()
+    exact = np.r_[1:64:4, 3:64:4]
+    np.testing.assert_array_equal(g_[exact], f[exact])
+    assert np.all(np.isneginf(g_[2::4]))
+    assert np.all((g_[::4] == f[::4]) | np.isneginf(g_[::4]))
+
+
 def test_profiler_times_the_phases(cuda, tmp_path):
     """A run with the Profiler registered (phases launched one by one, timed with CUDA
     events) writes the reference's profile file and ends where the captured-graph run ends."""
