@@ -301,13 +301,18 @@ class SubsetSurrogate:
         self._main = model.strategy
         return self
 
-    def predict(self, theta, lo, hi, out_llk, bufs, mask=None):
+    def predict(self, theta, lo, hi, out_llk, bufs, mask=None, floor=None):
         """Coarse data log-likelihood of device θ rows into out_llk; rows flagged in mask are
-        skipped and sources above the surface are flagged there."""
+        skipped and sources above the surface are flagged there; with floor (early rejection
+        of the first-stage moves) rows found below it may stop with -inf."""
         strat = self.strategies[self.level]
         strat.layout.variant = self._main.layout.variant   # the exact model's (autotuned) launch shape
-        strat.forward(theta, out_llk, mask=mask, status=mask)
+        strat.forward(theta, out_llk, mask=mask, status=mask, floor=floor)
         return out_llk
+
+    @property
+    def supports_floor(self):
+        return bool(self.strategies) and getattr(self.strategies[self.level], "supports_floor", False)
 
     def buffers(self, n, p):
         return None
@@ -567,9 +572,12 @@ class DelayedAcceptance(Metropolis):
             sst = _native.StageState(*(t.data_ptr() for t in (st.beta, st.dbeta_cov, st.scaling, st.sigma,
                                                              st.chol, st.w, counters, st.epoch, st.flags)))
             self._chain = (torch.zeros(n, p, **f64), torch.zeros(n, **f64), torch.zeros(n, **f64),
-                           torch.zeros(n, **f64), torch.zeros(n, dtype=torch.int32, device=DEVICE), sst, counters)
+                           torch.zeros(n, **f64), torch.zeros(n, dtype=torch.int32, device=DEVICE), sst, counters,
+                           torch.empty(n, **f64))
         bufs, sur_cur, sur_cand, passed, index, count, screened = self._sbufs
-        th_s, pr_s, su_s, po_s, mask2, sst, _ = self._chain
+        th_s, pr_s, su_s, po_s, mask2, sst, _, floor = self._chain
+        # early rejection of the first-stage moves (the coarse model's Metropolis test)
+        early = self.early_reject and getattr(sur, "supports_floor", False)
         self.screened = screened
         lo, hi = self._bounds
         st = step.state.struct
@@ -586,7 +594,12 @@ class DelayedAcceptance(Metropolis):
                 sid = 1000 + o * inner + j
                 _native.call("ag_propose", st, ptr(th_s), n, p, ptr(model.lo), ptr(model.hi), self.seed, sid,
                              ptr(cand), ptr(mask), ptr(cprior), s)
-                sur.predict(cand, lo, hi, sur_cand, bufs, mask=mask)
+                if early:
+                    _native.call("ag_accept_floor", ctypes.byref(sst), n, self.seed, sid, ptr(mask), ptr(cprior),
+                                 ptr(po_s), ptr(floor), s)
+                    sur.predict(cand, lo, hi, sur_cand, bufs, mask=mask, floor=floor)
+                else:
+                    sur.predict(cand, lo, hi, sur_cand, bufs, mask=mask)
                 _native.call("ag_accept", ctypes.byref(sst), n, p, self.seed, sid, ptr(mask), ptr(cand),
                              ptr(cprior), ptr(sur_cand), ptr(th_s), ptr(pr_s), ptr(su_s), ptr(po_s), s)
             _native.call("ag_da_moved", n, p, ptr(step.theta), ptr(th_s), ptr(passed), ptr(index), ptr(count), s)

@@ -276,6 +276,36 @@ def test_subset_surrogate_transition_posterior(cuda):
         assert abs(td[:, j].std() - sd) < 0.5 * sd, j
 
 
+def test_subset_da_early_rejection_keeps_the_chains(cuda):
+    """Early rejection of the first-stage (coarse-model) moves and of the plain stages: a CDM
+    delayed-acceptance run with it ends where the run without it ends, bit for bit."""
+    from gpu_helpers import cdm_los_oracle, cdm_prior_rows
+    from altar_gb300.models import CDM
+    g = np.linspace(-20e3, 20e3, 48)
+    X, Y = [a.ravel() for a in np.meshgrid(g, g)]
+    los = np.tile(LOS, (X.size, 1))
+    truth = cdm_prior_rows(1, seed=21)
+    d = cdm_los_oracle(truth, X, Y, los)[0] + np.random.default_rng(2).normal(0, 3e-3, X.size)
+    psets = {"location": Contiguous(2, Uniform((-1e4, 1e4))), "depth": Contiguous(1, Uniform((1e3, 1e4))),
+             "opening": Contiguous(1, Uniform((-50, 50))), "a": Contiguous(3, Uniform((100, 3000))),
+             "omega": Contiguous(3, Uniform((-90, 90)))}
+    out = {}
+    for early in (False, True):
+        model = CDM(psets, observations=Observations(X, Y, los, d, 9e-6))
+        da = DelayedAcceptance(surrogate=SubsetSurrogate(strides=(8, 4)), delta_limit=1.0, check_chains=128,
+                               inner=5, outer=2, stop_beta=1.0, early_reject=early)
+        app = Application(model, job=Job(chains=1024, steps=5), rng=RNG(4), controller=Annealer(sampler=da))
+        app.initialize()
+        app.controller.posterior(model, max_stages=12)
+        w = app.controller.worker
+        out[early] = ([t.cpu().numpy() for t in (w.step.theta, w.step.data, w.step.posterior)],
+                      [(r.get("mode"), r["accepted"], r["rejected"]) for r in w.reports])
+    assert any(m == "da" for m, _, _ in out[True][1])
+    for a, b in zip(out[False][0], out[True][0]):
+        np.testing.assert_array_equal(a, b)
+    assert out[False][1] == out[True][1]
+
+
 def test_trained_network_gain(cuda):
     """What training the network gains.  Two-stage delayed acceptance screens every proposal
     with the network's log-likelihood and runs the exact model only on the survivors, so its
