@@ -327,7 +327,7 @@ class DelayedAcceptance(Metropolis):
 
     def __init__(self, surrogate=None, rms_limit=0.5, delta_limit=2.0, fit_chains=4096, check_chains=256,
                  epochs=40, refit_epochs=None, start_beta=0.0, stop_beta=0.1, retry_every=3, spread=3.0,
-                 inner=10, outer=1, screen_limit=None, **kwds):
+                 inner=10, outer=1, screen_limit=None, screen_steps=None, **kwds):
         """rms_limit: largest RMS field error (data standard deviations) of a usable surrogate;
         delta_limit: largest spread (standard deviation over trial proposals) of the error of
         the surrogate's tempered log-posterior ratio, β[(s(y) - s(x)) - (l(y) - l(x))].  Delayed
@@ -349,6 +349,10 @@ class DelayedAcceptance(Metropolis):
         # walk but the finest passes screen_limit, the stage walks with two-stage delayed
         # acceptance (every step screened by the coarse model, the exact model on the survivors)
         self.screen_limit = None if screen_limit is None else float(screen_limit)
+        # two-stage steps per screened stage (None: the job's steps); a screened step costs a
+        # coarse evaluation plus an exact one for the survivors only, so a screened stage can
+        # afford the longer walk that keeps the population mixed
+        self.screen_steps = None if screen_steps is None else int(screen_steps)
         self.delta = None
         self._prepare_s = 0.0
         self._backoff = 0
@@ -632,7 +636,8 @@ class DelayedAcceptance(Metropolis):
         s = stream_handle()
         # the constant parts of the surrogate log-likelihood (q0, norm) cancel in both stages
         sur.predict(step.theta, lo, hi, sur_cur, bufs)
-        for k in range(self.steps):
+        steps = self.screen_steps if (self.mode == "screen" and self.screen_steps) else self.steps
+        for k in range(steps):
             _native.call("ag_propose", st, ptr(step.theta), n, p, ptr(model.lo), ptr(model.hi), self.seed, k,
                          ptr(cand), ptr(mask), ptr(cprior), s)
             sur.predict(cand, lo, hi, sur_cand, bufs, mask=mask)

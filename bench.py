@@ -255,7 +255,8 @@ def anneal(kind, X, Y, los, d, N, rank, args, seed=1234, max_stages=None):
                                     refit_epochs=args.refit_epochs,
                                     start_beta=args.da_start_beta, stop_beta=args.da_stop_beta,
                                     inner=args.da_inner,
-                                    outer=args.da_outer, screen_limit=args.screen_limit)
+                                    outer=args.da_outer, screen_limit=args.screen_limit,
+                                    screen_steps=args.screen_steps)
     model = CDM(cdm_psets(), observations=Observations(X, Y, los, d, SIGMA ** 2), autotune=not args.no_autotune)
     app = Application(model, job=Job(chains=N, steps=args.walk_steps), rng=RNG(seed + rank),
                       controller=Annealer(sampler=sampler))
@@ -1021,6 +1022,8 @@ def main():
     ap.add_argument("--screen-limit", type=float, default=None,
                     help="coarse-model DA: ratio spread up to which a stage that fails --delta-limit "
                          "still screens every step on the finest level (two-stage delayed acceptance)")
+    ap.add_argument("--screen-steps", type=int, default=None,
+                    help="two-stage steps per screened stage (default: the job's steps)")
     ap.add_argument("--subset-inner", type=int, nargs="+", default=None,
                     help="surrogate moves per exact correction at each subset level (default: --da-inner)")
     ap.add_argument("--delta-limit", type=float, default=2.0)
