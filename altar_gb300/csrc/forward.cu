@@ -57,11 +57,13 @@ static_assert(sizeof(ChainC) % 16 == 0, "ChainC must be a whole number of float4
 
 // Chain slots ordered by cost.  The chains of one CTA share its ring of station tiles, so a
 // CTA advances at the pace of its most expensive chain; with rectangles integrated by
-// quadrature the work of a chain ranges from ~1,500 to ~3,300 FLOP per station.  The set-up
-// therefore runs in two passes: cdm_cost_kernel classifies every requested chain (masked,
-// above the free surface, or the cost bucket of its plan) and counts the chains per bucket;
-// cdm_setup_kernel gives each chain the next slot of its bucket, buckets in decreasing cost,
-// so the CTAs hold chains of similar cost and the expensive ones are scheduled first.
+// quadrature, with node counts that depend on each tile's distance, the work of a chain
+// ranges over several times its minimum.  The set-up therefore runs in two passes:
+// cdm_cost_kernel classifies every requested chain (masked, above the free surface, or the
+// cost bucket of its plan averaged over a sample of the tiles) and counts the chains per
+// bucket; cdm_setup_kernel gives each chain the next slot of its bucket, buckets in
+// decreasing cost, so the CTAs hold chains of similar cost and the expensive ones are
+// scheduled first (which also shortens the tail of the launch for one-chain CTAs).
 constexpr int kCostBuckets = 64;
 constexpr int kCostBucketFlop = 96;      // FLOP per station per bucket
 
