@@ -137,6 +137,8 @@ _SIGNATURES = {
     "ag_station_boxes": (c_int, [P, c_int32, c_int32, P, P]),
     "ag_forward_llk_subset": (c_int, [c_int, P, P, c_int32, P, c_double, P, P, P, P, P, P, c_size_t, P]),
     "ag_forward_llk_floor": (c_int, [c_int, P, P, c_int32, P, c_double, P, P, P, P, P, c_size_t, P]),
+    "ag_forward_llk_subset_floor": (c_int, [c_int, P, P, c_int32, P, c_double, P, P, P, P, P, P, c_size_t, P]),
+    "ag_da_floor": (c_int, [P, c_int32, c_uint64, c_uint32, P, P, P, P, P, P, P, P, P]),
     "ag_linear_kpad": (c_int32, [c_int32]),
     "ag_linear_prepare": (c_int, [P, c_int32, c_int32, P, P]),
     "ag_linear_workspace_bytes": (c_size_t, [c_int32, c_int32, c_int32]),

@@ -608,9 +608,17 @@ class DelayedAcceptance(Metropolis):
                              ptr(cprior), ptr(sur_cand), ptr(th_s), ptr(pr_s), ptr(su_s), ptr(po_s), s)
             _native.call("ag_da_moved", n, p, ptr(step.theta), ptr(th_s), ptr(passed), ptr(index), ptr(count), s)
             mask2.zero_()
-            _native.call("ag_forward_llk_subset", strat.kind, ctypes.byref(strat.layout), ptr(th_s), n,
-                         strat.stations.struct, strat.norm, ptr(index), ptr(count), ptr(cdata), ptr(mask2), None,
-                         ptr(strat._ws), strat._ws_bytes, s)
+            if self.early_reject and getattr(strat, "supports_floor", False):
+                # early rejection of the exact correction (the stage-2 test's own uniform)
+                _native.call("ag_da_floor", st, n, self.seed, o, ptr(mask2), ptr(passed), ptr(pr_s), ptr(su_s),
+                             ptr(step.prior), ptr(sur_cur), ptr(step.posterior), ptr(floor), s)
+                _native.call("ag_forward_llk_subset_floor", strat.kind, ctypes.byref(strat.layout), ptr(th_s), n,
+                             strat.stations.struct, strat.norm, ptr(index), ptr(count), ptr(floor), ptr(cdata),
+                             ptr(mask2), ptr(strat._ws), strat._ws_bytes, s)
+            else:
+                _native.call("ag_forward_llk_subset", strat.kind, ctypes.byref(strat.layout), ptr(th_s), n,
+                             strat.stations.struct, strat.norm, ptr(index), ptr(count), ptr(cdata), ptr(mask2),
+                             None, ptr(strat._ws), strat._ws_bytes, s)
             _native.call("ag_da_accept", st, n, p, self.seed, o, ptr(mask2), ptr(passed), ptr(th_s), ptr(pr_s),
                          ptr(cdata), ptr(su_s), ptr(step.theta), ptr(step.prior), ptr(step.data),
                          ptr(step.posterior), ptr(sur_cur), ptr(screened), s)
@@ -634,6 +642,9 @@ class DelayedAcceptance(Metropolis):
         lo, hi = self._bounds
         st = step.state.struct
         s = stream_handle()
+        early = self.early_reject and getattr(strat, "supports_floor", False)
+        if early and (getattr(self, "_dfloor", None) is None or self._dfloor.shape[0] != n):
+            self._dfloor = torch.empty(n, dtype=torch.float64, device=DEVICE)
         # the constant parts of the surrogate log-likelihood (q0, norm) cancel in both stages
         sur.predict(step.theta, lo, hi, sur_cur, bufs)
         steps = self.screen_steps if (self.mode == "screen" and self.screen_steps) else self.steps
@@ -643,9 +654,17 @@ class DelayedAcceptance(Metropolis):
             sur.predict(cand, lo, hi, sur_cand, bufs, mask=mask)
             _native.call("ag_da_screen", st, n, self.seed, k, ptr(mask), ptr(cprior), ptr(sur_cand),
                          ptr(step.prior), ptr(sur_cur), ptr(passed), ptr(index), ptr(count), s)
-            _native.call("ag_forward_llk_subset", strat.kind, ctypes.byref(strat.layout), ptr(cand), n,
-                         strat.stations.struct, strat.norm, ptr(index), ptr(count), ptr(cdata), ptr(mask), None,
-                         ptr(strat._ws), strat._ws_bytes, s)
+            if early:
+                # early rejection of the exact stage (the stage-2 test's own uniform)
+                _native.call("ag_da_floor", st, n, self.seed, k, ptr(mask), ptr(passed), ptr(cprior), ptr(sur_cand),
+                             ptr(step.prior), ptr(sur_cur), ptr(step.posterior), ptr(self._dfloor), s)
+                _native.call("ag_forward_llk_subset_floor", strat.kind, ctypes.byref(strat.layout), ptr(cand), n,
+                             strat.stations.struct, strat.norm, ptr(index), ptr(count), ptr(self._dfloor),
+                             ptr(cdata), ptr(mask), ptr(strat._ws), strat._ws_bytes, s)
+            else:
+                _native.call("ag_forward_llk_subset", strat.kind, ctypes.byref(strat.layout), ptr(cand), n,
+                             strat.stations.struct, strat.norm, ptr(index), ptr(count), ptr(cdata), ptr(mask),
+                             None, ptr(strat._ws), strat._ws_bytes, s)
             _native.call("ag_da_accept", st, n, p, self.seed, k, ptr(mask), ptr(passed), ptr(cand), ptr(cprior),
                          ptr(cdata), ptr(sur_cand), ptr(step.theta), ptr(step.prior), ptr(step.data),
                          ptr(step.posterior), ptr(sur_cur), ptr(screened), s)

@@ -741,6 +741,17 @@ extern "C" int ag_forward_llk_floor(int model, const ag_layout* layout, const do
                        nullptr, workspace, workspace_bytes, stream);
 }
 
+extern "C" int ag_forward_llk_subset_floor(int model, const ag_layout* layout, const double* theta, int32_t n,
+                                           const ag_station_set* st, double norm, const int32_t* index,
+                                           const int32_t* count, const double* llk_floor, double* llk,
+                                           uint32_t* chain_status, void* workspace, size_t workspace_bytes,
+                                           void* stream) {
+    AG_REQUIRE(index != nullptr && count != nullptr && llk_floor != nullptr,
+               "index, count and llk_floor must not be NULL");
+    return forward_llk(model, layout, theta, n, st, norm, nullptr, index, count, llk_floor, llk, chain_status,
+                       nullptr, workspace, workspace_bytes, stream);
+}
+
 extern "C" int ag_forward_llk_subset(int model, const ag_layout* layout, const double* theta,
                                      int32_t n, const ag_station_set* st, double norm,
                                      const int32_t* index, const int32_t* count, double* llk,

@@ -529,6 +529,30 @@ __global__ void da_accept_kernel(int n, int p, const double* __restrict__ beta, 
     if (threadIdx.x == 3 && s_cnt[3] && screened) atomicAdd(screened, (unsigned long long)s_cnt[3]);
 }
 
+// The exact log-likelihood below which the stage-2 test of da_accept_kernel certainly
+// rejects chain i (early rejection of the exact correction): the test rejects when
+// log u > (cprior + β cdata − post) − dsur, so below (log u + post − cprior + dsur)/β, lowered
+// by a relative 1e-9 for the rounding of the test; -inf where no evaluation is made.
+__global__ void da_floor_kernel(int n, const double* __restrict__ beta, uint64_t seed, uint32_t step,
+                                const uint32_t* __restrict__ epoch, const uint32_t* __restrict__ mask,
+                                const int32_t* __restrict__ pass, const double* __restrict__ cprior,
+                                const double* __restrict__ csur, const double* __restrict__ prior,
+                                const double* __restrict__ sur, const double* __restrict__ post,
+                                double* __restrict__ floor) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double b = *beta;
+    double f = -INFINITY;
+    if (!mask[i] && pass[i] && b > 0.0) {
+        const double dsur = (cprior[i] + b * csur[i]) - (prior[i] + b * sur[i]);
+        u32x4 r = draw(seed, (uint32_t)i, 2u, STREAM_ACCEPT, step, *epoch);
+        f = (log(u01_open_closed(r.x, r.y)) + post[i] - cprior[i] + dsur) / b;
+        f -= (fabs(f) + 1.0) * 1e-9;
+        if (!(f == f)) f = -INFINITY;
+    }
+    floor[i] = f;
+}
+
 // chains whose surrogate-chain state moved away from the exact state go to the exact
 // correction: pass[i] = (θ_s ≠ θ) and no support violation, compacted into index
 __global__ void da_moved_kernel(int n, int p, const double* __restrict__ theta,
@@ -859,6 +883,16 @@ extern "C" int ag_da_screen(const ag_stage_state* st, int32_t n, uint64_t seed, 
     da_screen_kernel<<<nblk(n, 256), 256, 0, s>>>(n, st->beta, seed, step, st->epoch, mask, cprior, csur,
                                                   prior, sur, pass, index, count);
     return launch_status("da_screen_kernel");
+}
+
+extern "C" int ag_da_floor(const ag_stage_state* st, int32_t n, uint64_t seed, uint32_t step, const uint32_t* mask,
+                           const int32_t* pass, const double* cprior, const double* csur, const double* prior,
+                           const double* sur, const double* post, double* llk_floor, void* stream) {
+    AG_REQUIRE(st && n > 0 && mask && pass && cprior && csur && prior && sur && post && llk_floor,
+               "invalid arguments");
+    da_floor_kernel<<<nblk(n, 256), 256, 0, as_stream(stream)>>>(n, st->beta, seed, step, st->epoch, mask, pass,
+                                                                  cprior, csur, prior, sur, post, llk_floor);
+    return launch_status("da_floor_kernel");
 }
 
 extern "C" int ag_da_accept(const ag_stage_state* st, int32_t n, int32_t p, uint64_t seed, uint32_t step,

@@ -163,6 +163,12 @@ int ag_forward_llk_subset(int model, const ag_layout* layout, const double* thet
                           const int32_t* count, double* llk, uint32_t* chain_status,
                           float* residuals, void* workspace, size_t workspace_bytes, void* stream);
 
+/* ag_forward_llk_subset with early rejection (as ag_forward_llk_floor, floors by chain index) */
+int ag_forward_llk_subset_floor(int model, const ag_layout* layout, const double* theta, int32_t n,
+                                const ag_station_set* stations, double norm, const int32_t* index,
+                                const int32_t* count, const double* llk_floor, double* llk,
+                                uint32_t* chain_status, void* workspace, size_t workspace_bytes, void* stream);
+
 /*
  * Work of the CDM likelihood kernel for each chain over the stations' m
  * observations: the FP32 operations (FMA = 2) and special-function operations
@@ -487,6 +493,12 @@ int ag_da_accept(const ag_stage_state* st, int32_t n, int32_t p, uint64_t seed, 
                  const uint32_t* mask, const int32_t* pass, const double* cand, const double* cprior,
                  const double* cdata, const double* csur, double* theta, double* prior, double* data,
                  double* post, double* sur, unsigned long long* screened, void* stream);
+/* early rejection of the stage-2 correction: llk_floor[i] = the exact log-likelihood below which
+ * ag_da_accept with the same arguments certainly rejects chain i (-inf where it evaluates none);
+ * for ag_forward_llk_subset_floor */
+int ag_da_floor(const ag_stage_state* st, int32_t n, uint64_t seed, uint32_t step, const uint32_t* mask,
+                const int32_t* pass, const double* cprior, const double* csur, const double* prior,
+                const double* sur, const double* post, double* llk_floor, void* stream);
 
 /* surrogate-transition variant: pass[i] = 1 where the surrogate chain θ_s moved away from θ;
  * those chains are listed in index[0 .. *count) for the exact correction (ag_da_accept with

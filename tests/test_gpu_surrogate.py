@@ -276,9 +276,12 @@ def test_subset_surrogate_transition_posterior(cuda):
         assert abs(td[:, j].std() - sd) < 0.5 * sd, j
 
 
-def test_subset_da_early_rejection_keeps_the_chains(cuda):
-    """Early rejection of the first-stage (coarse-model) moves and of the plain stages: a CDM
-    delayed-acceptance run with it ends where the run without it ends, bit for bit."""
+@pytest.mark.parametrize("inner", [5, 1])
+def test_subset_da_early_rejection_keeps_the_chains(cuda, inner):
+    """Early rejection of the first-stage (coarse-model) moves, of the exact corrections and
+    of the plain stages: a CDM delayed-acceptance run with it ends where the run without it
+    ends, bit for bit (inner 5: surrogate transitions and an exact correction; inner 1:
+    two-stage screening of every step)."""
     from gpu_helpers import cdm_los_oracle, cdm_prior_rows
     from altar_gb300.models import CDM
     g = np.linspace(-20e3, 20e3, 48)
@@ -293,7 +296,7 @@ def test_subset_da_early_rejection_keeps_the_chains(cuda):
     for early in (False, True):
         model = CDM(psets, observations=Observations(X, Y, los, d, 9e-6))
         da = DelayedAcceptance(surrogate=SubsetSurrogate(strides=(8, 4)), delta_limit=1.0, check_chains=128,
-                               inner=5, outer=2, stop_beta=1.0, early_reject=early)
+                               inner=inner, outer=2, stop_beta=1.0, early_reject=early)
         app = Application(model, job=Job(chains=1024, steps=5), rng=RNG(4), controller=Annealer(sampler=da))
         app.initialize()
         app.controller.posterior(model, max_stages=12)
