@@ -158,10 +158,15 @@ class CUDAAnnealing:
             ck.save(ck.path, self.step, self.iteration)
         return self
 
-    def finish(self, annealer):
-        if annealer.archiver is not None:
-            annealer.archiver.record(step=self.step)
+    def forget_graphs(self):
+        """Release the captured graphs; the next stage captures afresh (after a change of the
+        sampler's settings that changes its launch sequence)."""
         for ex in self._graphs.values():
             _native.load().ag_graph_destroy(ex)
         self._graphs.clear()
         return self
+
+    def finish(self, annealer):
+        if annealer.archiver is not None:
+            annealer.archiver.record(step=self.step)
+        return self.forget_graphs()

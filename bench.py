@@ -794,6 +794,7 @@ def run_ours(args):
     stream = worker.stream
 
     samp = ann.sampler
+    early_on = bool(getattr(samp, "early_reject", False)) and getattr(model.strategy, "supports_floor", False)
     S = app.job.steps
     with torch.cuda.stream(stream):
         ann.model = model
@@ -886,6 +887,32 @@ def run_ours(args):
         t_e2e = sum(a.elapsed_time(b) for a, b in e2e_ev) / len(e2e_ev) / 1e3
         t_e2e = max_over_ranks(t_e2e, dist, device="cuda")
         io_bytes = sum(t.numel() * t.element_size() for t in host)
+
+        # the same stages with every candidate's likelihood evaluated in full (early rejection
+        # off): the chains are the same, each chain-step carries a whole likelihood evaluation
+        t_full = None
+        if early_on:
+            samp.early_reject = False
+            worker.forget_graphs()
+            for t, saved in snapshot:
+                t.copy_(saved)
+            stage()                                      # captures the stage graph once more
+            worker.bottom(annealer=ann)
+            for t, saved in snapshot:
+                t.copy_(saved)
+            torch.cuda.synchronize()
+            full_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                       for _ in range(args.steps)]
+            for a, b in full_ev:
+                flush.zero_()
+                a.record(stream)
+                stage()
+                b.record(stream)
+                worker.bottom(annealer=ann)
+            torch.cuda.synchronize()
+            t_full = sum(a.elapsed_time(b) for a, b in full_ev) / len(full_ev) / 1e3
+            t_full = max_over_ranks(t_full, dist, device="cuda")
+            samp.early_reject = True
         worker.finish(annealer=ann)
 
     if rank != 0:
@@ -931,6 +958,11 @@ def run_ours(args):
                                     "(MEASURED_PEAKS.json has no FP32 figure)"},
         "e2e": {"value": world * N * S / t_e2e, "unit": "chain-steps/s", "h2d_bytes_per_step": io_bytes,
                 "d2h_bytes_per_step": io_bytes},
+        # the sampler evaluates each candidate until it is certain to be rejected (early rejection:
+        # the same chains, bit for bit); the same timed stages with every likelihood in full:
+        "early_rejection": {"enabled": early_on,
+                            "value_full_evaluations": (world * N * S / t_full) if t_full else None,
+                            "ms_per_step_full_evaluations": t_full * 1e3 if t_full else None},
         # per stage (one CUDA graph): COV median + cooperative COV schedule, Σ, Cholesky, CDF,
         # counts and ranks, gather, adapt; per Metropolis step propose, acceptance floor, CDM cost
         # classes, CDM set-up, CDM likelihood, accept
