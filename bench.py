@@ -655,7 +655,8 @@ def run_sweep(args, X, Y, los, d, N, rank):
         args.walk_steps = steps
         runs[f"plain{steps}"] = [anneal("plain", X, Y, los, d, N, rank, args, seed=sd) for sd in seeds]
     args.walk_steps = 5
-    args.surrogate, args.subset_strides, args.da_inner, args.da_outer = "subset", [32, 16, 8], 10, 2
+    inner, outer = (int(v) for v in args.sweep_da.split("x"))
+    args.surrogate, args.subset_strides, args.da_inner, args.da_outer = "subset", [32, 16, 8], inner, outer
     args.subset_inner, args.delta_limit, args.da_stop_beta = None, 1.0, 1.0
     anneal("da", X, Y, los, d, N, rank, args, seed=1, max_stages=3)
     runs["da"] = [anneal("da", X, Y, los, d, N, rank, args, seed=sd) for sd in seeds]
@@ -1054,6 +1055,9 @@ def main():
     ap.add_argument("--screen-limit", type=float, default=None,
                     help="coarse-model DA: ratio spread up to which a stage that fails --delta-limit "
                          "still screens every step on the finest level (two-stage delayed acceptance)")
+    ap.add_argument("--sweep-da", default="10x2",
+                    help="--mode sweep: the delayed-acceptance setting as INNERxOUTER (first-stage moves x "
+                         "exact corrections per stage)")
     ap.add_argument("--screen-steps", type=int, default=None,
                     help="two-stage steps per screened stage (default: the job's steps)")
     ap.add_argument("--subset-inner", type=int, nargs="+", default=None,
