@@ -632,6 +632,41 @@ def run_dense(args):
     return 0
 
 
+def equal_posterior(runs, ref_key, trap_llk=TRAP_LLK):
+    """Per sampler of ``runs`` ({sampler: [run, ...]}, each run with ``time_s``, ``stages``,
+    ``llk_max`` and ``invariants["mean"]``): mean time and stages, the runs in a secondary
+    mode (final best log-likelihood more than trap_llk below the best of all runs), and the
+    z-score of each summary's seed mean against the reference sampler's over the runs in
+    the main mode, z = (m - m_ref) / sqrt(s²/K + s_ref²/K) with s the summary's spread over
+    a sampler's K runs.  A sampler reaches the reference posterior when K >= 2, every
+    |z| <= 2 and it has no more runs in a secondary mode than the reference."""
+    best = max(r["llk_max"] for rs in runs.values() for r in rs)
+    main = {key: [r for r in rs if r["llk_max"] >= best - trap_llk] for key, rs in runs.items()}
+    stats = {}
+    for key, rs in main.items():
+        m = np.array([r["invariants"]["mean"] for r in rs], dtype=np.float64)
+        if len(rs) == 0:
+            width = len(runs[key][0]["invariants"]["mean"])
+            stats[key] = (np.full(width, np.nan), np.zeros(width), 0)
+        else:
+            stats[key] = (m.mean(0), m.std(0, ddof=1) if len(rs) > 1 else np.zeros(m.shape[1]), len(rs))
+    mref, sref, kref = stats[ref_key]
+    ref_trapped = len(runs[ref_key]) - kref
+    out = {}
+    for key, (m, sdev, k) in stats.items():
+        z = (m - mref) / np.sqrt(sdev ** 2 / max(k, 1) + sref ** 2 / max(kref, 1) + 1e-300)
+        trapped = len(runs[key]) - k
+        out[key] = {"time_s": float(np.mean([r["time_s"] for r in runs[key]])),
+                    "stages": float(np.mean([r["stages"] for r in runs[key]])), "z": z.tolist(),
+                    "trapped_runs": trapped,
+                    "reaches": bool(key == ref_key or (k >= 2 and np.all(np.abs(z) <= 2.0)
+                                                       and trapped <= ref_trapped)),
+                    "times_s": [r["time_s"] for r in runs[key]],
+                    "llk_max": [r["llk_max"] for r in runs[key]],
+                    "summary_means": [r["invariants"]["mean"] for r in runs[key]]}
+    return out
+
+
 def run_sweep(args, X, Y, los, d, N, rank):
     """Time to β = 1 at equal posterior.  Plain Metropolis with each of --sweep-steps steps
     per stage and the coarse-model delayed-acceptance sampler (stage 1 the exact CDM on every
@@ -663,26 +698,8 @@ def run_sweep(args, X, Y, los, d, N, rank):
     runs["da"] = [anneal("da", X, Y, los, d, N, rank, args, seed=sd) for sd in seeds]
     torch.cuda.synchronize()
     names = runs["da"][0]["invariants"]["names"]
-    best = max(r["llk_max"] for rs in runs.values() for r in rs)
-    main = {key: [r for r in rs if r["llk_max"] >= best - TRAP_LLK] for key, rs in runs.items()}
-    stats = {}
-    for key, rs in main.items():
-        m = np.array([r["invariants"]["mean"] for r in rs])
-        stats[key] = (m.mean(0), m.std(0, ddof=1) if len(rs) > 1 else np.zeros(m.shape[1]), len(rs))
     ref_key = f"plain{max(args.sweep_steps)}"
-    mref, sref, kref = stats[ref_key]
-    out = {}
-    for key, (m, sdev, k) in stats.items():
-        z = (m - mref) / np.sqrt(sdev ** 2 / max(k, 1) + sref ** 2 / max(kref, 1) + 1e-300)
-        trapped = len(runs[key]) - k
-        out[key] = {"time_s": float(np.mean([r["time_s"] for r in runs[key]])),
-                    "stages": float(np.mean([r["stages"] for r in runs[key]])), "z": z.tolist(),
-                    "trapped_runs": trapped,
-                    "reaches": bool(key == ref_key or (k >= 2 and np.all(np.abs(z) <= 2.0)
-                                                       and trapped <= len(runs[ref_key]) - kref)),
-                    "times_s": [r["time_s"] for r in runs[key]],
-                    "llk_max": [r["llk_max"] for r in runs[key]],
-                    "summary_means": [r["invariants"]["mean"] for r in runs[key]]}
+    out = equal_posterior(runs, ref_key)
     plain_ok = [k for k in out if k.startswith("plain") and out[k]["reaches"]]
     cheapest = min(plain_ok, key=lambda k: out[k]["time_s"])
     line = {"metric": "CDM time-to-beta=1 at equal posterior", "unit": "s", "higher_is_better": False,
