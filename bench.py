@@ -675,14 +675,11 @@ def run_sweep(args, X, Y, los, d, N, rank):
     run over --seeds.  The reference posterior is the longest plain walk.  A run whose final
     population's best log-likelihood lies more than TRAP_LLK below the best of all runs has
     settled in a secondary mode of the likelihood (an annealing trait of CATMIP, a few per
-    cent of the runs); such runs are counted per sampler and left out of the summaries.  For
-    each sampler and each mode-independent summary (the means of centroid, depth, opening
-    and sorted semi-axes), z = (seed mean - reference seed mean) / sqrt(s²/K + s_ref²/K) over
-    the runs in the main mode, s the spread of the summary over a sampler's K such runs (one
-    run's Monte Carlo standard error).  A sampler reaches the posterior when every |z| <= 2
-    and it settles in the main mode no more often than the reference; the speed-up is the
-    time of the cheapest plain walk that reaches it over the delayed-acceptance time (mean
-    over all runs, trapped ones included)."""
+    cent of the runs).  equal_posterior compares the mode-independent summaries (the means
+    of centroid, depth, opening and sorted semi-axes) of each sampler's runs in the main mode
+    with the reference's; the speed-up is the time of the cheapest plain walk that reaches
+    the reference posterior over the delayed-acceptance time (mean over all runs, trapped
+    ones included)."""
     import torch
     seeds = args.seeds
     anneal("plain", X, Y, los, d, N, rank, args, seed=1, max_stages=3)        # one-time costs
