@@ -670,8 +670,8 @@ def equal_posterior(runs, ref_key, trap_llk=TRAP_LLK):
 def run_sweep(args, X, Y, los, d, N, rank):
     """Time to β = 1 at equal posterior.  Plain Metropolis with each of --sweep-steps steps
     per stage and the coarse-model delayed-acceptance sampler (stage 1 the exact CDM on every
-    32nd/16th/8th station, --sweep-da INNERxOUTER: rounds of INNER stage-1 moves, each ended by an
-    exact correction, OUTER rounds per stage)
+    32nd/16th/8th station, --sweep-da INNERxOUTER ...: rounds of INNER stage-1 moves, each ended by
+    an exact correction, OUTER rounds per stage; the first setting is the line's "da")
     run over --seeds.  The reference posterior is the longest plain walk.  A run whose final
     population's best log-likelihood lies more than TRAP_LLK below the best of all runs has
     settled in a secondary mode of the likelihood (an annealing trait of CATMIP, a few per
@@ -688,11 +688,15 @@ def run_sweep(args, X, Y, los, d, N, rank):
         args.walk_steps = steps
         runs[f"plain{steps}"] = [anneal("plain", X, Y, los, d, N, rank, args, seed=sd) for sd in seeds]
     args.walk_steps = 5
-    inner, outer = (int(v) for v in args.sweep_da.split("x"))
-    args.surrogate, args.subset_strides, args.da_inner, args.da_outer = "subset", [32, 16, 8], inner, outer
+    args.surrogate, args.subset_strides = "subset", [32, 16, 8]
     args.subset_inner, args.delta_limit, args.da_stop_beta = None, 1.0, 1.0
-    anneal("da", X, Y, los, d, N, rank, args, seed=1, max_stages=3)
-    runs["da"] = [anneal("da", X, Y, los, d, N, rank, args, seed=sd) for sd in seeds]
+    da_keys = {}
+    for i, spec in enumerate(args.sweep_da):
+        args.da_inner, args.da_outer = (int(v) for v in spec.split("x"))
+        key = "da" if i == 0 else f"da{spec}"
+        da_keys[spec] = key
+        anneal("da", X, Y, los, d, N, rank, args, seed=1, max_stages=3)
+        runs[key] = [anneal("da", X, Y, los, d, N, rank, args, seed=sd) for sd in seeds]
     torch.cuda.synchronize()
     names = runs["da"][0]["invariants"]["names"]
     ref_key = f"plain{max(args.sweep_steps)}"
@@ -709,7 +713,10 @@ def run_sweep(args, X, Y, los, d, N, rank):
             "samplers": out, "cheapest_plain_at_equal_posterior": cheapest,
             "da_reaches_equal_posterior": out["da"]["reaches"],
             "speedup_da_vs_plain_at_equal_posterior": out[cheapest]["time_s"] / out["da"]["time_s"],
-            "speedup_da_vs_plain5": out["plain5"]["time_s"] / out["da"]["time_s"] if "plain5" in out else None}
+            "speedup_da_vs_plain5": out["plain5"]["time_s"] / out["da"]["time_s"] if "plain5" in out else None,
+            "da_settings": {spec: {"key": key, "time_s": out[key]["time_s"], "reaches": out[key]["reaches"],
+                                   "speedup_vs_cheapest_plain": out[cheapest]["time_s"] / out[key]["time_s"]}
+                            for spec, key in da_keys.items()}}
     if rank == 0:
         print(json.dumps(line))
     return 0
@@ -1073,9 +1080,9 @@ def main():
     ap.add_argument("--screen-limit", type=float, default=None,
                     help="coarse-model DA: ratio spread up to which a stage that fails --delta-limit "
                          "still screens every step on the finest level (two-stage delayed acceptance)")
-    ap.add_argument("--sweep-da", default="20x1",
-                    help="--mode sweep: the delayed-acceptance setting as INNERxOUTER (first-stage moves x "
-                         "exact corrections per stage)")
+    ap.add_argument("--sweep-da", nargs="+", default=["20x1"],
+                    help="--mode sweep: delayed-acceptance settings as INNERxOUTER (first-stage moves x "
+                         "exact corrections per stage); the first is the line's 'da'")
     ap.add_argument("--screen-steps", type=int, default=None,
                     help="two-stage steps per screened stage (default: the job's steps)")
     ap.add_argument("--subset-inner", type=int, nargs="+", default=None,

@@ -104,3 +104,39 @@ def test_every_run_trapped():
     lost = [_run([3.0, 3.0], llk=-1e4) for _ in range(3)]
     out = bench.equal_posterior({"ref": ref, "lost": lost}, "ref")
     assert out["lost"]["trapped_runs"] == 3 and not out["lost"]["reaches"]
+
+
+def test_sweep_line_with_several_da_settings(monkeypatch, capsys):
+    """run_sweep with stand-in runs: the first delayed-acceptance setting is the line's
+    "da", every setting gets its time, verdict and speed-up against the cheapest plain walk
+    that reaches the reference."""
+    import argparse
+    import json
+    import torch
+
+    monkeypatch.setattr(torch.cuda, "synchronize", lambda *a, **k: None)
+    # every sampler sees the same per-seed scatter; the 5-step walk is shifted off it
+    scatter = dict(zip([1, 2, 3, 4, 5], np.random.default_rng(11).standard_normal((5, 7))))
+
+    def fake_anneal(kind, X, Y, los, d, N, rank, args, seed=1234, max_stages=None):
+        if kind == "plain":
+            t, shift = 2.0 * args.walk_steps, (4.0 if args.walk_steps == 5 else 0.0)
+        else:
+            t, shift = float(args.da_inner) / 2, 0.0
+        mean = shift + scatter.get(seed, np.zeros(7))
+        return {"time_s": t, "stages": 40, "llk_max": 0.0,
+                "invariants": {"mean": mean.tolist(), "names": list("abcdefg")}}
+
+    monkeypatch.setattr(bench, "anneal", fake_anneal)
+    args = argparse.Namespace(seeds=[1, 2, 3, 4, 5], sweep_steps=[5, 15, 20], sweep_da=["20x1", "10x1"],
+                              walk_steps=5)
+    assert bench.run_sweep(args, np.zeros(4), np.zeros(4), None, None, 8, 0) == 0
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert line["config"]["reference"] == "plain20"
+    assert line["cheapest_plain_at_equal_posterior"] == "plain15"
+    assert not line["samplers"]["plain5"]["reaches"]
+    assert set(line["da_settings"]) == {"20x1", "10x1"}
+    assert line["da_settings"]["20x1"]["key"] == "da" and line["da_settings"]["10x1"]["key"] == "da10x1"
+    assert line["value"] == pytest.approx(10.0)
+    assert line["speedup_da_vs_plain_at_equal_posterior"] == pytest.approx(30.0 / 10.0)
+    assert line["da_settings"]["10x1"]["speedup_vs_cheapest_plain"] == pytest.approx(30.0 / 5.0)
