@@ -361,7 +361,7 @@ AG_CDM_FN float f32_up(double v) {
 constexpr int kFlopSide = 251;          // one angular-dislocation pair
 constexpr int kFlopSteepExtra = 78;     // near-vertical pair: remainders of the cot β terms
 constexpr int kFlopQuadRect = 19;       // quadrature rectangle: strike frame, q, back to EFCS
-constexpr int kFlopQuadNode = 45;       // one point tensile dislocation, weighted sum
+constexpr int kFlopQuadNode = 43;       // one point tensile dislocation, weighted sum
 constexpr int kFlopStation = 31;        // coordinates, LOS projection, residual, float-float misfit
 constexpr int kSfuSide = 13, kSfuSteepExtra = 3, kSfuQuadNode = 2;
 
@@ -858,7 +858,9 @@ AG_DEVICE_INLINE void side_pair(const K& k, V Xr, V Yr, V& ue, V& un, V& uv, boo
 //   B = (3R+d) E/(R+d), T = 3q²/R⁵,
 //   ux = x [T - k s² (1/R³ - (A - y² B))],  uy = y [T - k s² (A - x² B)],
 //   uz = d T - k s² (s - x²(2R+d) E),
-// weighted and summed in FP32 (the nodes' terms vary smoothly: no cancellation).
+// weighted and summed in FP32 (the nodes' terms vary smoothly: no cancellation).  The node
+// weight w enters as W = w (-k sin²δ), formed once per node for all of a lane's stations, and
+// as w T per station, so each component's weighted term is one FMA into its sum.
 template <class V>
 AG_DEVICE_INLINE void rect_quad(const RectQ& Q, const float4* node, int nn, V Xr, V Yr, V& ue, V& un, V& uv) {
     const V a = V(Q.h0.x), b = V(Q.h0.y);
@@ -866,12 +868,12 @@ AG_DEVICE_INLINE void rect_quad(const RectQ& Q, const float4* node, int nn, V Xr
     const V ys = vfma(a, Yr, vneg(vmul(b, Xr)));
     const V q = vfma(ys, V(Q.h0.z), V(-Q.h0.w));
     const V q3 = vmul(vmul(q, q), V(3.0f));
-    const V nks2 = V(Q.h1.x);
     V sx(0.0f), sy(0.0f), sz(0.0f);
 #pragma unroll 2
     for (int k = 0; k < nn; ++k) {
         const float4 nd = node[k];
         const V x = vsub(xs, V(nd.x)), y = vsub(ys, V(nd.y)), d = V(nd.z), w = V(nd.w);
+        const V W = V(__fmul_rn(nd.w, Q.h1.x));
         const V x2 = vmul(x, x), y2 = vmul(y, y);
         const V R2 = vfma(d, d, vadd(x2, y2));
         const V iR = vrsqrt(R2);
@@ -882,17 +884,14 @@ AG_DEVICE_INLINE void rect_quad(const RectQ& Q, const float4* node, int nn, V Xr
         const V iR2 = vmul(iR, iR);
         const V E = vmul(A, iR2);
         const V iR3 = vmul(iR2, iR);
-        const V T = vmul(q3, vmul(iR3, iR2));
+        const V Tw = vmul(vmul(q3, w), vmul(iR3, iR2));
         const V B = vmul(vmul(vfma(V(3.0f), R, d), E), iRd);
         const V G1 = vfma(vneg(x2), B, A);
         const V G2 = vfma(vneg(y2), B, A);
-        const V ux = vmul(x, vfma(nks2, vsub(iR3, G2), T));
-        const V uy = vmul(y, vfma(nks2, G1, T));
         const V I5 = vfma(vneg(vmul(x2, vfma(V(2.0f), R, d))), E, s);
-        const V uz = vfma(nks2, I5, vmul(d, T));
-        sx = vfma(w, ux, sx);
-        sy = vfma(w, uy, sy);
-        sz = vfma(w, uz, sz);
+        sx = vfma(x, vfma(W, vsub(iR3, G2), Tw), sx);
+        sy = vfma(y, vfma(W, G1, Tw), sy);
+        sz = vfma(W, I5, vfma(d, Tw, sz));
     }
     // back to EFCS: x̂ = (a, b), ŷ = (-b, a)
     ue = vfma(a, sx, vfma(vneg(b), sy, ue));

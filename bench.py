@@ -40,7 +40,7 @@ PRIORS = [(-1e4, 1e4), (-1e4, 1e4), (1e3, 1e4), (-50.0, 50.0), (100.0, 3000.0), 
 # FP32 work of the fused CDM kernel: per (chain, station) pair it is the plan of the chain over
 # the station's tile, summed by the library (ag_cdm_work): 251 FLOP (FMA = 2) and 13
 # special-function operations per rectangle side evaluated as an angular-dislocation pair (78
-# FLOP and 3 more for a near-vertical side), 19 FLOP + 45 FLOP and 2 special-function
+# FLOP and 3 more for a near-vertical side), 19 FLOP + 43 FLOP and 2 special-function
 # operations per node for a rectangle integrated by quadrature, + 31 per station; the
 # constants are counted from the source by tests/cdm_host/cdm_host.cpp
 L2_FLUSH_BYTES = 256 << 20
