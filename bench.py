@@ -1012,7 +1012,7 @@ def run_ours(args):
         saved = (args.surrogate, args.subset_strides, args.da_inner, args.da_outer, args.delta_limit,
                  args.da_stop_beta, args.subset_inner)
         # 20 first-stage moves and one exact correction per stage: the fastest setting that reaches
-        # the converged posterior in the five-seed sweep (bench.py --mode sweep --sweep-da 20x1)
+        # the converged posterior in the seed sweeps (bench.py --mode sweep --sweep-da 20x1)
         args.surrogate, args.subset_strides, args.da_inner, args.da_outer = "subset", [32, 16, 8], 20, 1
         args.subset_inner = None
         args.delta_limit, args.da_stop_beta = 1.0, 1.0
@@ -1031,9 +1031,10 @@ def run_ours(args):
             "minus_plain_in_sd": ((np.array(da["invariants"]["mean"]) - np.array(full["invariants"]["mean"]))
                                   / np.where(sd > 0, sd, 1)).tolist(),
             "note": "the plain 5-step walk is under-mixed along the opening/semi-axis ridge; at equal "
-                    "posterior (bench.py --mode sweep --sweep-da 20x1: five seeds against a 20-step "
-                    "walk) this sampler is 4.98x faster than the cheapest plain walk that reaches it "
-                    "(15 steps per stage)"}
+                    "posterior (bench.py --mode sweep --sweep-steps 15 20 --sweep-da 20x1: seeds "
+                    "against a 20-step walk) this sampler is 5.09x faster over ten seeds (4.98x and "
+                    "5.22x on two sets of five) than the cheapest plain walk that reaches it (15 steps "
+                    "per stage)"}
     if rank == 0:
         print(json.dumps(line))
     if dist is not None:
