@@ -7,7 +7,6 @@ import torch
 
 from altar_gb300 import Application
 from altar_gb300.bayesian import Annealer
-from altar_gb300.bayesian.coolingstep import CoolingStep
 from altar_gb300.bayesian.sharding import _Block
 from altar_gb300.distributions import Uniform
 from altar_gb300.models import Contiguous, Mogi
