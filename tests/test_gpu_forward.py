@@ -2,8 +2,8 @@
 
 Tolerances (FP32 device arithmetic against FP64 references):
   * CDM LOS displacement, per source, normwise: |u_gpu - u_ref|_inf <= 1e-5 |u_ref|_inf
-    for every source (the benchmark spec's bound), whatever the angle of its sides and its
-    depth.  Rectangles whose sides would cancel (deep relative to their size) are
+    for every source (the accuracy bound of the forward model), whatever the angle of its
+    sides and its depth.  Rectangles whose sides would cancel (deep relative to their size) are
     integrated by quadrature of point tensile dislocations; near shallow vertices each
     station takes the configuration whose legs point away from it; near-vertical sides are
     evaluated from cancellation-free remainders.  Host build of the same arithmetic: 1,300

@@ -108,8 +108,8 @@ def test_every_run_trapped():
 
 def test_sweep_line_with_several_da_settings(monkeypatch, capsys):
     """run_sweep with stand-in runs: the first delayed-acceptance setting is the line's
-    "da", every setting gets its time, verdict and speed-up against the cheapest plain walk
-    that reaches the reference."""
+    "da"; every setting gets its time, whether it reaches the reference posterior, and its
+    speed-up against the cheapest plain walk that reaches it."""
     import argparse
     import json
     import torch
