@@ -341,8 +341,11 @@ class DelayedAcceptance(Metropolis):
         start_beta <= β < stop_beta; the stages after stop_beta walk exactly, which lets
         the final population relax with the exact kernel alone.  The defaults (10 surrogate
         moves and one exact correction per stage, ratio spread up to 2, exact stages from
-        β = 0.1) were the fastest setting measured on the CDM workload whose posterior
-        summaries matched plain Metropolis to within its own run-to-run spread."""
+        β = 0.1) were the fastest setting measured on the CDM workload with the MLP surrogate
+        whose posterior summaries matched plain Metropolis to within its own run-to-run
+        spread.  With the coarse-model surrogate (SubsetSurrogate) the fastest setting that
+        reached the converged posterior on that workload was inner=20, outer=1,
+        delta_limit=1.0, stop_beta=1.0."""
         super().__init__(**kwds)
         self.delta_limit = float(delta_limit)
         # coarse-model surrogates: when no level passes delta_limit for the surrogate-transition
